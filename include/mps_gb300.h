@@ -1,0 +1,216 @@
+/*
+ * mps_gb300.h -- C ABI of the GB300 spectral-Ewald mutual-polarisation solve.
+ *
+ * Every entry point takes caller-owned DEVICE pointers (unless marked "host"),
+ * plain sizes, and the CUDA stream to run on; it returns an int status
+ * (enum mps_status).  No C++ exception crosses this boundary and no entry
+ * point synchronises the device except where an output size is data
+ * dependent (the *_count calls) or a Krylov solve reads its convergence flags.
+ *
+ * Array layouts (all row-major / C order, element type as declared):
+ *   positions   x[n][3]            float64
+ *   moments     m[nvec][n][3]      float64  (nvec independent real vectors;
+ *                                            the Python layer passes the real
+ *                                            and imaginary parts of a complex
+ *                                            array as nvec = 2)
+ *   grids       g[nvec][3][Nz][Ny][Nx] float64, x fastest -- the same linear
+ *                                            node index ix + Nx*iy + Nx*Ny*iz as
+ *                                            the reference's Fortran-ordered grids
+ *   pair lists  int64, directed, p1[k] receives the field of p2[k]
+ *
+ * Reference interfaces are cited as EW/<file>:<lines> for
+ * "CPU - Ewald test/<file>" and CH/<file> for "Capacitance_Hetero/<file>".
+ */
+#ifndef MPS_GB300_H
+#define MPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t (a CUstream). NULL = the legacy default stream. */
+typedef struct CUstream_st *mps_stream_t;
+
+enum mps_status {
+    MPS_OK = 0,
+    MPS_BAD_ARG = 1,          /* ValueError in the reference's Python layer        */
+    MPS_RC_GT_HALF_BOX = 2,   /* EW/capacitance.py:364-365                         */
+    MPS_TABLE_RANGE = 3,      /* EW/ewald.py:999-1007 separation outside the table */
+    MPS_NOT_CONVERGED = 4,    /* GMRES hit maxit (the reference ignores its flag)   */
+    MPS_CUDA_ERR = 5,
+    MPS_CUFFT_ERR = 6,
+    MPS_NO_MEMORY = 7
+};
+
+enum mps_precision {
+    MPS_FP64 = 0,             /* every stage in float64                              */
+    MPS_FP32 = 1              /* float32 matvec (grids, FFT, pair sum), float64 I/O  */
+};
+
+const char *mps_status_string(int status);
+int mps_abi_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Stateless operators (the reference's ewald.py functions, one each)         */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces EW/ewald.py:604-931 real_space_table(r, xi).
+ * r: n separations (no zero).  tables: 6 x (n+1) float64, rows pot_charge,
+ * pot_dip, field_dip_1, field_dip_2, field_dip_force_1, field_dip_force_2,
+ * each with its r = 0 self value in column 0. */
+int mps_real_space_table(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:84-111 cell_list(x, box, rmax).
+ * box: host double[3].  cell: n x 3 int64.  ncell: host int64[3] (output). */
+int mps_cell_list(const double *x, int64_t n, const double *box, double rmax,
+                  int64_t *cell, int64_t *ncell, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:114-199 neighbor_list(cell, Ncell): two calls sharing a
+ * workspace of mps_neighbor_list_workspace() bytes.  _count writes the number of
+ * directed candidate pairs to the host int64 *n_pairs (synchronises); _fill
+ * writes them in the reference's order into p1, p2 (int64, n_pairs each). */
+size_t mps_neighbor_list_workspace(int64_t n, const int64_t *ncell);
+int mps_neighbor_list_count(const int64_t *cell, int64_t n, const int64_t *ncell,
+                            void *workspace, size_t workspace_bytes, int64_t *n_pairs, mps_stream_t stream);
+int mps_neighbor_list_fill(const int64_t *cell, int64_t n, const int64_t *ncell,
+                           void *workspace, size_t workspace_bytes, int64_t *p1, int64_t *p2, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:939-1016 prepare_real_space_pairs(x, box, p1, p2, rc, perp, para, rvals).
+ * _count keeps the candidates with minimum-image distance d < rc and writes their
+ * number to host *n_kept (synchronises); _fill writes p1f, p2f (int64), rhat
+ * (n_kept x 3), A, B (float64) in candidate order.  A separation outside
+ * rvals returns MPS_TABLE_RANGE. */
+size_t mps_real_space_pairs_workspace(int64_t n_cand);
+int mps_real_space_pairs_count(const double *x, int64_t n, const double *box, const int64_t *p1,
+                               const int64_t *p2, int64_t n_cand, double rc, void *workspace,
+                               size_t workspace_bytes, int64_t *n_kept, mps_stream_t stream);
+int mps_real_space_pairs_fill(const double *x, int64_t n, const double *box, const int64_t *p1,
+                              const int64_t *p2, int64_t n_cand, double rc, const double *perp,
+                              const double *para, const double *rvals, int64_t n_tab, void *workspace,
+                              size_t workspace_bytes, int64_t *p1f, int64_t *p2f, double *rhat, double *A,
+                              double *B, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:1019-1072 real_space_fast(m, lambdap, p1, p2, rhat, A, B, self_perp).
+ * m, out: nvec x n x 3.  lambdap: n (the particle permittivity). */
+int mps_real_space_fast(const double *m, int64_t n, int64_t nvec, const double *lambdap, const int64_t *p1,
+                        const int64_t *p2, const double *rhat, const double *A, const double *B,
+                        int64_t n_pairs, double self_perp, double *out, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:205-223 pre_calculations(P, h).  h: host double[3].
+ * offset: P^3 x 3 int64, offsetxyz: P^3 x 3 float64. */
+int mps_pre_calculations(int P, const double *h, int64_t *offset, double *offsetxyz, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:233-296 prepare_grid_kernel(x, Ngrid, h, xi, eta, P, ...).
+ * Ngrid, h, eta: host arrays of 3.  linnode: n x P^3 int64, w_spread and
+ * w_contract: n x P^3 float64. */
+int mps_grid_kernel(const double *x, int64_t n, const int64_t *Ngrid, const double *h, double xi,
+                    const double *eta, int P, int64_t *linnode, double *w_spread, double *w_contract,
+                    mps_stream_t stream);
+
+/* Replaces EW/ewald.py:299-331 spread_fast(m, Ngrid, linnode, w_spread).
+ * grid: nvec x 3 x G, zeroed by the call. */
+int mps_spread_fast(const double *m, int64_t n, int64_t nvec, const int64_t *Ngrid, const int64_t *linnode,
+                    const double *w_spread, int64_t P3, double *grid, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:334-368 contract_fast(Htilde, Ngrid, linnode, w_contract).
+ * grid: nvec x 3 x G; out: nvec x n x 3. */
+int mps_contract_fast(const double *grid, int64_t n, int64_t nvec, const int64_t *Ngrid, const int64_t *linnode,
+                      const double *w_contract, int64_t P3, double *out, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:523-582 precompute_kspace(Ngrid, box, xi, eta).
+ * khat: Nx x Ny x Nz x 3 float64 (real; the reference stores it as complex with
+ * zero imaginary part), Hcoef: Nx x Ny x Nz, both in the reference's fftshift
+ * order and C layout. */
+int mps_precompute_kspace(const int64_t *Ngrid, const double *box, double xi, const double *eta,
+                          double *khat, double *Hcoef, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:585-599 scale_fast(fH, khat, Hcoef).
+ * fH, out: interleaved complex128 arrays Nx x Ny x Nz x 3 (C layout). */
+int mps_scale_fast(const double *fH, const double *khat, const double *Hcoef, int64_t G, double *out,
+                   mps_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* System object: everything that depends on positions only, built once per   */
+/* solve (the real_precomp / grid_precomp / k_precomp tuples of               */
+/* EW/capacitance.py:370-385), plus cuFFT plans and grids.                     */
+/* ------------------------------------------------------------------------- */
+typedef struct mps_system mps_system;
+
+typedef struct mps_system_desc {
+    int64_t n;                /* particles                                         */
+    const double *x;          /* device n x 3                                       */
+    const double *lambdap;    /* device n_diag x n particle permittivities (eps)   */
+    int64_t n_diag;           /* >= 1 permittivity sets (contrast spectrum axis)   */
+    double box[3];
+    double xi;                /* Ewald splitting parameter                          */
+    double rc;                /* real-space cutoff                                  */
+    int64_t Ngrid[3];         /* grid nodes per axis                                */
+    int32_t P;                /* Gaussian support (nodes per axis)                  */
+    double eta[3];            /* spectral splitting; <= 0 derives P (h xi)^2 / pi   */
+    const double *perp;       /* device table, field_dip_1 (I - rr part)            */
+    const double *para;       /* device table, field_dip_2 (rr part)                */
+    const double *rvals;      /* device table separations (rvals[0] = 0)            */
+    int64_t n_tab;
+    double slab_factor;       /* EW/ewald.py:1233-1236 (1.0 in the reference)       */
+    int32_t max_rhs;          /* largest batch of vectors one matvec will take      */
+} mps_system_desc;
+
+/* Builds cell list, filtered CSR pair list with interpolated couplings, grid
+ * geometry, Green's coefficients and FFT plans (EW/capacitance.py:369-385).
+ * Allocates device memory; synchronises once (pair count). */
+int mps_system_create(const mps_system_desc *desc, mps_system **out, mps_stream_t stream);
+void mps_system_destroy(mps_system *sys);
+
+/* n_pairs kept (d < rc), cell counts per axis. Host outputs. */
+int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t *ncell);
+
+/* Replaces EW/ewald.py:1146-1236 magnetic_field for nrhs real vectors.
+ * m, out: nrhs x n x 3 float64.  diag_index: host int32[nrhs] selecting the
+ * permittivity set of each vector (NULL = set 0).  precision: enum mps_precision.
+ * The wave-space part is the real part of the reference's complex pipeline
+ * (real-to-complex FFTs; the unpaired Nyquist bins of even axes are coupled
+ * symmetrically). */
+int mps_matvec(mps_system *sys, const double *m, double *out, int32_t nrhs, const int32_t *diag_index,
+               int32_t precision, mps_stream_t stream);
+
+/* Replaces EW/ewald.py:1146-1236 magnetic_field with the reference's complex
+ * FFT pipeline, for one complex vector given as m_ri = [Re m; Im m]
+ * (2 x n x 3), out_ri the same. */
+int mps_matvec_complex(mps_system *sys, const double *m_ri, double *out_ri, int32_t diag_index,
+                       mps_stream_t stream);
+
+typedef struct mps_solve_opts {
+    double tol;               /* relative residual target ||b - A x|| / ||b||        */
+    int32_t restart;          /* inner GMRES steps per cycle                          */
+    int32_t maxit;            /* restart cycles (fp64) / refinement steps (mixed)     */
+    int32_t precision;        /* MPS_FP64: GMRES on the fp64 operator.
+                                 MPS_FP32: iterative refinement, fp64 residuals,
+                                 inner GMRES on the fp32 operator                    */
+    double inner_tol;         /* mixed: relative tolerance of each inner solve        */
+    int32_t inner_maxit;      /* mixed: restart cycles of each inner solve            */
+} mps_solve_opts;
+
+typedef struct mps_solve_info {
+    int32_t converged;        /* 1 if relres <= tol                                   */
+    int32_t matvecs_fp64;
+    int32_t matvecs_fp32;
+    int32_t cycles;           /* restart cycles (fp64) or refinement steps (mixed)   */
+    double relres;            /* final true relative residual (fp64 operator)        */
+} mps_solve_info;
+
+/* Replaces EW/capacitance.py:205-321 magnetic_dipole (GMRES on A m = b) for
+ * nrhs right-hand sides solved together (batched matvecs, independent Krylov
+ * spaces).  b, x0, x: nrhs x n x 3 float64; x0 may alias x or be NULL (zero).
+ * info: host array of nrhs.  Returns MPS_NOT_CONVERGED if any system missed tol. */
+int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
+              const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
+              mps_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPS_GB300_H */

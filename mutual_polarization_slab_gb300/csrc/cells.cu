@@ -1,0 +1,539 @@
+// K1/K2: cell binning by counting sort, candidate neighbour lists and the
+// cutoff-filtered pair lists (EW/ewald.py:84-199, 939-1016).
+//
+// Integer outputs are bit-exact with the reference: the cell coordinate uses
+// the same float64 operations (numpy mod, divide, multiply, floor) and the pair
+// order reproduces the reference's emission order (occupied cells by linear
+// index, 27 neighbour cells with the x offset outermost, home particle, then
+// neighbour particle, both by increasing id).  Floating-point pair data use
+// explicitly rounded operations (no FMA contraction) so they match numpy's.
+#include "cells.cuh"
+
+namespace mps {
+
+__constant__ int c_off27[27][3];
+
+static bool g_off_ready = false;
+
+static int ensure_offsets() {
+    if (g_off_ready) return MPS_OK;
+    int h[27][3];
+    int k = 0;
+    for (int a = -1; a <= 1; ++a)
+        for (int b = -1; b <= 1; ++b)
+            for (int c = -1; c <= 1; ++c) {
+                h[k][0] = a;
+                h[k][1] = b;
+                h[k][2] = c;
+                ++k;
+            }
+    MPS_CUDA_TRY(cudaMemcpyToSymbol(c_off27, h, sizeof(h)));
+    g_off_ready = true;
+    return MPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+__global__ void k_cell_assign(const double *__restrict__ x, int64_t n, double Lx, double Ly, double Lz,
+                              int64_t ncx, int64_t ncy, int64_t ncz, int64_t *__restrict__ cell3) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double L[3] = {Lx, Ly, Lz};
+        const int64_t nc[3] = {ncx, ncy, ncz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double w = np_mod(x[3 * i + d], L[d]);
+            double f = floor(__dmul_rn(__ddiv_rn(w, L[d]), (double)nc[d]));
+            cell3[3 * i + d] = (int64_t)f;
+        }
+    }
+}
+
+__global__ void k_cell_lin(const int64_t *__restrict__ cell3, int64_t n, int64_t ncx, int64_t ncy, int64_t ncz,
+                           int32_t *__restrict__ lin, int32_t *__restrict__ counts) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        // clamp: a coordinate rounding up to exactly L lands in the last cell
+        int64_t cx = min(max(cell3[3 * i + 0], (int64_t)0), ncx - 1);
+        int64_t cy = min(max(cell3[3 * i + 1], (int64_t)0), ncy - 1);
+        int64_t cz = min(max(cell3[3 * i + 2], (int64_t)0), ncz - 1);
+        int32_t c = (int32_t)(cx + ncx * (cy + ncy * cz));
+        lin[i] = c;
+        atomicAdd(&counts[c], 1);
+    }
+}
+
+__global__ void k_cell_scatter(const int32_t *__restrict__ lin, int64_t n, const int64_t *__restrict__ starts,
+                               int32_t *__restrict__ cursor, int32_t *__restrict__ unsorted) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t c = lin[i];
+        int64_t p = starts[c] + atomicAdd(&cursor[c], 1);
+        unsorted[p] = (int32_t)i;
+    }
+}
+
+// One warp per cell: rank each member by id (ids are unique) -> stable order.
+__global__ void k_cell_rank(const int32_t *__restrict__ unsorted, const int32_t *__restrict__ counts,
+                            const int64_t *__restrict__ starts, int64_t ncells, int32_t *__restrict__ sorted) {
+    const int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < ncells; c += nwarps) {
+        int32_t len = counts[c];
+        int64_t s0 = starts[c];
+        for (int32_t e = lane; e < len; e += 32) {
+            int32_t v = unsorted[s0 + e];
+            int32_t rank = 0;
+            for (int32_t j = 0; j < len; ++j) rank += (unsorted[s0 + j] < v);
+            sorted[s0 + rank] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ int32_t nb_cell(int32_t c, int o, int64_t ncx, int64_t ncy, int64_t ncz) {
+    int64_t cx = c % ncx, cy = (c / ncx) % ncy, cz = c / (ncx * ncy);
+    cx = wrap_index(cx + c_off27[o][0], ncx);
+    cy = wrap_index(cy + c_off27[o][1], ncy);
+    cz = wrap_index(cz + c_off27[o][2], ncz);
+    return (int32_t)(cx + ncx * (cy + ncy * cz));
+}
+
+// Candidate counts in emission-slot order: slot(s,o) = 27*start[c] + o*count[c] + (s - start[c]).
+__global__ void k_candidate_slots(const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                                  const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
+                                  int64_t ncx, int64_t ncy, int64_t ncz, int64_t *__restrict__ slot_count) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / 27;
+        int o = (int)(t % 27);
+        int32_t a = sorted[s];
+        int32_t c = lin[a];
+        int32_t nb = nb_cell(c, o, ncx, ncy, ncz);
+        int64_t cnt = counts[nb] - (nb == c ? 1 : 0);
+        int64_t slot = 27 * starts[c] + (int64_t)o * counts[c] + (s - starts[c]);
+        slot_count[slot] = cnt;
+    }
+}
+
+__global__ void k_candidate_fill(const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                                 const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
+                                 int64_t ncx, int64_t ncy, int64_t ncz, const int64_t *__restrict__ slot_off,
+                                 int64_t *__restrict__ p1, int64_t *__restrict__ p2) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / 27;
+        int o = (int)(t % 27);
+        int32_t a = sorted[s];
+        int32_t c = lin[a];
+        int32_t nb = nb_cell(c, o, ncx, ncy, ncz);
+        int64_t slot = 27 * starts[c] + (int64_t)o * counts[c] + (s - starts[c]);
+        int64_t w = slot_off[slot];
+        int64_t b0 = starts[nb], len = counts[nb];
+        for (int64_t j = 0; j < len; ++j) {
+            int32_t b = sorted[b0 + j];
+            if (b == a) continue;
+            p1[w] = a;
+            p2[w] = b;
+            ++w;
+        }
+    }
+}
+
+// Minimum-image separation exactly as numpy evaluates r - L*trunc(2r/L) and
+// sqrt(sum(r*r)) (left-to-right over x, y, z).
+__device__ __forceinline__ double min_image_sep(const double *__restrict__ x, int64_t a, int64_t b, const double *L,
+                                                double r[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double v = __dsub_rn(x[3 * a + d], x[3 * b + d]);
+        double t = trunc(__ddiv_rn(__dmul_rn(2.0, v), L[d]));
+        r[d] = __dsub_rn(v, __dmul_rn(L[d], t));
+    }
+    double s = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+    return __dsqrt_rn(s);
+}
+
+// First index i with rv[i] >= d (numpy searchsorted side='left').
+__device__ __forceinline__ int64_t search_left(const double *__restrict__ rv, int64_t n, double d) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (rv[mid] < d)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Interpolated couplings at separation d; returns false when d is outside the table.
+__device__ __forceinline__ bool table_lerp(const double *__restrict__ perp, const double *__restrict__ para,
+                                           const double *__restrict__ rv, int64_t ntab, double d, double *A,
+                                           double *B) {
+    int64_t i = search_left(rv, ntab, d);
+    if (i <= 0 || i >= ntab) return false;
+    double rl = rv[i - 1], rh = rv[i];
+    double t = __ddiv_rn(__dsub_rn(d, rl), __dsub_rn(rh, rl));
+    double omt = __dsub_rn(1.0, t);
+    *A = __dadd_rn(__dmul_rn(perp[i - 1], omt), __dmul_rn(perp[i], t));
+    *B = __dadd_rn(__dmul_rn(para[i - 1], omt), __dmul_rn(para[i], t));
+    return true;
+}
+
+__global__ void k_pair_flag(const double *__restrict__ x, double Lx, double Ly, double Lz,
+                            const int64_t *__restrict__ p1, const int64_t *__restrict__ p2, int64_t ncand, double rc,
+                            int32_t *__restrict__ flag) {
+    const double L[3] = {Lx, Ly, Lz};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ncand; k += (int64_t)gridDim.x * blockDim.x) {
+        double r[3];
+        double d = min_image_sep(x, p1[k], p2[k], L, r);
+        flag[k] = d < rc ? 1 : 0;
+    }
+}
+
+__global__ void k_pair_fill(const double *__restrict__ x, double Lx, double Ly, double Lz,
+                            const int64_t *__restrict__ p1, const int64_t *__restrict__ p2, int64_t ncand,
+                            const int32_t *__restrict__ flag, const int64_t *__restrict__ off,
+                            const double *__restrict__ perp, const double *__restrict__ para,
+                            const double *__restrict__ rv, int64_t ntab, int64_t *__restrict__ p1f,
+                            int64_t *__restrict__ p2f, double *__restrict__ rhat, double *__restrict__ A,
+                            double *__restrict__ B, int *__restrict__ err) {
+    const double L[3] = {Lx, Ly, Lz};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ncand; k += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[k]) continue;
+        double r[3];
+        int64_t a = p1[k], b = p2[k];
+        double d = min_image_sep(x, a, b, L, r);
+        int64_t w = off[k];
+        p1f[w] = a;
+        p2f[w] = b;
+        rhat[3 * w + 0] = __ddiv_rn(r[0], d);
+        rhat[3 * w + 1] = __ddiv_rn(r[1], d);
+        rhat[3 * w + 2] = __ddiv_rn(r[2], d);
+        double av = 0.0, bv = 0.0;
+        if (!table_lerp(perp, para, rv, ntab, d, &av, &bv)) atomicExch(err, 1);
+        A[w] = av;
+        B[w] = bv;
+    }
+}
+
+// Filtered per-particle neighbour counts, slot (a, o) at a*27 + o.
+__global__ void k_csr_count(const double *__restrict__ x, double Lx, double Ly, double Lz,
+                            const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                            const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
+                            int64_t ncx, int64_t ncy, int64_t ncz, double rc, int64_t *__restrict__ cnt27) {
+    const double L[3] = {Lx, Ly, Lz};
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / 27;
+        int o = (int)(t % 27);
+        int32_t a = sorted[s];
+        int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
+        int64_t b0 = starts[nb], len = counts[nb];
+        int64_t cnt = 0;
+        for (int64_t j = 0; j < len; ++j) {
+            int32_t b = sorted[b0 + j];
+            if (b == a) continue;
+            double r[3];
+            cnt += min_image_sep(x, a, b, L, r) < rc;
+        }
+        cnt27[(int64_t)a * 27 + o] = cnt;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_pair(PairData<T> &pd, int64_t w, int32_t b, double A, double B,
+                                           const double rh[3]) {
+    pd.nbr[w] = b;
+    pd.A[w] = (T)A;
+    pd.BA[w] = (T)(B - A);
+    pd.rx[w] = (T)rh[0];
+    pd.ry[w] = (T)rh[1];
+    pd.rz[w] = (T)rh[2];
+}
+
+__global__ void k_csr_fill(const double *__restrict__ x, double Lx, double Ly, double Lz,
+                           const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                           const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
+                           int64_t ncx, int64_t ncy, int64_t ncz, double rc, const int64_t *__restrict__ off27,
+                           const double *__restrict__ perp, const double *__restrict__ para,
+                           const double *__restrict__ rv, int64_t ntab, PairData<double> p64, PairData<float> p32,
+                           int *__restrict__ err) {
+    const double L[3] = {Lx, Ly, Lz};
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / 27;
+        int o = (int)(t % 27);
+        int32_t a = sorted[s];
+        int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
+        int64_t b0 = starts[nb], len = counts[nb];
+        int64_t w = off27[(int64_t)a * 27 + o];
+        for (int64_t j = 0; j < len; ++j) {
+            int32_t b = sorted[b0 + j];
+            if (b == a) continue;
+            double r[3];
+            double d = min_image_sep(x, a, b, L, r);
+            if (!(d < rc)) continue;
+            double rh[3] = {__ddiv_rn(r[0], d), __ddiv_rn(r[1], d), __ddiv_rn(r[2], d)};
+            double A = 0.0, B = 0.0;
+            if (!table_lerp(perp, para, rv, ntab, d, &A, &B)) atomicExch(err, 1);
+            store_pair(p64, w, b, A, B, rh);
+            store_pair(p32, w, b, A, B, rh);
+            ++w;
+        }
+    }
+}
+
+__global__ void k_row_ptr(const int64_t *__restrict__ off27, const int64_t *__restrict__ cnt27, int64_t n,
+                          int64_t *__restrict__ row_ptr) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a <= n; a += (int64_t)gridDim.x * blockDim.x) {
+        row_ptr[a] = a < n ? off27[a * 27] : off27[n * 27 - 1] + cnt27[n * 27 - 1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+void compute_ncell(const double *box, double rmax, int64_t *ncell) {
+    for (int d = 0; d < 3; ++d) {
+        int64_t v = (int64_t)floor(box[d] / rmax);
+        ncell[d] = v < 3 ? 3 : v;
+    }
+}
+
+size_t cell_bins_bytes(int64_t n, int64_t ncells) {
+    size_t b = 0;
+    b += 256 + (size_t)n * 4;         // lin
+    b += 256 + (size_t)ncells * 4;    // counts
+    b += 256 + (size_t)ncells * 8;    // starts
+    b += 256 + (size_t)ncells * 4;    // cursor
+    b += 256 + (size_t)n * 4;         // sorted
+    b += 256 + (size_t)n * 4;         // unsorted
+    b += 256 + scan_workspace(ncells);
+    return b;
+}
+
+static void *carve(char *&p, size_t bytes) {
+    uintptr_t u = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+    p = (char *)(u + bytes);
+    return (void *)u;
+}
+
+int cell_bins_build(const int64_t *cell3, int64_t n, const int64_t *ncell, void *ws, CellBins &cb, cudaStream_t s) {
+    int rc = ensure_offsets();
+    if (rc) return rc;
+    int64_t ncells = ncell[0] * ncell[1] * ncell[2];
+    char *p = (char *)ws;
+    cb.ncell[0] = ncell[0];
+    cb.ncell[1] = ncell[1];
+    cb.ncell[2] = ncell[2];
+    cb.ncells = ncells;
+    cb.n = n;
+    cb.lin = (int32_t *)carve(p, (size_t)n * 4);
+    cb.counts = (int32_t *)carve(p, (size_t)ncells * 4);
+    cb.starts = (int64_t *)carve(p, (size_t)ncells * 8);
+    cb.cursor = (int32_t *)carve(p, (size_t)ncells * 4);
+    cb.sorted = (int32_t *)carve(p, (size_t)n * 4);
+    cb.unsorted = (int32_t *)carve(p, (size_t)n * 4);
+    void *scan_tmp = carve(p, scan_workspace(ncells));
+    if (n == 0) return MPS_OK;
+    MPS_CUDA_TRY(cudaMemsetAsync(cb.counts, 0, (size_t)ncells * 4, s));
+    MPS_CUDA_TRY(cudaMemsetAsync(cb.cursor, 0, (size_t)ncells * 4, s));
+    k_cell_lin<<<grid_for(n, 256), 256, 0, s>>>(cell3, n, ncell[0], ncell[1], ncell[2], cb.lin, cb.counts);
+    MPS_LAUNCH_CHECK();
+    rc = exclusive_scan_i32_to_i64(cb.counts, cb.starts, ncells, scan_tmp, s);
+    if (rc) return rc;
+    k_cell_scatter<<<grid_for(n, 256), 256, 0, s>>>(cb.lin, n, cb.starts, cb.cursor, cb.unsorted);
+    MPS_LAUNCH_CHECK();
+    k_cell_rank<<<grid_for(ncells * 32, 256), 256, 0, s>>>(cb.unsorted, cb.counts, cb.starts, ncells, cb.sorted);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int cell_assign(const double *x, int64_t n, const double *box, const int64_t *ncell, int64_t *cell3, cudaStream_t s) {
+    if (n == 0) return MPS_OK;
+    k_cell_assign<<<grid_for(n, 256), 256, 0, s>>>(x, n, box[0], box[1], box[2], ncell[0], ncell[1], ncell[2], cell3);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int csr_pairs_count(const double *x, const double *box, double rc, const CellBins &cb, int64_t *cnt27, int64_t *off27,
+                    void *scan_tmp, int64_t *total_host, cudaStream_t s) {
+    int64_t n = cb.n;
+    k_csr_count<<<grid_for(27 * n, 256), 256, 0, s>>>(x, box[0], box[1], box[2], cb.sorted, cb.lin, cb.counts,
+                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], rc, cnt27);
+    MPS_LAUNCH_CHECK();
+    int r = exclusive_scan_i64(cnt27, off27, 27 * n, scan_tmp, s);
+    if (r) return r;
+    int64_t last[2];
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last[0], off27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last[1], cnt27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    *total_host = last[0] + last[1];
+    return MPS_OK;
+}
+
+int csr_pairs_fill(const double *x, const double *box, double rc, const CellBins &cb, const int64_t *cnt27,
+                   const int64_t *off27, const double *perp, const double *para, const double *rv, int64_t ntab,
+                   int64_t *row_ptr, PairData<double> p64, PairData<float> p32, int *err, cudaStream_t s) {
+    int64_t n = cb.n;
+    k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
+    MPS_LAUNCH_CHECK();
+    k_csr_fill<<<grid_for(27 * n, 256), 256, 0, s>>>(x, box[0], box[1], box[2], cb.sorted, cb.lin, cb.counts,
+                                                     cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], rc, off27,
+                                                     perp, para, rv, ntab, p64, p32, err);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+}  // namespace mps
+
+using namespace mps;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int mps_cell_list(const double *x, int64_t n, const double *box, double rmax, int64_t *cell,
+                             int64_t *ncell, mps_stream_t stream) {
+    if (n < 0 || !box || !ncell || !(rmax > 0) || (n > 0 && (!x || !cell))) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (!(box[d] > 0)) return MPS_BAD_ARG;
+    compute_ncell(box, rmax, ncell);
+    return cell_assign(x, n, box, ncell, cell, (cudaStream_t)stream);
+}
+
+static size_t nl_layout(int64_t n, const int64_t *ncell, size_t *bins_bytes) {
+    int64_t ncells = ncell[0] * ncell[1] * ncell[2];
+    size_t b = cell_bins_bytes(n, ncells);
+    *bins_bytes = b;
+    b += 256 + (size_t)27 * n * 8;         // slot counts
+    b += 256 + (size_t)27 * n * 8;         // slot offsets
+    b += 256 + scan_workspace(27 * n);
+    return b;
+}
+
+extern "C" size_t mps_neighbor_list_workspace(int64_t n, const int64_t *ncell) {
+    size_t bb;
+    return nl_layout(n, ncell, &bb) + 256;
+}
+
+static int nl_common(const int64_t *cell, int64_t n, const int64_t *ncell, void *ws, size_t ws_bytes, CellBins &cb,
+                     int64_t *&slot_cnt, int64_t *&slot_off, void *&scan_tmp, cudaStream_t s) {
+    if (n < 0 || !ncell || !ws) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (ncell[d] < 1) return MPS_BAD_ARG;
+    size_t bb;
+    if (ws_bytes < nl_layout(n, ncell, &bb)) return MPS_BAD_ARG;
+    int r = cell_bins_build(cell, n, ncell, ws, cb, s);
+    if (r) return r;
+    char *p = (char *)ws + bb;
+    slot_cnt = (int64_t *)carve(p, (size_t)27 * n * 8);
+    slot_off = (int64_t *)carve(p, (size_t)27 * n * 8);
+    scan_tmp = carve(p, scan_workspace(27 * n));
+    return MPS_OK;
+}
+
+extern "C" int mps_neighbor_list_count(const int64_t *cell, int64_t n, const int64_t *ncell, void *workspace,
+                                       size_t workspace_bytes, int64_t *n_pairs, mps_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!n_pairs) return MPS_BAD_ARG;
+    *n_pairs = 0;
+    if (n == 0) return MPS_OK;
+    CellBins cb;
+    int64_t *sc, *so;
+    void *st;
+    int r = nl_common(cell, n, ncell, workspace, workspace_bytes, cb, sc, so, st, s);
+    if (r) return r;
+    k_candidate_slots<<<grid_for(27 * n, 256), 256, 0, s>>>(cb.sorted, cb.lin, cb.counts, cb.starts, n, ncell[0],
+                                                            ncell[1], ncell[2], sc);
+    MPS_LAUNCH_CHECK();
+    r = exclusive_scan_i64(sc, so, 27 * n, st, s);
+    if (r) return r;
+    int64_t last[2];
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last[0], so + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last[1], sc + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    *n_pairs = last[0] + last[1];
+    return MPS_OK;
+}
+
+extern "C" int mps_neighbor_list_fill(const int64_t *cell, int64_t n, const int64_t *ncell, void *workspace,
+                                      size_t workspace_bytes, int64_t *p1, int64_t *p2, mps_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n == 0) return MPS_OK;
+    CellBins cb;
+    int64_t *sc, *so;
+    void *st;
+    int r = nl_common(cell, n, ncell, workspace, workspace_bytes, cb, sc, so, st, s);
+    if (r) return r;
+    k_candidate_slots<<<grid_for(27 * n, 256), 256, 0, s>>>(cb.sorted, cb.lin, cb.counts, cb.starts, n, ncell[0],
+                                                            ncell[1], ncell[2], sc);
+    MPS_LAUNCH_CHECK();
+    r = exclusive_scan_i64(sc, so, 27 * n, st, s);
+    if (r) return r;
+    k_candidate_fill<<<grid_for(27 * n, 256), 256, 0, s>>>(cb.sorted, cb.lin, cb.counts, cb.starts, n, ncell[0],
+                                                           ncell[1], ncell[2], so, p1, p2);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+extern "C" size_t mps_real_space_pairs_workspace(int64_t n_cand) {
+    return 256 * 4 + (size_t)n_cand * 4 + (size_t)n_cand * 8 + scan_workspace(n_cand) + 16;
+}
+
+static int pairs_layout(int64_t n_cand, void *ws, size_t ws_bytes, int32_t *&flag, int64_t *&off, void *&tmp,
+                        int *&err) {
+    if (ws_bytes < mps_real_space_pairs_workspace(n_cand) || !ws) return MPS_BAD_ARG;
+    char *p = (char *)ws;
+    flag = (int32_t *)carve(p, (size_t)n_cand * 4);
+    off = (int64_t *)carve(p, (size_t)n_cand * 8);
+    err = (int *)carve(p, 16);
+    tmp = carve(p, scan_workspace(n_cand));
+    return MPS_OK;
+}
+
+extern "C" int mps_real_space_pairs_count(const double *x, int64_t n, const double *box, const int64_t *p1,
+                                          const int64_t *p2, int64_t n_cand, double rc, void *workspace,
+                                          size_t workspace_bytes, int64_t *n_kept, mps_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!n_kept || !box || n_cand < 0) return MPS_BAD_ARG;
+    *n_kept = 0;
+    if (n_cand == 0) return MPS_OK;
+    int32_t *flag;
+    int64_t *off;
+    void *tmp;
+    int *err;
+    int r = pairs_layout(n_cand, workspace, workspace_bytes, flag, off, tmp, err);
+    if (r) return r;
+    k_pair_flag<<<grid_for(n_cand, 256), 256, 0, s>>>(x, box[0], box[1], box[2], p1, p2, n_cand, rc, flag);
+    MPS_LAUNCH_CHECK();
+    r = exclusive_scan_i32_to_i64(flag, off, n_cand, tmp, s);
+    if (r) return r;
+    int64_t lo;
+    int32_t lf;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&lo, off + n_cand - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&lf, flag + n_cand - 1, 4, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    *n_kept = lo + lf;
+    return MPS_OK;
+}
+
+extern "C" int mps_real_space_pairs_fill(const double *x, int64_t n, const double *box, const int64_t *p1,
+                                         const int64_t *p2, int64_t n_cand, double rc, const double *perp,
+                                         const double *para, const double *rvals, int64_t n_tab, void *workspace,
+                                         size_t workspace_bytes, int64_t *p1f, int64_t *p2f, double *rhat, double *A,
+                                         double *B, mps_stream_t stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_cand == 0) return MPS_OK;
+    if (!box || n_tab < 2) return MPS_BAD_ARG;
+    int32_t *flag;
+    int64_t *off;
+    void *tmp;
+    int *err;
+    int r = pairs_layout(n_cand, workspace, workspace_bytes, flag, off, tmp, err);
+    if (r) return r;
+    // flags and offsets were produced by _count on the same workspace
+    MPS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    k_pair_fill<<<grid_for(n_cand, 256), 256, 0, s>>>(x, box[0], box[1], box[2], p1, p2, n_cand, flag, off, perp,
+                                                      para, rvals, n_tab, p1f, p2f, rhat, A, B, err);
+    MPS_LAUNCH_CHECK();
+    int herr = 0;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    return herr ? MPS_TABLE_RANGE : MPS_OK;
+}

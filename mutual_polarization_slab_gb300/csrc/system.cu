@@ -1,0 +1,939 @@
+// System object (precomputed geometry + FFT plans), the batched matvec, and the
+// GMRES / mixed-precision iterative-refinement solvers
+// (EW/ewald.py:1146-1236, EW/capacitance.py:60-321).
+#include <cufft.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "grid.cuh"
+#include "realspace.cuh"
+
+using namespace mps;
+
+// cuFFT plans are cached per process, keyed by (type, grid, batch), so building a
+// new system for a new configuration of the same grid creates no plan.  Each
+// system owns its work area; the (work area, stream, exec) sequence is issued
+// under one mutex.
+struct PlanKey {
+    int type, nx, ny, nz, batch;
+    bool operator<(const PlanKey &o) const {
+        if (type != o.type) return type < o.type;
+        if (nx != o.nx) return nx < o.nx;
+        if (ny != o.ny) return ny < o.ny;
+        if (nz != o.nz) return nz < o.nz;
+        return batch < o.batch;
+    }
+};
+struct CachedPlan {
+    cufftHandle h;
+    size_t work;
+};
+static std::map<PlanKey, CachedPlan> g_plans;
+static std::mutex g_plan_mu;
+
+// Per-stage timing of the matvec (diagnostics): slab, spread, forward FFT,
+// scale, inverse FFT, contract, real space.
+constexpr int kStages = 7;
+struct StageEvents {
+    cudaEvent_t ev[kStages + 1];
+    int precision;
+};
+
+struct mps_system {
+    int64_t n = 0;
+    int max_rhs = 1;
+    int64_t n_diag = 1;
+    double box[3];
+    double xi, rc, slab_factor;
+    GridParams gp;
+    int64_t Gc = 0;
+    double *x = nullptr;
+    double *diag = nullptr;     // n_diag x n : dielectric + self
+    int64_t ncell[3];
+    int64_t n_pairs = 0;
+    int64_t *row_ptr = nullptr;
+    PairData<double> p64{};
+    PairData<float> p32{};
+    int32_t *start = nullptr;
+    double *w64 = nullptr;
+    float *w32 = nullptr;
+    double *h64 = nullptr;
+    float *h32 = nullptr;
+    double *grid64 = nullptr;
+    void *spec64 = nullptr;
+    float *grid32 = nullptr;
+    void *spec32 = nullptr;
+    void *cgrid = nullptr;      // complex (drop-in) pipeline, 3 x G double2
+    double *rgrid2 = nullptr;   // 2 x 3 x G
+    double *slab = nullptr;     // max_rhs
+    int32_t *diag_idx = nullptr;  // max_rhs (device)
+    int32_t *diag_idx_host = nullptr;  // pinned mirror
+    void *fft_work = nullptr;
+    size_t fft_work_bytes = 0;
+    bool profile = false;
+    std::vector<StageEvents> pending;
+    std::vector<StageEvents> spare;
+    double stage_ms[2][kStages] = {{0}};
+    int64_t stage_count[2] = {0, 0};
+};
+
+static void free_system(mps_system *s) {
+    if (!s) return;
+    for (auto &e : s->pending)
+        for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
+    for (auto &e : s->spare)
+        for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
+    void *ptrs[] = {s->x, s->diag, s->row_ptr, s->p64.nbr, s->p64.A, s->p64.BA, s->p64.rx, s->p64.ry, s->p64.rz,
+                    s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32, s->h64, s->h32,
+                    s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
+                    s->fft_work};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
+    delete s;
+}
+
+template <typename P>
+static int dalloc(P **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return e == cudaErrorMemoryAllocation ? MPS_NO_MEMORY : MPS_CUDA_ERR;
+    }
+    return MPS_OK;
+}
+
+#define MPS_TRY(expr)           \
+    do {                        \
+        int _r = (expr);        \
+        if (_r != MPS_OK) return _r; \
+    } while (0)
+
+#define CUFFT_TRY(expr)                              \
+    do {                                             \
+        if ((expr) != CUFFT_SUCCESS) return MPS_CUFFT_ERR; \
+    } while (0)
+
+static int get_plan(cufftType type, const GridParams &gp, int batch, CachedPlan *out) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    PlanKey key{(int)type, gp.N[0], gp.N[1], gp.N[2], batch};
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) {
+        *out = it->second;
+        return MPS_OK;
+    }
+    cufftHandle h;
+    CUFFT_TRY(cufftCreate(&h));
+    if (cufftSetAutoAllocation(h, 0) != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return MPS_CUFFT_ERR;
+    }
+    int n[3] = {gp.N[2], gp.N[1], gp.N[0]};
+    size_t ws = 0;
+    if (cufftMakePlanMany(h, 3, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, &ws) != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        return MPS_CUFFT_ERR;
+    }
+    CachedPlan cp{h, ws};
+    g_plans[key] = cp;
+    *out = cp;
+    return MPS_OK;
+}
+
+static int ensure_work(mps_system *s, size_t need) {
+    if (need <= s->fft_work_bytes) return MPS_OK;
+    if (s->fft_work) {
+        MPS_CUDA_TRY(cudaDeviceSynchronize());
+        cudaFree(s->fft_work);
+    }
+    s->fft_work = nullptr;
+    s->fft_work_bytes = 0;
+    MPS_TRY(dalloc(&s->fft_work, need));
+    s->fft_work_bytes = need;
+    return MPS_OK;
+}
+
+// Runs one cached plan on this system's work area and stream.
+static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *out, int dir, cudaStream_t st) {
+    CachedPlan cp;
+    MPS_TRY(get_plan(type, s->gp, batch, &cp));
+    MPS_TRY(ensure_work(s, cp.work));
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    CUFFT_TRY(cufftSetWorkArea(cp.h, s->fft_work));
+    CUFFT_TRY(cufftSetStream(cp.h, st));
+    switch (type) {
+        case CUFFT_D2Z: CUFFT_TRY(cufftExecD2Z(cp.h, (cufftDoubleReal *)in, (cufftDoubleComplex *)out)); break;
+        case CUFFT_Z2D: CUFFT_TRY(cufftExecZ2D(cp.h, (cufftDoubleComplex *)in, (cufftDoubleReal *)out)); break;
+        case CUFFT_R2C: CUFFT_TRY(cufftExecR2C(cp.h, (cufftReal *)in, (cufftComplex *)out)); break;
+        case CUFFT_C2R: CUFFT_TRY(cufftExecC2R(cp.h, (cufftComplex *)in, (cufftReal *)out)); break;
+        case CUFFT_Z2Z:
+            CUFFT_TRY(cufftExecZ2Z(cp.h, (cufftDoubleComplex *)in, (cufftDoubleComplex *)out, dir));
+            break;
+        default: return MPS_BAD_ARG;
+    }
+    return MPS_OK;
+}
+
+static int ensure_grids(mps_system *s, int precision) {
+    size_t nr = (size_t)s->max_rhs * 3;
+    if (precision == MPS_FP64) {
+        if (!s->grid64) MPS_TRY(dalloc(&s->grid64, nr * s->gp.G * sizeof(double)));
+        if (!s->spec64) MPS_TRY(dalloc(&s->spec64, nr * s->Gc * 2 * sizeof(double)));
+    } else {
+        if (!s->grid32) MPS_TRY(dalloc(&s->grid32, nr * s->gp.G * sizeof(float)));
+        if (!s->spec32) MPS_TRY(dalloc(&s->spec32, nr * s->Gc * 2 * sizeof(float)));
+    }
+    return MPS_OK;
+}
+
+static int upload_diag_idx(mps_system *s, const int32_t *diag_index, int nrhs, cudaStream_t st) {
+    // stage through pinned memory so the async copy does not read caller memory late
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int r = 0; r < nrhs; ++r) {
+        int32_t v = diag_index ? diag_index[r] : 0;
+        if (v < 0 || v >= s->n_diag) return MPS_BAD_ARG;
+        s->diag_idx_host[r] = v;
+    }
+    MPS_CUDA_TRY(cudaMemcpyAsync(s->diag_idx, s->diag_idx_host, sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+    return MPS_OK;
+}
+
+static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStream_t st) {
+    *ev = nullptr;
+    if (!s->profile) return MPS_OK;
+    StageEvents e;
+    if (!s->spare.empty()) {
+        e = s->spare.back();
+        s->spare.pop_back();
+    } else {
+        for (int k = 0; k <= kStages; ++k) MPS_CUDA_TRY(cudaEventCreate(&e.ev[k]));
+    }
+    e.precision = precision;
+    s->pending.push_back(e);
+    *ev = &s->pending.back();
+    MPS_CUDA_TRY(cudaEventRecord((*ev)->ev[0], st));
+    return MPS_OK;
+}
+
+#define STAGE_MARK(k)                                                   \
+    do {                                                                \
+        if (ev) MPS_CUDA_TRY(cudaEventRecord(ev->ev[(k)], st));         \
+    } while (0)
+
+template <typename T>
+static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    const bool dbl = sizeof(T) == 8;
+    MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32));
+    T *grid = dbl ? (T *)s->grid64 : (T *)s->grid32;
+    void *spec = dbl ? s->spec64 : s->spec32;
+    const T *w = dbl ? (const T *)s->w64 : (const T *)s->w32;
+    const T *hh = dbl ? (const T *)s->h64 : (const T *)s->h32;
+    const double vol = s->box[0] * s->box[1] * s->box[2];
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
+    MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    STAGE_MARK(1);
+    MPS_TRY(spread<T>(m, s->n, nrhs, s->start, w, s->gp, grid, st));
+    STAGE_MARK(2);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, 3 * nrhs, grid, spec, 0, st));
+    STAGE_MARK(3);
+    MPS_TRY(scale_half<T>(spec, nrhs, s->gp, hh, st));
+    STAGE_MARK(4);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 3 * nrhs, spec, grid, 0, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract<T>(grid, s->n, nrhs, s->start, w, s->gp, out, st));
+    STAGE_MARK(6);
+    if (dbl)
+        MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
+    else
+        MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
+static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+    return precision == MPS_FP64 ? matvec_impl<double>(s, m, out, nrhs, st) : matvec_impl<float>(s, m, out, nrhs, st);
+}
+
+// ---------------------------------------------------------------------------
+// Krylov kernels (float64).  Vectors of length n3 = 3n; nrhs independent
+// systems stacked with stride n3 (vectors) / ld (bases).
+// ---------------------------------------------------------------------------
+constexpr int kDotThreads = 256;
+constexpr int kDotItems = 8;
+constexpr int kDotChunk = kDotThreads * kDotItems;
+constexpr int kMaxCols = 64;
+
+// partial[r][blk][c] = sum over the block's rows of V_r[c][i] * w_r[i]
+__global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restrict__ V, int64_t ldv, int64_t vstride,
+                                                          int ncols, const double *__restrict__ w, int64_t wstride,
+                                                          int64_t n3, double *__restrict__ partial, int nblk) {
+    __shared__ double red[kDotThreads / 32][kMaxCols];
+    const int r = blockIdx.y;
+    const double *Vr = V + r * vstride;
+    const double *wr = w + r * wstride;
+    const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
+    double wv[kDotItems];
+#pragma unroll
+    for (int k = 0; k < kDotItems; ++k) {
+        int64_t i = i0 + (int64_t)k * kDotThreads + threadIdx.x;
+        wv[k] = i < n3 ? wr[i] : 0.0;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int c = 0; c < ncols; ++c) {
+        const double *Vc = Vr + (int64_t)c * ldv;
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < kDotItems; ++k) {
+            int64_t i = i0 + (int64_t)k * kDotThreads + threadIdx.x;
+            if (i < n3) acc += Vc[i] * wv[k];
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) red[wid][c] = acc;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kDotThreads / 32; ++q) s += red[q][c];
+        partial[((int64_t)r * nblk + blockIdx.x) * kMaxCols + c] = s;
+    }
+}
+
+__global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, int ncols, int nrhs,
+                                  double *__restrict__ out, int64_t ostride) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrhs * ncols) return;
+    const int r = t / ncols, c = t % ncols;
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += partial[((int64_t)r * nblk + b) * kMaxCols + c];
+    out[(int64_t)r * ostride + c] = s;
+}
+
+// w_r[i] -= sum_c V_r[c][i] * h_r[c]
+__global__ void k_sub_basis(const double *__restrict__ V, int64_t ldv, int64_t vstride, int ncols,
+                            const double *__restrict__ h, int64_t hstride, double *__restrict__ w, int64_t wstride,
+                            int64_t n3) {
+    __shared__ double hs[kMaxCols];
+    const int r = blockIdx.y;
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) hs[c] = h[(int64_t)r * hstride + c];
+    __syncthreads();
+    const double *Vr = V + r * vstride;
+    double *wr = w + r * wstride;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = wr[i];
+        for (int c = 0; c < ncols; ++c) acc -= Vr[(int64_t)c * ldv + i] * hs[c];
+        wr[i] = acc;
+    }
+}
+
+// x_r[i] += sum_c V_r[c][i] * y_r[c] for c < k_r
+__global__ void k_add_basis(const double *__restrict__ V, int64_t ldv, int64_t vstride, const double *__restrict__ y,
+                            int64_t ystride, const int32_t *__restrict__ kcount, double *__restrict__ x,
+                            int64_t xstride, int64_t n3) {
+    __shared__ double ys[kMaxCols];
+    const int r = blockIdx.y;
+    const int k = kcount[r];
+    for (int c = threadIdx.x; c < k; c += blockDim.x) ys[c] = y[(int64_t)r * ystride + c];
+    __syncthreads();
+    const double *Vr = V + r * vstride;
+    double *xr = x + r * xstride;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = xr[i];
+        for (int c = 0; c < k; ++c) acc += Vr[(int64_t)c * ldv + i] * ys[c];
+        xr[i] = acc;
+    }
+}
+
+// out = a - b (per system)
+__global__ void k_sub(const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ out,
+                      int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = a[i] - b[i];
+}
+
+// dst_r = src_r * scale_r (scale_r = 1/norm; zero norm -> zero vector)
+__global__ void k_scale_vec(const double *__restrict__ src, int64_t sstride, double *__restrict__ dst,
+                            int64_t dstride, const double *__restrict__ nrm, int64_t nstride, int64_t n3) {
+    const int r = blockIdx.y;
+    const double v = nrm[r * nstride];
+    const double f = v != 0.0 ? 1.0 / v : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x)
+        dst[r * dstride + i] = src[r * sstride + i] * f;
+}
+
+__global__ void k_sqrt_copy(const double *__restrict__ a, double *__restrict__ b, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = sqrt(a[i]);
+}
+
+// y += x
+__global__ void k_axpy1(const double *__restrict__ x, double *__restrict__ y, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] += x[i];
+}
+
+struct GmresState {
+    double *H;      // [r][(restart+1) * restart], column j at offset j*(restart+1)
+    double *cs, *sn;  // [r][restart]
+    double *g;      // [r][restart+1]
+    double *h1, *h2;  // [r][kMaxCols]
+    double *nrm2;   // [r]
+    double *beta;   // [r]
+    double *bnorm;  // [r]
+    double *res;    // [r] residual estimate / true relres
+    int32_t *kcount;  // [r]
+    double *y;      // [r][restart]
+};
+
+// Start of a cycle: beta = sqrt(nrm2), g = [beta, 0...], relres = beta / bnorm.
+__global__ void k_cycle_start(GmresState st, int restart, int nrhs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrhs) return;
+    const double b = sqrt(st.nrm2[r]);
+    st.beta[r] = b;
+    for (int i = 0; i <= restart; ++i) st.g[r * (restart + 1) + i] = 0.0;
+    st.g[r * (restart + 1)] = b;
+    st.res[r] = st.bnorm[r] > 0 ? b / st.bnorm[r] : 0.0;
+    st.kcount[r] = 0;
+}
+
+// Arnoldi column j: H[:,j] = h1 + h2, H[j+1,j] = ||w||, then Givens rotations.
+__global__ void k_arnoldi_givens(GmresState st, int restart, int j, int nrhs, const int32_t *__restrict__ frozen) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrhs) return;
+    if (frozen[r]) return;
+    const int ld = restart + 1;
+    double *Hc = st.H + (int64_t)r * ld * restart + (int64_t)j * ld;
+    for (int i = 0; i <= j; ++i) Hc[i] = st.h1[r * kMaxCols + i] + st.h2[r * kMaxCols + i];
+    const double wn = sqrt(st.nrm2[r]);
+    st.nrm2[r] = wn;  // the following normalisation of w divides by the norm
+    Hc[j + 1] = wn;
+    double *cs = st.cs + r * restart, *sn = st.sn + r * restart, *g = st.g + r * ld;
+    for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * Hc[i] + sn[i] * Hc[i + 1];
+        Hc[i + 1] = -sn[i] * Hc[i] + cs[i] * Hc[i + 1];
+        Hc[i] = t;
+    }
+    const double a = Hc[j], b = Hc[j + 1];
+    const double den = hypot(a, b);
+    if (den == 0.0) {
+        cs[j] = 1.0;
+        sn[j] = 0.0;
+    } else {
+        cs[j] = a / den;
+        sn[j] = b / den;
+    }
+    Hc[j] = cs[j] * a + sn[j] * b;
+    Hc[j + 1] = 0.0;
+    const double gj = g[j];
+    g[j] = cs[j] * gj;
+    g[j + 1] = -sn[j] * gj;
+    st.res[r] = st.bnorm[r] > 0 ? fabs(g[j + 1]) / st.bnorm[r] : 0.0;
+    st.kcount[r] = j + 1;
+}
+
+// Back substitution H[:k,:k] y = g[:k].
+__global__ void k_backsolve(GmresState st, int restart, int nrhs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrhs) return;
+    const int ld = restart + 1;
+    const int k = st.kcount[r];
+    const double *H = st.H + (int64_t)r * ld * restart;
+    const double *g = st.g + r * ld;
+    double *y = st.y + r * restart;
+    for (int i = k - 1; i >= 0; --i) {
+        double v = g[i];
+        for (int c = i + 1; c < k; ++c) v -= H[(int64_t)c * ld + i] * y[c];
+        const double d = H[(int64_t)i * ld + i];
+        y[i] = d != 0.0 ? v / d : 0.0;
+    }
+}
+
+static char *carve_ws(char *&p, size_t bytes) {
+    uintptr_t u = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+    p = (char *)(u + bytes);
+    return (char *)u;
+}
+
+// Dots of the first ncols basis vectors with w, for every system.
+static int multidot(const double *V, int64_t ldv, int64_t vstride, int ncols, const double *w, int64_t wstride,
+                    int64_t n3, int nrhs, double *partial, double *out, int64_t ostride, cudaStream_t s) {
+    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    dim3 g(nblk, nrhs);
+    k_multidot<<<g, kDotThreads, 0, s>>>(V, ldv, vstride, ncols, w, wstride, n3, partial, nblk);
+    MPS_LAUNCH_CHECK();
+    k_reduce_partials<<<(nrhs * ncols + 127) / 128, 128, 0, s>>>(partial, nblk, ncols, nrhs, out, ostride);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+// Core restarted GMRES (Arnoldi with classical Gram-Schmidt applied twice, Givens
+// rotations, all float64) for nrhs systems with batched matvecs of the given
+// precision.  x holds the initial guess on entry and the solution on exit.
+// Basis layout V[j][r][i]: basis vector j of every system is one contiguous
+// nrhs x n3 block, which is exactly the batched matvec's input.
+static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, double tol, int restart, int maxit,
+                      int precision, int *conv, double *relres_out, int *cycles_out, int *mv_count,
+                      cudaStream_t st) {
+    const int64_t n3 = 3 * s->n;
+    const int ld = restart + 1;
+    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    const int64_t ldv = (int64_t)nrhs * n3;
+    size_t bytes = 0;
+    bytes += 256 + sizeof(double) * (size_t)ld * ldv;                 // V
+    bytes += 256 + sizeof(double) * (size_t)ldv;                      // w
+    bytes += 256 + sizeof(double) * (size_t)nrhs * ld * restart;      // H
+    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * restart);     // cs sn
+    bytes += 256 + sizeof(double) * (size_t)nrhs * ld;                // g
+    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * kMaxCols);    // h1 h2
+    bytes += 4 * (256 + sizeof(double) * (size_t)nrhs);               // nrm2 beta bnorm res
+    bytes += 2 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount frozen
+    bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
+    bytes += 256 + sizeof(double) * (size_t)nrhs * nblk * kMaxCols;   // partial
+    char *base = nullptr;
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&base, bytes, st));
+    char *p = base;
+    double *V = (double *)carve_ws(p, sizeof(double) * (size_t)ld * ldv);
+    double *w = (double *)carve_ws(p, sizeof(double) * (size_t)ldv);
+    GmresState S;
+    S.H = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld * restart);
+    S.cs = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    S.sn = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    S.g = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld);
+    S.h1 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
+    S.h2 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
+    S.nrm2 = (double *)carve_ws(p, sizeof(double) * nrhs);
+    S.beta = (double *)carve_ws(p, sizeof(double) * nrhs);
+    S.bnorm = (double *)carve_ws(p, sizeof(double) * nrhs);
+    S.res = (double *)carve_ws(p, sizeof(double) * nrhs);
+    S.kcount = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    int32_t *frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    double *partial = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * nblk * kMaxCols);
+
+    std::vector<double> hres(nrhs);
+    std::vector<int32_t> hfrozen(nrhs, 0);
+    int rc = MPS_OK;
+    const dim3 vgrid(grid_for(n3, 256, 152 * 8), nrhs);
+    int cyc = 0;
+    auto fail = [&](int code) {
+        cudaFreeAsync(base, st);
+        return code;
+    };
+#define GM_TRY(expr)                       \
+    do {                                   \
+        int _r = (expr);                   \
+        if (_r != MPS_OK) return fail(_r); \
+    } while (0)
+#define GM_LAUNCH()                     \
+    do {                                \
+        count_launch();                 \
+        GM_CUDA(cudaGetLastError());    \
+    } while (0)
+#define GM_CUDA(expr)                                      \
+    do {                                                   \
+        cudaError_t _e = (expr);                           \
+        if (_e != cudaSuccess) {                           \
+            set_last_error(_e, #expr, __FILE__, __LINE__); \
+            return fail(MPS_CUDA_ERR);                     \
+        }                                                  \
+    } while (0)
+
+    // ||b|| per system
+    GM_TRY(multidot(b, n3, n3, 1, b, n3, n3, nrhs, partial, S.nrm2, 1, st));
+    k_sqrt_copy<<<(nrhs + 31) / 32, 32, 0, st>>>(S.nrm2, S.bnorm, nrhs);
+    GM_LAUNCH();
+    for (int r = 0; r < nrhs; ++r) conv[r] = 0;
+    for (cyc = 0; cyc < maxit; ++cyc) {
+        // r0 = b - A x  -> V[0] (unnormalised)
+        GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
+        ++*mv_count;
+        k_sub<<<grid_for(ldv, 256), 256, 0, st>>>(b, w, V, ldv);
+        GM_LAUNCH();
+        GM_TRY(multidot(V, ldv, n3, 1, V, n3, n3, nrhs, partial, S.nrm2, 1, st));
+        k_cycle_start<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs);
+        GM_LAUNCH();
+        GM_CUDA(cudaMemcpyAsync(hres.data(), S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        GM_CUDA(cudaStreamSynchronize(st));
+        bool all = true;
+        for (int r = 0; r < nrhs; ++r) {
+            relres_out[r] = hres[r];
+            conv[r] = hres[r] <= tol;
+            hfrozen[r] = conv[r];
+            all = all && conv[r];
+        }
+        if (all) break;
+        GM_CUDA(cudaMemcpyAsync(frozen, hfrozen.data(), sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+        k_scale_vec<<<vgrid, 256, 0, st>>>(V, n3, V, n3, S.beta, 1, n3);
+        GM_LAUNCH();
+        for (int j = 0; j < restart; ++j) {
+            GM_TRY(matvec_any(s, V + (int64_t)j * ldv, w, nrhs, precision, st));
+            ++*mv_count;
+            // classical Gram-Schmidt, twice
+            GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h1, kMaxCols, st));
+            k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h1, kMaxCols, w, n3, n3);
+            GM_LAUNCH();
+            GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h2, kMaxCols, st));
+            k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h2, kMaxCols, w, n3, n3);
+            GM_LAUNCH();
+            GM_TRY(multidot(w, n3, n3, 1, w, n3, n3, nrhs, partial, S.nrm2, 1, st));
+            k_arnoldi_givens<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, j, nrhs, frozen);
+            GM_LAUNCH();
+            k_scale_vec<<<vgrid, 256, 0, st>>>(w, n3, V + (int64_t)(j + 1) * ldv, n3, S.nrm2, 1, n3);
+            GM_LAUNCH();
+            GM_CUDA(cudaMemcpyAsync(hres.data(), S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+            GM_CUDA(cudaStreamSynchronize(st));
+            bool done = true, changed = false;
+            for (int r = 0; r < nrhs; ++r) {
+                if (!hfrozen[r] && hres[r] <= tol) {
+                    hfrozen[r] = 1;
+                    changed = true;
+                }
+                done = done && hfrozen[r];
+            }
+            if (done) break;
+            if (changed)
+                GM_CUDA(cudaMemcpyAsync(frozen, hfrozen.data(), sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+        }
+        k_backsolve<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs);
+        GM_LAUNCH();
+        k_add_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, S.y, restart, S.kcount, x, n3, n3);
+        GM_LAUNCH();
+    }
+    // final true residual
+    GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
+    ++*mv_count;
+    k_sub<<<grid_for(ldv, 256), 256, 0, st>>>(b, w, w, ldv);
+    GM_LAUNCH();
+    GM_TRY(multidot(w, n3, n3, 1, w, n3, n3, nrhs, partial, S.nrm2, 1, st));
+    {
+        std::vector<double> nr(nrhs), nb(nrhs);
+        GM_CUDA(cudaMemcpyAsync(nr.data(), S.nrm2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        GM_CUDA(cudaMemcpyAsync(nb.data(), S.bnorm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        GM_CUDA(cudaStreamSynchronize(st));
+        for (int r = 0; r < nrhs; ++r) {
+            relres_out[r] = nb[r] > 0 ? sqrt(nr[r]) / nb[r] : 0.0;
+            conv[r] = relres_out[r] <= tol;
+            if (!conv[r]) rc = MPS_NOT_CONVERGED;
+        }
+    }
+    *cycles_out = cyc;
+    cudaFreeAsync(base, st);
+#undef GM_TRY
+#undef GM_CUDA
+#undef GM_LAUNCH
+    return rc;
+}
+
+// Relative residuals ||b - A x|| / ||b|| with the float64 operator; r receives b - A x.
+static int true_residual(mps_system *s, const double *b, const double *x, double *r, double *ax, int nrhs,
+                         double *partial, double *nrm, std::vector<double> &relres, cudaStream_t st) {
+    const int64_t n3 = 3 * s->n;
+    MPS_TRY(matvec_any(s, x, ax, nrhs, MPS_FP64, st));
+    k_sub<<<grid_for((int64_t)nrhs * n3, 256), 256, 0, st>>>(b, ax, r, (int64_t)nrhs * n3);
+    MPS_LAUNCH_CHECK();
+    MPS_TRY(multidot(r, n3, n3, 1, r, n3, n3, nrhs, partial, nrm, 1, st));
+    MPS_TRY(multidot(b, n3, n3, 1, b, n3, n3, nrhs, partial, nrm + nrhs, 1, st));
+    std::vector<double> hn(2 * nrhs);
+    MPS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int q = 0; q < nrhs; ++q) relres[q] = hn[nrhs + q] > 0 ? sqrt(hn[q]) / sqrt(hn[nrhs + q]) : 0.0;
+    return MPS_OK;
+}
+
+// Iterative refinement: x <- x + d with A32 d ~= b - A64 x solved by float32-operator GMRES.
+static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, const mps_solve_opts *o, int *conv,
+                        double *relres_out, int *cycles_out, int *mv64, int *mv32, cudaStream_t st) {
+    const int64_t n3 = 3 * s->n;
+    const int64_t tot = (int64_t)nrhs * n3;
+    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+    const int inner_maxit = o->inner_maxit > 0 ? o->inner_maxit : 4;
+    double *buf = nullptr;
+    const size_t bytes = sizeof(double) * (3 * (size_t)tot + 2 * nrhs + (size_t)nrhs * nblk * kMaxCols);
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&buf, bytes, st));
+    double *r = buf, *dx = buf + tot, *ax = buf + 2 * tot, *nrm = buf + 3 * tot, *partial = nrm + 2 * nrhs;
+    std::vector<double> rel(nrhs);
+    std::vector<int> ic(nrhs);
+    std::vector<double> ir(nrhs);
+    int rc = MPS_NOT_CONVERGED;
+    int step = 0;
+    for (step = 0;; ++step) {
+        int e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
+        ++*mv64;
+        if (e) {
+            rc = e;
+            break;
+        }
+        bool all = true;
+        for (int q = 0; q < nrhs; ++q) {
+            relres_out[q] = rel[q];
+            conv[q] = rel[q] <= o->tol;
+            all = all && conv[q];
+            // a converged system gets a zero right-hand side: its correction stays zero
+            if (conv[q] && cudaMemsetAsync(r + q * n3, 0, sizeof(double) * n3, st) != cudaSuccess) e = MPS_CUDA_ERR;
+        }
+        if (e) {
+            rc = e;
+            break;
+        }
+        if (all) {
+            rc = MPS_OK;
+            break;
+        }
+        if (step >= o->maxit) break;
+        if (cudaMemsetAsync(dx, 0, sizeof(double) * tot, st) != cudaSuccess) {
+            rc = MPS_CUDA_ERR;
+            break;
+        }
+        int icyc = 0;
+        e = gmres_core(s, r, dx, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
+                       mv32, st);
+        if (e != MPS_OK && e != MPS_NOT_CONVERGED) {
+            rc = e;
+            break;
+        }
+        k_axpy1<<<grid_for(tot, 256), 256, 0, st>>>(dx, x, tot);
+        count_launch();
+        if (cudaGetLastError() != cudaSuccess) {
+            rc = MPS_CUDA_ERR;
+            break;
+        }
+    }
+    *cycles_out = step;
+    cudaFreeAsync(buf, st);
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps_stream_t stream) {
+    if (!d || !out) return MPS_BAD_ARG;
+    *out = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (d->n < 1 || !d->x || !d->lambdap || d->n_diag < 1 || !(d->xi > 0) || !(d->rc > 0) || d->P < 1 ||
+        !d->perp || !d->para || !d->rvals || d->n_tab < 2 || d->max_rhs < 1)
+        return MPS_BAD_ARG;
+    for (int k = 0; k < 3; ++k) {
+        if (!(d->box[k] > 0) || d->Ngrid[k] < 1) return MPS_BAD_ARG;
+        if (d->Ngrid[k] < d->P) return MPS_BAD_ARG;  // the stencil wraps at most once
+        if (d->rc > d->box[k] / 2.0) return MPS_RC_GT_HALF_BOX;
+    }
+    if (d->P > 32) return MPS_BAD_ARG;
+    mps_system *s = new mps_system();
+    s->n = d->n;
+    s->max_rhs = d->max_rhs;
+    s->n_diag = d->n_diag;
+    memcpy(s->box, d->box, sizeof(s->box));
+    s->xi = d->xi;
+    s->rc = d->rc;
+    s->slab_factor = d->slab_factor;
+    s->gp = make_grid_params(d->Ngrid, d->box, d->xi, d->eta, d->P);
+    s->Gc = (int64_t)(s->gp.N[0] / 2 + 1) * s->gp.N[1] * s->gp.N[2];
+    const int64_t n = d->n;
+    int rc = MPS_OK;
+#define CR_TRY(expr)               \
+    do {                           \
+        rc = (expr);               \
+        if (rc != MPS_OK) {        \
+            free_system(s);        \
+            return rc;             \
+        }                          \
+    } while (0)
+    CR_TRY(dalloc(&s->x, sizeof(double) * 3 * n));
+    if (cudaMemcpyAsync(s->x, d->x, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        CR_TRY(MPS_CUDA_ERR);
+    CR_TRY(dalloc(&s->diag, sizeof(double) * n * d->n_diag));
+    CR_TRY(build_diag(d->lambdap, n * d->n_diag, d->perp, s->diag, st));
+    CR_TRY(dalloc(&s->slab, sizeof(double) * d->max_rhs));
+    CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * d->max_rhs));
+    if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * d->max_rhs) != cudaSuccess) CR_TRY(MPS_NO_MEMORY);
+    if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
+    // cell list + pair CSR
+    compute_ncell(d->box, d->rc, s->ncell);
+    const int64_t ncells = s->ncell[0] * s->ncell[1] * s->ncell[2];
+    int64_t *cell3 = nullptr, *cnt27 = nullptr, *off27 = nullptr;
+    void *bins = nullptr, *scan_tmp = nullptr;
+    int *err = nullptr;
+    CR_TRY(dalloc(&cell3, sizeof(int64_t) * 3 * n));
+    CR_TRY(dalloc(&bins, cell_bins_bytes(n, ncells)));
+    CR_TRY(dalloc(&cnt27, sizeof(int64_t) * 27 * n));
+    CR_TRY(dalloc(&off27, sizeof(int64_t) * 27 * n));
+    CR_TRY(dalloc(&scan_tmp, scan_workspace(27 * n)));
+    CR_TRY(dalloc(&err, sizeof(int)));
+    auto tmp_free = [&]() {
+        cudaFree(cell3);
+        cudaFree(bins);
+        cudaFree(cnt27);
+        cudaFree(off27);
+        cudaFree(scan_tmp);
+        cudaFree(err);
+    };
+    CellBins cb;
+    rc = cell_assign(s->x, n, d->box, s->ncell, cell3, st);
+    if (!rc) rc = cell_bins_build(cell3, n, s->ncell, bins, cb, st);
+    int64_t np = 0;
+    if (!rc) rc = csr_pairs_count(s->x, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);
+    if (rc) {
+        tmp_free();
+        free_system(s);
+        return rc;
+    }
+    s->n_pairs = np;
+    rc = dalloc(&s->row_ptr, sizeof(int64_t) * (n + 1));
+    if (!rc) rc = dalloc(&s->p64.nbr, sizeof(int32_t) * np);
+    if (!rc) rc = dalloc(&s->p64.A, sizeof(double) * np);
+    if (!rc) rc = dalloc(&s->p64.BA, sizeof(double) * np);
+    if (!rc) rc = dalloc(&s->p64.rx, sizeof(double) * np);
+    if (!rc) rc = dalloc(&s->p64.ry, sizeof(double) * np);
+    if (!rc) rc = dalloc(&s->p64.rz, sizeof(double) * np);
+    if (!rc) rc = dalloc(&s->p32.A, sizeof(float) * np);
+    if (!rc) rc = dalloc(&s->p32.BA, sizeof(float) * np);
+    if (!rc) rc = dalloc(&s->p32.rx, sizeof(float) * np);
+    if (!rc) rc = dalloc(&s->p32.ry, sizeof(float) * np);
+    if (!rc) rc = dalloc(&s->p32.rz, sizeof(float) * np);
+    s->p32.nbr = s->p64.nbr;
+    if (!rc && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (!rc)
+        rc = csr_pairs_fill(s->x, d->box, d->rc, cb, cnt27, off27, d->perp, d->para, d->rvals, d->n_tab, s->row_ptr,
+                            s->p64, s->p32, err, st);
+    int herr = 0;
+    if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    tmp_free();
+    if (!rc && herr) rc = MPS_TABLE_RANGE;
+    if (rc) {
+        free_system(s);
+        return rc;
+    }
+    // grid geometry + Green's coefficients
+    CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n));
+    CR_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P));
+    CR_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P));
+    CR_TRY(grid_geometry(s->x, n, s->gp, s->start, s->w64, s->w32, st));
+    CR_TRY(dalloc(&s->h64, sizeof(double) * s->Gc));
+    CR_TRY(dalloc(&s->h32, sizeof(float) * s->Gc));
+    CR_TRY(green_half(s->gp, s->h64, s->h32, st));
+#undef CR_TRY
+    *out = s;
+    return MPS_OK;
+}
+
+extern "C" void mps_system_destroy(mps_system *sys) {
+    if (sys) cudaDeviceSynchronize();
+    free_system(sys);
+}
+
+extern "C" int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t *ncell) {
+    if (!sys) return MPS_BAD_ARG;
+    if (n_pairs) *n_pairs = sys->n_pairs;
+    if (ncell)
+        for (int d = 0; d < 3; ++d) ncell[d] = sys->ncell[d];
+    return MPS_OK;
+}
+
+extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t nrhs, const int32_t *diag_index,
+                          int32_t precision, mps_stream_t stream) {
+    if (!sys || !m || !out || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
+    if (precision != MPS_FP64 && precision != MPS_FP32) return MPS_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
+    return matvec_any(sys, m, out, nrhs, precision, st);
+}
+
+extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *out_ri, int32_t diag_index,
+                                  mps_stream_t stream) {
+    if (!sys || !m_ri || !out_ri || sys->max_rhs < 2) return MPS_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    int32_t di[2] = {diag_index, diag_index};
+    MPS_TRY(upload_diag_idx(sys, di, 2, st));
+    const int64_t G = sys->gp.G;
+    if (!sys->rgrid2) MPS_TRY(dalloc(&sys->rgrid2, sizeof(double) * 6 * G));
+    if (!sys->cgrid) MPS_TRY(dalloc(&sys->cgrid, sizeof(double) * 2 * 3 * G));
+    const double vol = sys->box[0] * sys->box[1] * sys->box[2];
+    MPS_TRY(slab_terms(m_ri, sys->n, 2, sys->slab_factor / vol, sys->slab, st));
+    MPS_TRY(spread<double>(m_ri, sys->n, 2, sys->start, sys->w64, sys->gp, sys->rgrid2, st));
+    MPS_TRY(pack_complex(sys->rgrid2, G, sys->cgrid, st));
+    MPS_TRY(exec_plan(sys, CUFFT_Z2Z, 3, sys->cgrid, sys->cgrid, CUFFT_FORWARD, st));
+    MPS_TRY(scale_full_c2c(sys->cgrid, sys->gp, st));
+    MPS_TRY(exec_plan(sys, CUFFT_Z2Z, 3, sys->cgrid, sys->cgrid, CUFFT_INVERSE, st));
+    MPS_TRY(unpack_complex(sys->cgrid, G, sys->rgrid2, st));
+    MPS_TRY(contract<double>(sys->rgrid2, sys->n, 2, sys->start, sys->w64, sys->gp, out_ri, st));
+    return real_space_csr<double>(m_ri, out_ri, sys->n, 2, sys->row_ptr, sys->p64, sys->diag, sys->diag_idx, sys->slab,
+                                  true, st);
+}
+
+extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
+                         const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
+                         mps_stream_t stream) {
+    if (!sys || !b || !x || !opts || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
+    if (opts->restart < 1 || opts->restart >= kMaxCols || opts->maxit < 1 || !(opts->tol > 0)) return MPS_BAD_ARG;
+    if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32) return MPS_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
+    const int64_t n3 = 3 * sys->n;
+    const size_t vbytes = sizeof(double) * (size_t)nrhs * n3;
+    if (x0 == nullptr) {
+        MPS_CUDA_TRY(cudaMemsetAsync(x, 0, vbytes, st));
+    } else if (x0 != x) {
+        MPS_CUDA_TRY(cudaMemcpyAsync(x, x0, vbytes, cudaMemcpyDeviceToDevice, st));
+    }
+    std::vector<int> conv(nrhs, 0);
+    std::vector<double> relres(nrhs, 0.0);
+    int cycles = 0, mv64 = 0, mv32 = 0;
+    int rc;
+    if (opts->precision == MPS_FP64) {
+        rc = gmres_core(sys, b, x, nrhs, opts->tol, opts->restart, opts->maxit, MPS_FP64, conv.data(), relres.data(),
+                        &cycles, &mv64, st);
+    } else {
+        rc = refine_mixed(sys, b, x, nrhs, opts, conv.data(), relres.data(), &cycles, &mv64, &mv32, st);
+    }
+    if (info) {
+        for (int q = 0; q < nrhs; ++q) {
+            info[q].converged = conv[q];
+            info[q].relres = relres[q];
+            info[q].cycles = cycles;
+            info[q].matvecs_fp64 = mv64;
+            info[q].matvecs_fp32 = mv32;
+        }
+    }
+    return rc;
+}
+
+extern "C" int mps_system_profile(mps_system *sys, int32_t enable) {
+    if (!sys) return MPS_BAD_ARG;
+    sys->profile = enable != 0;
+    return MPS_OK;
+}
+
+extern "C" int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count) {
+    if (!sys || !ms || !count) return MPS_BAD_ARG;
+    for (auto &e : sys->pending) {
+        MPS_CUDA_TRY(cudaEventSynchronize(e.ev[kStages]));
+        const int p = e.precision == MPS_FP64 ? 0 : 1;
+        for (int k = 0; k < kStages; ++k) {
+            float t = 0.f;
+            MPS_CUDA_TRY(cudaEventElapsedTime(&t, e.ev[k], e.ev[k + 1]));
+            sys->stage_ms[p][k] += t;
+        }
+        sys->stage_count[p] += 1;
+        sys->spare.push_back(e);
+    }
+    sys->pending.clear();
+    for (int p = 0; p < 2; ++p) {
+        for (int k = 0; k < kStages; ++k) ms[p * kStages + k] = sys->stage_ms[p][k];
+        count[p] = sys->stage_count[p];
+        for (int k = 0; k < kStages; ++k) sys->stage_ms[p][k] = 0.0;
+        sys->stage_count[p] = 0;
+    }
+    return MPS_OK;
+}

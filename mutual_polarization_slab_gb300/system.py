@@ -1,0 +1,181 @@
+"""Device-resident spectral-Ewald system: the GPU form of the reference's
+``real_precomp`` / ``grid_precomp`` / ``k_precomp`` tuples
+(``CPU - Ewald test/capacitance.py:369-385``) plus FFT plans and grids.
+
+One object per particle configuration.  It owns device memory through the C ABI
+(``mps_system_create``) and frees it on ``close()`` / garbage collection.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+PRECISIONS = {"fp64": L.MPS_FP64, "fp32": L.MPS_FP32, "mixed": L.MPS_FP32}
+
+
+def as_device(a, dtype=torch.float64) -> torch.Tensor:
+    """Contiguous CUDA tensor view/copy of a numpy array or tensor."""
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dtype, device="cuda")
+
+
+@dataclass
+class SolveInfo:
+    converged: bool
+    relres: float
+    matvecs_fp64: int
+    matvecs_fp32: int
+    cycles: int
+
+
+def spectral_parameters(box, xi, errortol):
+    """rc, Ngrid, h, P, eta derived from one tolerance (``capacitance.py:357-362``)."""
+    box = np.asarray(box, dtype=np.float64).reshape(3)
+    lt = math.sqrt(-math.log(errortol))
+    rc = lt / xi
+    kcut = 2.0 * xi * lt
+    Ngrid = np.ceil(1.0 + box * kcut / math.pi).astype(np.int64)
+    h = box / Ngrid
+    P = int(math.ceil(-2.0 * math.log(errortol) / math.pi))
+    eta = P * (h * xi) ** 2 / math.pi
+    return rc, Ngrid, h, P, eta
+
+
+class SpectralEwaldSystem:
+    """Precomputed geometry of one configuration and its batched operator.
+
+    Parameters mirror ``magnetic_field`` (``ewald.py:1146-1168``): positions
+    ``x (N,3)``, permittivities ``lambdap`` (``(N,)`` or ``(n_sets, N)`` for a
+    contrast spectrum), ``box``, ``xi``, cutoff ``rc``, grid ``Ngrid``, support
+    ``P``, tables ``perp``/``para`` on separations ``rvals`` (``rvals[0] = 0``,
+    self value in ``perp[0]``), ``slab_factor``.
+    """
+
+    def __init__(self, x, lambdap, box, xi, rc, Ngrid, P, perp, para, rvals, slab_factor=1.0, eta=None,
+                 max_rhs=3):
+        lib = L.lib()
+        self._lib = lib
+        self._h = C.c_void_p(0)
+        self.x = as_device(x).reshape(-1, 3)
+        lam = as_device(lambdap)
+        if lam.dim() == 1:
+            lam = lam.reshape(1, -1)
+        self.lambdap = lam.contiguous()
+        self.n = int(self.x.shape[0])
+        if self.lambdap.shape[1] != self.n:
+            raise ValueError("lambdap must have N entries per permittivity set")
+        self.box = np.asarray(box, dtype=np.float64).reshape(3)
+        self.xi = float(xi)
+        self.rc = float(rc)
+        self.Ngrid = np.asarray(Ngrid, dtype=np.int64).reshape(3)
+        self.P = int(P)
+        self.slab_factor = float(slab_factor)
+        self.max_rhs = int(max_rhs)
+        self.perp = as_device(perp)
+        self.para = as_device(para)
+        self.rvals = as_device(rvals)
+        if np.any(self.rc > self.box / 2.0):
+            raise ValueError("Real-space cutoff exceeds half the box size; tolerance unmet.")
+        d = L.SystemDesc()
+        d.n = self.n
+        d.x = self.x.data_ptr()
+        d.lambdap = self.lambdap.data_ptr()
+        d.n_diag = int(self.lambdap.shape[0])
+        d.box = (C.c_double * 3)(*self.box)
+        d.xi = self.xi
+        d.rc = self.rc
+        d.Ngrid = (C.c_int64 * 3)(*self.Ngrid)
+        d.P = self.P
+        eta = np.zeros(3) if eta is None else np.asarray(eta, dtype=np.float64).reshape(3)
+        d.eta = (C.c_double * 3)(*eta)
+        d.perp = self.perp.data_ptr()
+        d.para = self.para.data_ptr()
+        d.rvals = self.rvals.data_ptr()
+        d.n_tab = int(self.rvals.numel())
+        d.slab_factor = self.slab_factor
+        d.max_rhs = self.max_rhs
+        L.check(lib.mps_system_create(C.byref(d), C.byref(self._h), L.stream_handle()), "mps_system_create")
+        np_ = C.c_int64(0)
+        nc = (C.c_int64 * 3)()
+        L.check(lib.mps_system_info(self._h, C.byref(np_), nc))
+        self.n_pairs = int(np_.value)
+        self.ncell = np.array(list(nc), dtype=np.int64)
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if self._h and self._h.value:
+            self._lib.mps_system_destroy(self._h)
+            self._h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- operator ---------------------------------------------------------
+    def _diag_arg(self, nrhs, diag_index):
+        if diag_index is None:
+            return None
+        arr = (C.c_int32 * nrhs)(*[int(v) for v in diag_index])
+        return arr
+
+    def matvec(self, m, precision="fp64", diag_index=None, out=None) -> torch.Tensor:
+        """Field at the particles from real moments ``m`` of shape (N,3) or (R,N,3)."""
+        m = as_device(m)
+        single = m.dim() == 2
+        m = m.reshape(-1, self.n, 3).contiguous()
+        nrhs = m.shape[0]
+        if out is None:
+            out = torch.empty_like(m)
+        L.check(self._lib.mps_matvec(self._h, L.dptr(m), L.dptr(out), nrhs, self._diag_arg(nrhs, diag_index),
+                                     PRECISIONS[precision], L.stream_handle()), "mps_matvec")
+        return out[0] if single else out
+
+    def matvec_complex(self, m, diag_index=0) -> torch.Tensor:
+        """The reference's complex pipeline on one complex (N,3) vector; returns complex128."""
+        if isinstance(m, torch.Tensor):
+            mc = m.to(device="cuda", dtype=torch.complex128)
+        else:
+            mc = torch.as_tensor(np.asarray(m, dtype=np.complex128), device="cuda")
+        ri = torch.stack((mc.real, mc.imag)).contiguous()
+        out = torch.empty_like(ri)
+        L.check(self._lib.mps_matvec_complex(self._h, L.dptr(ri), L.dptr(out), int(diag_index), L.stream_handle()),
+                "mps_matvec_complex")
+        return torch.complex(out[0], out[1])
+
+    def solve(self, b, x0=None, tol=1e-8, restart=30, maxit=100, precision="fp64", inner_tol=1e-4,
+              inner_maxit=4, diag_index=None, raise_on_fail=False):
+        """GMRES (``precision='fp64'``) or float64 iterative refinement around a
+        float32-operator GMRES (``'mixed'``) for R right-hand sides at once.
+
+        ``b``, ``x0``: (N,3) or (R,N,3).  Returns (x, [SolveInfo] * R)."""
+        b = as_device(b)
+        single = b.dim() == 2
+        b = b.reshape(-1, self.n, 3).contiguous()
+        nrhs = b.shape[0]
+        x = torch.empty_like(b)
+        x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, 3).contiguous()
+        opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
+                           precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit))
+        info = (L.SolveInfo * nrhs)()
+        st = self._lib.mps_gmres(self._h, L.dptr(b), L.dptr(x0d) if x0d is not None else C.c_void_p(0), L.dptr(x),
+                                 nrhs, self._diag_arg(nrhs, diag_index), C.byref(opts), info, L.stream_handle())
+        if st != L.MPS_NOT_CONVERGED or raise_on_fail:
+            L.check(st, "mps_gmres")
+        infos = [SolveInfo(bool(i.converged), float(i.relres), int(i.matvecs_fp64), int(i.matvecs_fp32),
+                           int(i.cycles)) for i in info]
+        return (x[0] if single else x), infos
