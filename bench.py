@@ -1,0 +1,415 @@
+#!/usr/bin/env python
+"""Benchmark: particle-solves/s of the capacitance-tensor solve on one GB300.
+
+Workload (the configuration the metric is quoted on): N = 100,000 unit spheres,
+seeded random sequential addition at volume fraction 0.3 (seed 2), contrast
+beta = 0.9 (eps = 28), the three unit field directions (3x3 capacitance
+tensor), xi = 4/rc with rc = (60/phi)^(1/3) (about 60 neighbours), 192^3 grid,
+P = 10, fully periodic.  A step = build the configuration's geometry (cell
+list, pair list, grid weights, Green's coefficients) + solve the three
+directions to tolerance.  particle-solves/s = N x 3 / step time.
+
+Arms:
+  default           mixed precision (float32 operator, float64 refinement), the
+                    three directions batched into one solve
+  --impl reference  the reference algorithm on the host cores (the CPU oracle,
+                    a NumPy restatement of the reference's Python path), on a
+                    bounded sample of the same workload
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-solves/s at N=1e5 (3-direction capacitance tensor, rel. moment err <= 1e-6 vs FP64)"
+UNIT = "particle-solves/s"
+
+
+def workload(n=100_000, phi=0.3, seed=2, beta=0.9, grid=192, P=10):
+    from mutual_polarization_slab_gb300.workloads import rsa
+    x, box, _ = rsa(n, phi, seed=seed)
+    rc = (60.0 / phi) ** (1.0 / 3.0)
+    xi = 4.0 / rc
+    eps = np.full(n, (1.0 + 2.0 * beta) / (1.0 - beta))
+    Ng = np.array([grid, grid, grid])
+    return dict(x=x, box=box, eps=eps, rc=rc, xi=xi, Ngrid=Ng, P=P, n=n, phi=phi, beta=beta)
+
+
+def config_dict(w, extra=None):
+    d = {"workload": f"RSA N={w['n']} phi={w['phi']} beta={w['beta']} 3 field directions, "
+                     f"{int(w['Ngrid'][0])}^3 grid, P={w['P']}, xi={w['xi']:.4f}, rc={w['rc']:.4f}, "
+                     f"fully periodic; geometry setup + solve per step",
+         "n_particles": int(w["n"]), "n_rhs": 3, "grid": int(w["Ngrid"][0]), "P": int(w["P"]),
+         "l2": "per-step grids (9 x 192^3 fp32 = 255 MB) exceed the 129 MB L2; L2 also flushed between steps"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        idx = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", idx, f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+
+    from mutual_polarization_slab_gb300 import _lib
+    from mutual_polarization_slab_gb300 import capacitance as gcap
+    from mutual_polarization_slab_gb300.system import SpectralEwaldSystem
+
+    world, rank = dist_init()
+    w = workload(n=args.n, grid=args.grid)
+    n = w["n"]
+    perp, para, rv = gcap.default_table(w["xi"])
+    xd = torch.as_tensor(w["x"], device="cuda")
+    epsd = torch.as_tensor(w["eps"], device="cuda")
+    phi = 4.0 * math.pi * n / (3.0 * float(np.prod(w["box"])))
+    amp = torch.as_tensor(gcap.dilute_guess(w["eps"], phi, [1.0, 0.0, 0.0])[:, 0], device="cuda")
+    eye = torch.eye(3, dtype=torch.float64, device="cuda")
+    b = eye[:, None, :].expand(3, n, 3).contiguous()
+    x0 = torch.stack([amp[:, None] * eye[i] for i in range(3)]).contiguous()
+    tol, restart = args.tol, args.restart
+    lib = _lib.lib()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def make_system(prof=False):
+        s = SpectralEwaldSystem(xd, epsd, w["box"], w["xi"], w["rc"], w["Ngrid"], w["P"], perp, para, rv,
+                                slab_factor=0.0, max_rhs=3)
+        if prof:
+            s.profile(True)
+        return s
+
+    def step_mixed(prof=False):
+        s = make_system(prof)
+        sol, info = s.solve(b, x0, tol=tol, restart=restart, maxit=args.maxref, precision="mixed",
+                            inner_tol=args.inner_tol, inner_maxit=args.inner_maxit)
+        return s, sol, info
+
+    def step_fp64_plain():
+        """The drop-in: float64 GMRES, one field direction at a time, reference warm-start order."""
+        s = make_system()
+        guess = x0[0]
+        sols, infos = [], []
+        for i in range(3):
+            si, inf = s.solve(b[i], guess, tol=tol, restart=restart, maxit=100, precision="fp64")
+            sols.append(si)
+            infos += inf
+            guess = si[:, [2, 0, 1]].contiguous()
+        return s, torch.stack(sols), infos
+
+    def timed(fn, steps, warmup, profile_last=False):
+        for _ in range(warmup):
+            s, _, _ = fn()
+            s.close()
+        torch.cuda.synchronize()
+        barrier(world)
+        total = 0.0
+        launches0 = lib.mps_kernel_launches()
+        stage = None
+        res = None
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            s, sol, info = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+            res = (sol, info)
+            if k == steps - 1 and profile_last:
+                stage = s
+            else:
+                s.close()
+        launches = lib.mps_kernel_launches() - launches0
+        barrier(world)
+        return total / steps, launches, res, stage
+
+    # --- headline: mixed + batched
+    clk = Clocks()
+    ms_mixed, launches, (sol_m, info_m), _ = timed(step_mixed, args.steps, args.warmup)
+    clocks = clk.stop()
+    ms_mixed = max_over_ranks(ms_mixed, world)
+    value = world * n * 3 / (ms_mixed / 1e3)
+
+    # --- roofline: stage times of one profiled mixed step (same launches, events on the launching stream)
+    s_prof, sol_p, _ = step_mixed(prof=True)
+    torch.cuda.synchronize()
+    st = s_prof.stage_times()
+    s_prof.close()
+    roof = roofline(w, st)
+
+    # --- plain float64 GMRES drop-in (reference solver structure) + accuracy of the mixed result
+    ms_fp64, _, (sol_64, info_64), _ = timed(step_fp64_plain, max(1, min(args.steps, 2)), 1)
+    ms_fp64 = max_over_ranks(ms_fp64, world)
+    s_ref = make_system()
+    ref_sol, ref_info = s_ref.solve(b, x0, tol=1e-11, restart=restart, maxit=100, precision="fp64")
+    s_ref.close()
+    err = [float(torch.linalg.vector_norm(sol_m[i] - ref_sol[i]) / torch.linalg.vector_norm(ref_sol[i]))
+           for i in range(3)]
+    C_m = sol_m.mean(dim=1)
+    C_r = ref_sol.mean(dim=1)
+    cerr = float(torch.linalg.matrix_norm(C_m - C_r) / torch.linalg.matrix_norm(C_r))
+    err64 = [float(torch.linalg.vector_norm(sol_64[i] - ref_sol[i]) / torch.linalg.vector_norm(ref_sol[i]))
+             for i in range(3)]
+
+    # --- end to end through the public API with host buffers
+    e2e = run_e2e(args, w, world)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 operator + fp64 refinement", "data": "synthetic (seeded RSA)",
+        "config": config_dict(w, {"parallelism": f"replicas x{world}", "tol": tol, "restart": restart,
+                                  "inner_tol": args.inner_tol}),
+        "e2e": e2e,
+        "gpu_launches": int(launches / max(args.steps, 1)),
+        "gpu_launches_note": "kernels of libmps_gb300.so per timed step (cuFFT executions not counted)",
+        "clocks": clocks,
+        "roofline": roof,
+        "accuracy": {"rel_moment_error_vs_fp64": err, "capacitance_tensor_rel_error": cerr,
+                     "fp64_plain_rel_moment_error": err64,
+                     "mixed_matvecs": {"fp64": info_m[0].matvecs_fp64, "fp32": info_m[0].matvecs_fp32,
+                                       "refinement_steps": info_m[0].cycles},
+                     "fp64_plain_matvecs": sum(i.matvecs_fp64 for i in info_64)},
+        "fp64_plain": {"value": world * n * 3 / (ms_fp64 / 1e3), "ms_per_step": ms_fp64,
+                       "what": "float64 GMRES, one direction at a time with the reference's warm start"},
+        "speedup_vs_fp64_plain": ms_fp64 / ms_mixed,
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def roofline(w, st):
+    """Dominant kernel (largest stage time of this library's kernels in the fp32 matvec) vs HBM peak."""
+    n, P = w["n"], w["P"]
+    G = int(np.prod(w["Ngrid"]))
+    nx = int(w["Ngrid"][0])
+    Gc = (nx // 2 + 1) * int(w["Ngrid"][1]) * int(w["Ngrid"][2])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    cnt, ms = st["fp32"]
+    R = 3
+    # algorithmic bytes per launch (one batched fp32 matvec, R = 3 vectors, s = 4 bytes)
+    per_particle_geom = 3 * P * 4 + 12
+    algo = {
+        "spread": 3 * R * G * 4 + n * (R * 3 * 8 + per_particle_geom),
+        "contract": 3 * R * G * 4 + n * (per_particle_geom + R * 3 * 8),
+        "scale": 2 * 3 * R * Gc * 8 + Gc * 4,
+        "real_space": None,
+    }
+    cand = {k: v for k, v in ms.items() if k in ("spread", "contract", "scale", "real_space")}
+    if not cnt:
+        return None
+    top = max(cand, key=cand.get)
+    avg_ms = cand[top] / cnt
+    if algo.get(top) is None:
+        top = max((k for k in cand if algo.get(k)), key=cand.get)
+        avg_ms = cand[top] / cnt
+    achieved = algo[top] / (avg_ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": f"k_{top} (fp32, 3 vectors)", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+            "algorithmic_bytes_per_launch": algo[top], "avg_launch_ms": avg_ms, "launches": cnt,
+            "traffic": None,
+            "stage_ms_per_matvec_fp32": {k: v / cnt for k, v in ms.items()},
+            "stage_ms_per_matvec_fp64": ({k: v / st["fp64"][0] for k, v in st["fp64"][1].items()}
+                                         if st["fp64"][0] else None)}
+
+
+def run_e2e(args, w, world):
+    """Same metric through the public API (capacitance_tensor) with host numpy inputs/outputs."""
+    import torch
+
+    from mutual_polarization_slab_gb300 import capacitance as gcap
+    n = w["n"]
+    phi = 4.0 * math.pi * n / (3.0 * float(np.prod(w["box"])))
+    guess = gcap.dilute_guess(w["eps"], phi, [1.0, 0.0, 0.0])
+    xh = np.ascontiguousarray(w["x"])
+    eh = np.ascontiguousarray(w["eps"])
+
+    def call():
+        C, S, info = gcap.capacitance_tensor(xh, eh, w["box"], guess, w["xi"], args.tol, rc=w["rc"],
+                                             Ngrid=w["Ngrid"], P=w["P"], restart=args.restart, maxit=args.maxref,
+                                             precision="mixed", inner_tol=args.inner_tol,
+                                             inner_maxit=args.inner_maxit)
+        return C, S
+
+    for _ in range(max(1, args.warmup - 1)):
+        call()
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        C, S = call()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    h2d = xh.nbytes + eh.nbytes + guess.nbytes
+    d2h = S.nbytes + C.nbytes
+    return {"value": world * n * 3 / dt, "unit": UNIT, "ms_per_step": dt * 1e3, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "api": "capacitance.capacitance_tensor(numpy in, numpy out)"}
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def cpu_sample(target_s=20.0, n=2000, seed=2):
+    """The CPU oracle's float64 tensor solve on an N-particle sample of the same workload
+    (same phi, beta, rc, xi and grid spacing; GMRES(30))."""
+    from oracle import capacitance_oracle as co
+    from oracle import ewald_oracle as ew
+    w = workload(n=n, seed=seed, grid=2)
+    h_target = 111.76927955 / 192.0
+    ng = int(round(w["box"][0] / h_target))
+    Ng = np.array([ng, ng, ng])
+    perp, para, rv = ew.default_table(w["xi"])
+    t0 = time.perf_counter()
+    geo = ew.Geometry(w["x"], w["eps"], w["box"], w["xi"], w["rc"], Ng, w["P"], perp, para, rv, 0.0)
+    phi = 4 * math.pi * n / (3 * float(np.prod(w["box"])))
+    guess = co.dilute_guess(w["eps"], phi, [1.0, 0, 0])
+    C, S, infos = co.capacitance_tensor(geo, guess, 1e-7, 30, 20)
+    dt = time.perf_counter() - t0
+    return n * 3 / dt, dt, f"N={n} RSA phi=0.3 beta=0.9, {ng}^3 grid (h as at N=1e5), P=10, 3 directions, " \
+                           f"float64 GMRES(30) to 1e-7, geometry included; {dt:.1f} s"
+
+
+def cpu_baseline(args):
+    v, dt, sample = cpu_sample(n=args.cpu_n)
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+            "note": "NumPy restatement of the reference Python path; its FFT and GMRES run on one core"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    nproc = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(nproc))
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(nproc))
+    w = workload(n=args.cpu_n, grid=2)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_sample(n=args.cpu_n)
+    vals, dts = [], []
+    sample = ""
+    for _ in range(max(1, args.steps)):
+        v, dt, sample = cpu_sample(n=args.cpu_n)
+        vals.append(v)
+        dts.append(dt)
+    value = float(np.mean(vals))
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": float(np.mean(dts)) * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded RSA)",
+           "impl": "reference",
+           "config": config_dict(w, {"parallelism": "host cores", "sample": sample}),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=100_000)
+    ap.add_argument("--grid", type=int, default=192)
+    ap.add_argument("--tol", type=float, default=1e-7)
+    ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--maxref", type=int, default=8)
+    ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
+    ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=3)
+    ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=2000)
+    ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

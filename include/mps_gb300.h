@@ -209,6 +209,23 @@ int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int
               const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
               mps_stream_t stream);
 
+/* ------------------------------------------------------------------------- */
+/* Diagnostics (no counterpart in the reference, which only prints timers at  */
+/* EW/capacitance.py:92-108, 367-394).                                         */
+/* ------------------------------------------------------------------------- */
+
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t mps_kernel_launches(void);
+
+/* enable != 0: every matvec records CUDA events around its stages (slab sum,
+ * spread, forward FFT, scale, inverse FFT, contract, real space). */
+int mps_system_profile(mps_system *sys, int32_t enable);
+
+/* Accumulated stage times since the last call (synchronises on the recorded
+ * events): ms[14] = [float64 stages 0..6, float32 stages 0..6] in milliseconds,
+ * count[2] = matvecs recorded per precision.  Resets the accumulators. */
+int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

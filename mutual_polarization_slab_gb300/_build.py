@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libmps_gb300.so")
+RSA_LIB = os.path.join(HERE, "librsa_host.so")
 BUILD = os.path.join(HERE, "_build")
 
 SOURCES = ["common.cu", "cells.cu", "realspace.cu", "grid.cu", "system.cu"]
@@ -44,6 +45,20 @@ def is_stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def build_host(verbose: bool = False) -> str:
+    """Host-only helpers (random sequential addition) compiled with the system C compiler."""
+    cc = os.environ.get("CC") or shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler found for librsa_host.so")
+    tmp = RSA_LIB + ".tmp"
+    cmd = [cc, "-O2", "-fPIC", "-shared", "-o", tmp, os.path.join(CSRC, "rsa_host.c"), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, RSA_LIB)
+    return RSA_LIB
+
+
 def build(verbose: bool = False, extra_flags=None) -> str:
     nvcc = nvcc_path()
     os.makedirs(BUILD, exist_ok=True)
@@ -67,6 +82,7 @@ def build(verbose: bool = False, extra_flags=None) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_host(verbose)
     return LIB
 
 

@@ -22,7 +22,8 @@ EXPORTS = (
     "mps_real_space_pairs_workspace", "mps_real_space_pairs_count", "mps_real_space_pairs_fill",
     "mps_real_space_fast", "mps_pre_calculations", "mps_grid_kernel", "mps_spread_fast", "mps_contract_fast",
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
-    "mps_matvec", "mps_matvec_complex", "mps_gmres",
+    "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
+    "mps_system_stage_times",
 )
 
 p = C.c_void_p
@@ -76,6 +77,9 @@ _SIGS = {
     "mps_matvec": (C.c_int, [p, p, p, i32, C.POINTER(i32), i32, p]),
     "mps_matvec_complex": (C.c_int, [p, p, p, i32, p]),
     "mps_gmres": (C.c_int, [p, p, p, p, i32, C.POINTER(i32), C.POINTER(SolveOpts), C.POINTER(SolveInfo), p]),
+    "mps_kernel_launches": (C.c_uint64, []),
+    "mps_system_profile": (C.c_int, [p, i32]),
+    "mps_system_stage_times": (C.c_int, [p, PD, P64]),
 }
 
 _lib = None

@@ -126,6 +126,23 @@ class SpectralEwaldSystem:
     def __exit__(self, *exc):
         self.close()
 
+    # -- diagnostics --------------------------------------------------------
+    STAGES = ("slab", "spread", "fft_fwd", "scale", "fft_inv", "contract", "real_space")
+
+    def profile(self, enable=True):
+        """Record CUDA events around every matvec stage from now on."""
+        L.check(self._lib.mps_system_profile(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        """{precision: (matvec count, {stage: total ms})} since the last call."""
+        ms = (C.c_double * 14)()
+        cnt = (C.c_int64 * 2)()
+        L.check(self._lib.mps_system_stage_times(self._h, ms, cnt))
+        out = {}
+        for p, name in ((0, "fp64"), (1, "fp32")):
+            out[name] = (int(cnt[p]), {s: float(ms[p * 7 + k]) for k, s in enumerate(self.STAGES)})
+        return out
+
     # -- operator ---------------------------------------------------------
     def _diag_arg(self, nrhs, diag_index):
         if diag_index is None:

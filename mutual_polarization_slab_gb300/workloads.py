@@ -20,52 +20,37 @@ def box_for_fraction(n_particles: int, phi: float, radius: float = 1.0) -> float
     return (4.0 * math.pi * n_particles * radius ** 3 / (3.0 * phi)) ** (1.0 / 3.0)
 
 
-def rsa(n: int, phi: float, seed: int, radii=None, batch: int = 64, max_rounds: int = 2000):
-    """Random sequential addition of spheres in a periodic cube.
+def _rsa_lib():
+    import ctypes as C
+    import os
+    from . import _build
+    if not os.path.exists(_build.RSA_LIB) or os.path.getmtime(_build.RSA_LIB) < os.path.getmtime(
+            os.path.join(_build.CSRC, "rsa_host.c")):
+        _build.build_host()
+    lib = C.CDLL(_build.RSA_LIB)
+    lib.mps_rsa.restype = C.c_int
+    lib.mps_rsa.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int64, C.c_void_p]
+    return lib
 
-    Particle ``i`` is placed at the first of ``batch`` uniformly drawn candidate
-    positions that overlaps no earlier sphere (contact at ``a_i + a_j``); the
-    check goes through a cell grid whose cell edge is at least the largest
-    contact distance.  Returns ``(x, box, radii)`` with ``x`` in ``[0, L)``.
+
+def rsa(n: int, phi: float, seed: int, radii=None, max_tries: int = 10_000_000):
+    """Random sequential addition of ``n`` spheres in a periodic cube at volume
+    fraction ``phi`` (host C routine ``mps_rsa`` in ``csrc/rsa_host.c``).
+
+    Sphere i takes ``radii[i]`` (default 1) and is placed at the first uniformly
+    drawn position overlapping no earlier sphere.  Returns ``(x, box, radii)``
+    with ``x`` in ``[0, L)``.
     """
-    rng = np.random.default_rng(seed)
-    radii = np.ones(n) if radii is None else np.asarray(radii, dtype=np.float64).reshape(n)
-    L = (4.0 * math.pi * float(np.sum(radii ** 3)) / (3.0 * phi)) ** (1.0 / 3.0)
-    nc = max(3, int(L // (2.0 * radii.max())))
-    cw = L / nc
-    cap = 24
-    grid = np.full((nc, nc, nc, cap), -1, dtype=np.int64)
-    fill = np.zeros((nc, nc, nc), dtype=np.int64)
+    import ctypes as C
+    rad = np.ones(n) if radii is None else np.ascontiguousarray(np.asarray(radii, dtype=np.float64).reshape(n))
+    L = (4.0 * math.pi * float(np.sum(rad ** 3)) / (3.0 * phi)) ** (1.0 / 3.0)
+    box = np.array([L, L, L])
     x = np.zeros((n, 3))
-    for i in range(n):
-        for _ in range(max_rounds):
-            cand = rng.random((batch, 3)) * L
-            ci = np.minimum((cand // cw).astype(np.int64), nc - 1)
-            nb = (ci[:, None, :] + _OFFS[None]) % nc
-            ids = grid[nb[..., 0], nb[..., 1], nb[..., 2]].reshape(batch, -1)
-            valid = ids >= 0
-            if not valid.any():
-                c = 0
-            else:
-                safe = np.where(valid, ids, 0)
-                d = cand[:, None, :] - x[safe]
-                d -= L * np.round(d / L)
-                bad = valid & (np.sum(d * d, axis=2) < (radii[safe] + radii[i]) ** 2)
-                okc = np.nonzero(~bad.any(axis=1))[0]
-                if okc.size == 0:
-                    continue
-                c = int(okc[0])
-            x[i] = cand[c]
-            cc = ci[c]
-            s = fill[cc[0], cc[1], cc[2]]
-            if s >= cap:
-                raise RuntimeError("RSA cell capacity exceeded")
-            grid[cc[0], cc[1], cc[2], s] = i
-            fill[cc[0], cc[1], cc[2]] = s + 1
-            break
-        else:
-            raise RuntimeError(f"RSA stalled at particle {i}/{n} (phi={phi})")
-    return x, np.array([L, L, L]), radii
+    rc = _rsa_lib().mps_rsa(n, rad.ctypes.data_as(C.c_void_p), box.ctypes.data_as(C.c_void_p), int(seed),
+                            int(max_tries), x.ctypes.data_as(C.c_void_p))
+    if rc != 0:
+        raise RuntimeError(f"RSA failed (code {rc}) for n={n}, phi={phi}")
+    return x, box, rad
 
 
 def bct_chain_lattice(ncx: int, ncy: int, ncz: int, vacancy: float, jitter: float, seed: int):
