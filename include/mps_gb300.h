@@ -42,7 +42,8 @@ enum mps_status {
     MPS_NOT_CONVERGED = 4,    /* GMRES hit maxit (the reference ignores its flag)   */
     MPS_CUDA_ERR = 5,
     MPS_CUFFT_ERR = 6,
-    MPS_NO_MEMORY = 7
+    MPS_NO_MEMORY = 7,
+    MPS_SCRATCH_LIMIT = 8     /* input or output larger than a fixed-size buffer  */
 };
 
 enum mps_precision {
@@ -208,6 +209,33 @@ typedef struct mps_solve_info {
 int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
               const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
               mps_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* Allocation-free neighbour list (no counterpart in the reference: its Python */
+/* allocates freely).  For callers that must not allocate device memory while */
+/* they run, e.g. a simulation engine that owns all device memory and calls a */
+/* field/force plugin every time step: cudaMalloc/cudaFree synchronise the    */
+/* device and may fail mid-run.                                              */
+/* ------------------------------------------------------------------------- */
+
+/* Size of the fixed device scratch array behind mps_neighbor_list_noalloc,
+ * resident on every GPU that loads the library until the process exits. */
+#define MPS_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* Same result as mps_neighbor_list_count + mps_neighbor_list_fill (the
+ * reference's candidate pairs, in its order) without any workspace argument and
+ * without allocating: the scratch is a fixed MPS_NOALLOC_SCRATCH_BYTES device
+ * array inside the library.  Inputs and outputs are still the caller's:
+ * cell (n x 3 int64), p1/p2 with room for max_pairs int64 each.  *n_pairs (host)
+ * receives the pair count.  Returns MPS_SCRATCH_LIMIT, before touching the GPU,
+ * when mps_neighbor_list_workspace(n, ncell) exceeds the scratch (roughly
+ * n > 32,000 particles), and MPS_SCRATCH_LIMIT with *n_pairs set when the pairs
+ * do not fit in max_pairs.  The first call on a device looks up that device's
+ * scratch address; make it before any stream capture.  All calls share the one
+ * array: calls whose GPU work overlaps race, so serialise them.  Synchronises
+ * the stream (the pair count is data dependent). */
+int mps_neighbor_list_noalloc(const int64_t *cell, int64_t n, const int64_t *ncell, int64_t *p1, int64_t *p2,
+                              int64_t max_pairs, int64_t *n_pairs, mps_stream_t stream);
 
 /* ------------------------------------------------------------------------- */
 /* Diagnostics (no counterpart in the reference, which only prints timers at  */

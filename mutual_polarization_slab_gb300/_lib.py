@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmps_gb300.so")
 
 MPS_OK, MPS_BAD_ARG, MPS_RC_GT_HALF_BOX, MPS_TABLE_RANGE, MPS_NOT_CONVERGED, MPS_CUDA_ERR, MPS_CUFFT_ERR, \
-    MPS_NO_MEMORY = range(8)
+    MPS_NO_MEMORY, MPS_SCRATCH_LIMIT = range(9)
+NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 MPS_FP64, MPS_FP32 = 0, 1
 
 EXPORTS = (
@@ -23,7 +24,7 @@ EXPORTS = (
     "mps_real_space_fast", "mps_pre_calculations", "mps_grid_kernel", "mps_spread_fast", "mps_contract_fast",
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
-    "mps_system_stage_times",
+    "mps_system_stage_times", "mps_neighbor_list_noalloc",
 )
 
 p = C.c_void_p
@@ -80,6 +81,7 @@ _SIGS = {
     "mps_kernel_launches": (C.c_uint64, []),
     "mps_system_profile": (C.c_int, [p, i32]),
     "mps_system_stage_times": (C.c_int, [p, PD, P64]),
+    "mps_neighbor_list_noalloc": (C.c_int, [p, i64, P64, p, p, i64, P64, p]),
 }
 
 _lib = None

@@ -143,6 +143,8 @@ extern "C" const char *mps_status_string(int status) {
         case MPS_CUDA_ERR: return mps::g_last_error[0] ? mps::g_last_error : "CUDA error";
         case MPS_CUFFT_ERR: return "cuFFT error";
         case MPS_NO_MEMORY: return "out of device memory";
+        case MPS_SCRATCH_LIMIT:
+            return "input exceeds the fixed no-allocation scratch, or the outputs are too small for the pair count";
         default: return "unknown status";
     }
 }
