@@ -192,6 +192,10 @@ typedef struct mps_solve_opts {
                                  inner GMRES on the fp32 operator                    */
     double inner_tol;         /* mixed: relative tolerance of each inner solve        */
     int32_t inner_maxit;      /* mixed: restart cycles of each inner solve            */
+    int32_t residual_policy;  /* mixed: 0 = one float64 residual, later residuals from
+                                 the inner GMRES's Arnoldi relation; 1 = a float64
+                                 residual after every correction                     */
+    int32_t verify;           /* mixed: != 0 ends with a float64 true residual        */
 } mps_solve_opts;
 
 typedef struct mps_solve_info {

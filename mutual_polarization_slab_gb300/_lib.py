@@ -46,7 +46,7 @@ class SystemDesc(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", f64), ("restart", i32), ("maxit", i32), ("precision", i32), ("inner_tol", f64),
-                ("inner_maxit", i32)]
+                ("inner_maxit", i32), ("residual_policy", i32), ("verify", i32)]
 
 
 class SolveInfo(C.Structure):

@@ -12,6 +12,7 @@
 
 #include "grid.cuh"
 #include "realspace.cuh"
+#include "tiles.cuh"
 
 using namespace mps;
 
@@ -75,6 +76,10 @@ struct mps_system {
     int32_t *diag_idx_host = nullptr;  // pinned mirror
     void *fft_work = nullptr;
     size_t fft_work_bytes = 0;
+    TileBins tb64, tb32;        // tile binning for the tiled spread/contract (per precision tile depth)
+    double *partial64 = nullptr;
+    float *partial32 = nullptr;
+    bool tiled = true;
     bool profile = false;
     std::vector<StageEvents> pending;
     std::vector<StageEvents> spare;
@@ -95,6 +100,10 @@ static void free_system(mps_system *s) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
+    tile_bins_free(s->tb64);
+    tile_bins_free(s->tb32);
+    if (s->partial64) cudaFree(s->partial64);
+    if (s->partial32) cudaFree(s->partial32);
     delete s;
 }
 
@@ -227,9 +236,34 @@ static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStrea
         if (ev) MPS_CUDA_TRY(cudaEventRecord(ev->ev[(k)], st));         \
     } while (0)
 
+// Tile depth per precision: float64 accumulators take twice the registers.
+static int tile_depth(bool dbl) { return dbl ? 4 : 8; }
+
+// Lazily bins the particles for the tiled kernels of one precision.
+static int ensure_tiles(mps_system *s, bool dbl, cudaStream_t st, bool *use) {
+    *use = false;
+    const int tz = tile_depth(dbl);
+    if (!s->tiled || !tiles_supported(s->gp, tz)) return MPS_OK;
+    TileBins &tb = dbl ? s->tb64 : s->tb32;
+    if (!tb.mem) {
+        MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
+        const size_t pbytes = (size_t)tb.nentries * 9 * (dbl ? sizeof(double) : sizeof(float));
+        if (dbl)
+            MPS_TRY(dalloc(&s->partial64, pbytes));
+        else
+            MPS_TRY(dalloc(&s->partial32, pbytes));
+    }
+    *use = true;
+    return MPS_OK;
+}
+
 template <typename T>
 static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     const bool dbl = sizeof(T) == 8;
+    bool use_tiles = false;
+    MPS_TRY(ensure_tiles(s, dbl, st, &use_tiles));
+    const TileBins &tb = dbl ? s->tb64 : s->tb32;
+    T *partial = dbl ? (T *)s->partial64 : (T *)s->partial32;
     MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32));
     T *grid = dbl ? (T *)s->grid64 : (T *)s->grid32;
     void *spec = dbl ? s->spec64 : s->spec32;
@@ -240,7 +274,10 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
     MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
     STAGE_MARK(1);
-    MPS_TRY(spread<T>(m, s->n, nrhs, s->start, w, s->gp, grid, st));
+    if (use_tiles)
+        MPS_TRY(spread_tiled<T>(m, s->n, nrhs, s->start, w, s->gp, tb, grid, st));
+    else
+        MPS_TRY(spread<T>(m, s->n, nrhs, s->start, w, s->gp, grid, st));
     STAGE_MARK(2);
     MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, 3 * nrhs, grid, spec, 0, st));
     STAGE_MARK(3);
@@ -248,7 +285,10 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     STAGE_MARK(4);
     MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 3 * nrhs, spec, grid, 0, st));
     STAGE_MARK(5);
-    MPS_TRY(contract<T>(grid, s->n, nrhs, s->start, w, s->gp, out, st));
+    if (use_tiles)
+        MPS_TRY(contract_tiled<T>(grid, s->n, nrhs, s->start, w, s->gp, tb, partial, out, st));
+    else
+        MPS_TRY(contract<T>(grid, s->n, nrhs, s->start, w, s->gp, out, st));
     STAGE_MARK(6);
     if (dbl)
         MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
@@ -380,6 +420,23 @@ __global__ void k_axpy1(const double *__restrict__ x, double *__restrict__ y, in
         y[i] += x[i];
 }
 
+// out_r = sum_{c <= kcount[r] + extra - 1} coef_r[c] V_r[c]   (overwrites)
+__global__ void k_combine_basis(const double *__restrict__ V, int64_t ldv, int64_t vstride,
+                                const double *__restrict__ coef, int64_t cstride, const int32_t *__restrict__ kcount,
+                                int extra, double *__restrict__ out, int64_t ostride, int64_t n3) {
+    __shared__ double cs_[kMaxCols + 1];
+    const int r = blockIdx.y;
+    const int k = kcount[r] + extra;
+    for (int c = threadIdx.x; c < k; c += blockDim.x) cs_[c] = coef[(int64_t)r * cstride + c];
+    __syncthreads();
+    const double *Vr = V + r * vstride;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int c = 0; c < k; ++c) acc += Vr[(int64_t)c * ldv + i] * cs_[c];
+        out[r * ostride + i] = acc;
+    }
+}
+
 struct GmresState {
     double *H;      // [r][(restart+1) * restart], column j at offset j*(restart+1)
     double *cs, *sn;  // [r][restart]
@@ -440,6 +497,24 @@ __global__ void k_arnoldi_givens(GmresState st, int restart, int j, int nrhs, co
     st.kcount[r] = j + 1;
 }
 
+// Coefficients u (length k+1) of the least-squares residual b - A x_k = V_{k+1} u:
+// u = G_0^T ... G_{k-1}^T (0, ..., 0, g_k), i.e. the Arnoldi relation, no matvec.
+__global__ void k_ls_residual_coeffs(GmresState st, int restart, int nrhs, double *__restrict__ u, int ustride) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrhs) return;
+    const int ld = restart + 1;
+    const int k = st.kcount[r];
+    double *ur = u + (int64_t)r * ustride;
+    for (int i = 0; i <= k; ++i) ur[i] = 0.0;
+    ur[k] = st.g[r * ld + k];
+    const double *cs = st.cs + r * restart, *sn = st.sn + r * restart;
+    for (int i = k - 1; i >= 0; --i) {
+        const double a = ur[i], b = ur[i + 1];
+        ur[i] = cs[i] * a - sn[i] * b;
+        ur[i + 1] = sn[i] * a + cs[i] * b;
+    }
+}
+
 // Back substitution H[:k,:k] y = g[:k].
 __global__ void k_backsolve(GmresState st, int restart, int nrhs) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -480,9 +555,16 @@ static int multidot(const double *V, int64_t ldv, int64_t vstride, int ncols, co
 // precision.  x holds the initial guess on entry and the solution on exit.
 // Basis layout V[j][r][i]: basis vector j of every system is one contiguous
 // nrhs x n3 block, which is exactly the batched matvec's input.
+struct GmresFlags {
+    bool zero_guess = false;   // x is zero on entry: the first residual is b itself (no matvec)
+    bool final_check = true;   // end with a true residual b - A x (one more matvec)
+    bool ls_restart = false;   // restart cycles start from the least-squares residual (Arnoldi relation)
+    double *r_out = nullptr;   // optional: final residual vectors (nrhs x n3)
+};
+
 static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, double tol, int restart, int maxit,
                       int precision, int *conv, double *relres_out, int *cycles_out, int *mv_count,
-                      cudaStream_t st) {
+                      cudaStream_t st, GmresFlags fl = GmresFlags()) {
     const int64_t n3 = 3 * s->n;
     const int ld = restart + 1;
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
@@ -498,6 +580,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     bytes += 2 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount frozen
     bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
     bytes += 256 + sizeof(double) * (size_t)nrhs * nblk * kMaxCols;   // partial
+    bytes += 256 + sizeof(double) * (size_t)nrhs * (kMaxCols + 1);    // u
     char *base = nullptr;
     MPS_CUDA_TRY(cudaMallocAsync((void **)&base, bytes, st));
     char *p = base;
@@ -518,6 +601,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     int32_t *frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
     S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
     double *partial = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * nblk * kMaxCols);
+    double *u = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * (kMaxCols + 1));
 
     std::vector<double> hres(nrhs);
     std::vector<int32_t> hfrozen(nrhs, 0);
@@ -552,12 +636,23 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     k_sqrt_copy<<<(nrhs + 31) / 32, 32, 0, st>>>(S.nrm2, S.bnorm, nrhs);
     GM_LAUNCH();
     for (int r = 0; r < nrhs; ++r) conv[r] = 0;
+    bool resid_ready = false;     // V[0] already holds b - A x (unnormalised)
+    bool at_start_exit = false;   // left the loop at a cycle start: V[0] is the residual
+    bool w_is_resid = false;      // w holds the least-squares residual of the last cycle
     for (cyc = 0; cyc < maxit; ++cyc) {
         // r0 = b - A x  -> V[0] (unnormalised)
-        GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
-        ++*mv_count;
-        k_sub<<<grid_for(ldv, 256), 256, 0, st>>>(b, w, V, ldv);
-        GM_LAUNCH();
+        if (!resid_ready) {
+            if (cyc == 0 && fl.zero_guess) {
+                GM_CUDA(cudaMemcpyAsync(V, b, sizeof(double) * ldv, cudaMemcpyDeviceToDevice, st));
+            } else {
+                GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
+                ++*mv_count;
+                k_sub<<<grid_for(ldv, 256), 256, 0, st>>>(b, w, V, ldv);
+                GM_LAUNCH();
+            }
+        }
+        resid_ready = false;
+        w_is_resid = false;
         GM_TRY(multidot(V, ldv, n3, 1, V, n3, n3, nrhs, partial, S.nrm2, 1, st));
         k_cycle_start<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs);
         GM_LAUNCH();
@@ -570,7 +665,10 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             hfrozen[r] = conv[r];
             all = all && conv[r];
         }
-        if (all) break;
+        if (all) {
+            at_start_exit = true;
+            break;
+        }
         GM_CUDA(cudaMemcpyAsync(frozen, hfrozen.data(), sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
         k_scale_vec<<<vgrid, 256, 0, st>>>(V, n3, V, n3, S.beta, 1, n3);
         GM_LAUNCH();
@@ -607,6 +705,39 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         GM_LAUNCH();
         k_add_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, S.y, restart, S.kcount, x, n3, n3);
         GM_LAUNCH();
+        for (int r = 0; r < nrhs; ++r) relres_out[r] = hres[r];
+        if (fl.ls_restart || (fl.r_out && cyc == maxit - 1)) {
+            k_ls_residual_coeffs<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs, u, kMaxCols + 1);
+            GM_LAUNCH();
+            k_combine_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, u, kMaxCols + 1, S.kcount, 1, w, n3, n3);
+            GM_LAUNCH();
+            w_is_resid = true;
+            if (fl.ls_restart && cyc + 1 < maxit) {
+                GM_CUDA(cudaMemcpyAsync(V, w, sizeof(double) * ldv, cudaMemcpyDeviceToDevice, st));
+                resid_ready = true;
+            }
+        }
+    }
+    if (fl.r_out) {
+        if (at_start_exit) {
+            GM_CUDA(cudaMemcpyAsync(fl.r_out, V, sizeof(double) * ldv, cudaMemcpyDeviceToDevice, st));
+        } else if (w_is_resid) {
+            GM_CUDA(cudaMemcpyAsync(fl.r_out, w, sizeof(double) * ldv, cudaMemcpyDeviceToDevice, st));
+        } else {
+            GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
+            ++*mv_count;
+            k_sub<<<grid_for(ldv, 256), 256, 0, st>>>(b, w, fl.r_out, ldv);
+            GM_LAUNCH();
+        }
+    }
+    if (!fl.final_check) {
+        for (int r = 0; r < nrhs; ++r) {
+            conv[r] = relres_out[r] <= tol;
+            if (!conv[r]) rc = MPS_NOT_CONVERGED;
+        }
+        *cycles_out = cyc;
+        cudaFreeAsync(base, st);
+        return rc;
     }
     // final true residual
     GM_TRY(matvec_any(s, x, w, nrhs, precision, st));
@@ -649,7 +780,27 @@ static int true_residual(mps_system *s, const double *b, const double *x, double
     return MPS_OK;
 }
 
-// Iterative refinement: x <- x + d with A32 d ~= b - A64 x solved by float32-operator GMRES.
+// Norms ||r_q|| / ||b_q|| for every system (host result).
+static int rel_norms(const double *r, const double *b, int64_t n3, int nrhs, double *partial, double *nrm,
+                     std::vector<double> &rel, cudaStream_t st) {
+    MPS_TRY(multidot(r, n3, n3, 1, r, n3, n3, nrhs, partial, nrm, 1, st));
+    MPS_TRY(multidot(b, n3, n3, 1, b, n3, n3, nrhs, partial, nrm + nrhs, 1, st));
+    std::vector<double> hn(2 * nrhs);
+    MPS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int q = 0; q < nrhs; ++q) rel[q] = hn[nrhs + q] > 0 ? sqrt(hn[q]) / sqrt(hn[nrhs + q]) : 0.0;
+    return MPS_OK;
+}
+
+// Mixed precision: float32-operator GMRES (float64 Arnoldi) for the solve and
+// every correction, float64 for the refinement residual.
+//   step 0: x1 = GMRES32(b, from x0)
+//   r = b - A64 x1                       (the one float64 matvec)
+//   repeat: d = GMRES32(r, from 0); x += d; r <- b - A32-consistent residual
+// With residual_policy 0 the residual after a correction is the inner GMRES's
+// least-squares residual (Arnoldi relation: r - A32 d = V_{k+1} u), exact up to
+// float32 rounding on the small correction d; with policy 1 every step
+// recomputes b - A64 x.  verify != 0 adds a final float64 true residual.
 static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, const mps_solve_opts *o, int *conv,
                         double *relres_out, int *cycles_out, int *mv64, int *mv32, cudaStream_t st) {
     const int64_t n3 = 3 * s->n;
@@ -657,22 +808,31 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
     const int inner_maxit = o->inner_maxit > 0 ? o->inner_maxit : 4;
+    const bool incremental = o->residual_policy == 0;
     double *buf = nullptr;
-    const size_t bytes = sizeof(double) * (3 * (size_t)tot + 2 * nrhs + (size_t)nrhs * nblk * kMaxCols);
+    const size_t bytes = sizeof(double) * (4 * (size_t)tot + 2 * nrhs + (size_t)nrhs * nblk * kMaxCols);
     MPS_CUDA_TRY(cudaMallocAsync((void **)&buf, bytes, st));
-    double *r = buf, *dx = buf + tot, *ax = buf + 2 * tot, *nrm = buf + 3 * tot, *partial = nrm + 2 * nrhs;
+    double *r = buf, *dx = buf + tot, *ax = buf + 2 * tot, *rn = buf + 3 * tot, *nrm = buf + 4 * tot,
+           *partial = nrm + 2 * nrhs;
     std::vector<double> rel(nrhs);
     std::vector<int> ic(nrhs);
     std::vector<double> ir(nrhs);
     int rc = MPS_NOT_CONVERGED;
     int step = 0;
-    for (step = 0;; ++step) {
-        int e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
+    int e = MPS_OK;
+    {
+        GmresFlags f0;
+        f0.final_check = false;
+        f0.ls_restart = true;
+        int icyc = 0;
+        e = gmres_core(s, b, x, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc, mv32,
+                       st, f0);
+    }
+    if (e == MPS_OK || e == MPS_NOT_CONVERGED) {
+        e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
         ++*mv64;
-        if (e) {
-            rc = e;
-            break;
-        }
+    }
+    for (step = 1; e == MPS_OK; ++step) {
         bool all = true;
         for (int q = 0; q < nrhs; ++q) {
             relres_out[q] = rel[q];
@@ -681,33 +841,58 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
             // a converged system gets a zero right-hand side: its correction stays zero
             if (conv[q] && cudaMemsetAsync(r + q * n3, 0, sizeof(double) * n3, st) != cudaSuccess) e = MPS_CUDA_ERR;
         }
-        if (e) {
-            rc = e;
-            break;
-        }
+        if (e) break;
         if (all) {
             rc = MPS_OK;
             break;
         }
-        if (step >= o->maxit) break;
+        if (step > o->maxit) break;
         if (cudaMemsetAsync(dx, 0, sizeof(double) * tot, st) != cudaSuccess) {
-            rc = MPS_CUDA_ERR;
+            e = MPS_CUDA_ERR;
             break;
         }
+        GmresFlags fl;
+        fl.zero_guess = true;
+        fl.final_check = false;
+        fl.ls_restart = true;
+        fl.r_out = incremental ? rn : nullptr;
         int icyc = 0;
-        e = gmres_core(s, r, dx, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
-                       mv32, st);
-        if (e != MPS_OK && e != MPS_NOT_CONVERGED) {
-            rc = e;
+        int g = gmres_core(s, r, dx, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
+                           mv32, st, fl);
+        if (g != MPS_OK && g != MPS_NOT_CONVERGED) {
+            e = g;
             break;
         }
         k_axpy1<<<grid_for(tot, 256), 256, 0, st>>>(dx, x, tot);
         count_launch();
         if (cudaGetLastError() != cudaSuccess) {
-            rc = MPS_CUDA_ERR;
+            e = MPS_CUDA_ERR;
             break;
         }
+        if (incremental) {
+            if (cudaMemcpyAsync(r, rn, sizeof(double) * tot, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+                e = MPS_CUDA_ERR;
+                break;
+            }
+            e = rel_norms(r, b, n3, nrhs, partial, nrm, rel, st);
+        } else {
+            e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
+            ++*mv64;
+        }
     }
+    if (e == MPS_OK && o->verify) {
+        e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
+        ++*mv64;
+        if (e == MPS_OK) {
+            rc = MPS_OK;
+            for (int q = 0; q < nrhs; ++q) {
+                relres_out[q] = rel[q];
+                conv[q] = rel[q] <= o->tol;
+                if (!conv[q]) rc = MPS_NOT_CONVERGED;
+            }
+        }
+    }
+    if (e != MPS_OK) rc = e;
     *cycles_out = step;
     cudaFreeAsync(buf, st);
     return rc;

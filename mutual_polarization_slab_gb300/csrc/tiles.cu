@@ -1,0 +1,467 @@
+// Tiled spread (K4) and contract (K6).
+//
+// The grid is cut into 16 x 16 x TZ tiles, one CTA per tile.  Every particle is
+// binned (counting sort, ids ascending inside a tile) into each tile its P^3
+// stencil touches.
+//   spread:   thread (tx,ty) owns the TZ nodes of its column and accumulates
+//             them in registers over the tile's particles, then writes them
+//             once -- every grid node is written by exactly one thread, so no
+//             atomics and no zero-fill, and the summation order is fixed.
+//   contract: the CTA stages its grid tile in shared memory; one warp per
+//             (particle, tile) entry sums the stencil nodes inside the tile
+//             into a partial; a gather kernel adds each particle's partials in
+//             a fixed order.
+// Both produce the same sums as the reference's per-particle loops
+// (EW/ewald.py:370-467) up to summation order.
+#include "tiles.cuh"
+
+namespace mps {
+
+constexpr int kMaxTileList = 8;  // distinct tiles per axis touched by one stencil (ceil((P-1)/T)+2)
+constexpr int kChunk = 32;       // particles staged per spread iteration
+
+bool tiles_supported(const GridParams &gp, int tz) {
+    if (gp.P > kMaxP || gp.P < 1) return false;
+    if (gp.N[0] < kTileX || gp.N[1] < kTileY || gp.N[2] < tz) return false;
+    if ((gp.P - 1 + tz - 1) / tz + 2 > kMaxTileList) return false;
+    return true;
+}
+
+// Distinct tiles of one axis touched by indices (s + j) mod N, j < P, in order of first touch.
+__device__ __forceinline__ int axis_tiles(int s, int P, int N, int T, int *out) {
+    int cnt = 0;
+    for (int j = 0; j < P; ++j) {
+        int idx = s + j;
+        if (idx >= N) idx -= N;
+        const int t = idx / T;
+        bool seen = false;
+        for (int k = 0; k < cnt; ++k) seen |= (out[k] == t);
+        if (!seen) out[cnt++] = t;
+    }
+    return cnt;
+}
+
+struct TileGeom {
+    int N[3];
+    int T[3];
+    int nt[3];
+    int P;
+};
+
+__global__ void k_tile_count(const int32_t *__restrict__ start, int64_t n, TileGeom tg, int32_t *__restrict__ tcount,
+                             int64_t *__restrict__ pcount) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        int L[3][kMaxTileList];
+        int c[3];
+        for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * a + d], tg.P, tg.N[d], tg.T[d], L[d]);
+        for (int iz = 0; iz < c[2]; ++iz)
+            for (int iy = 0; iy < c[1]; ++iy)
+                for (int ix = 0; ix < c[0]; ++ix)
+                    atomicAdd(&tcount[((int64_t)L[2][iz] * tg.nt[1] + L[1][iy]) * tg.nt[0] + L[0][ix]], 1);
+        pcount[a] = (int64_t)c[0] * c[1] * c[2];
+    }
+}
+
+__global__ void k_tile_fill(const int32_t *__restrict__ start, int64_t n, TileGeom tg,
+                            const int64_t *__restrict__ tstart, int32_t *__restrict__ cursor,
+                            int32_t *__restrict__ unsorted) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        int L[3][kMaxTileList];
+        int c[3];
+        for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * a + d], tg.P, tg.N[d], tg.T[d], L[d]);
+        for (int iz = 0; iz < c[2]; ++iz)
+            for (int iy = 0; iy < c[1]; ++iy)
+                for (int ix = 0; ix < c[0]; ++ix) {
+                    const int64_t t = ((int64_t)L[2][iz] * tg.nt[1] + L[1][iy]) * tg.nt[0] + L[0][ix];
+                    unsorted[tstart[t] + atomicAdd(&cursor[t], 1)] = (int32_t)a;
+                }
+    }
+}
+
+// One warp per tile: order the tile's particles by id and record, for each
+// particle, where its entry for this tile landed.
+__global__ void k_tile_rank(const int32_t *__restrict__ unsorted, const int64_t *__restrict__ tstart, int64_t ntiles,
+                            const int32_t *__restrict__ start, TileGeom tg, const int64_t *__restrict__ pstart,
+                            int32_t *__restrict__ entries, int32_t *__restrict__ pentry) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = warp; t < ntiles; t += nw) {
+        const int64_t s0 = tstart[t];
+        const int len = (int)(tstart[t + 1] - s0);
+        const int tx = (int)(t % tg.nt[0]), ty = (int)((t / tg.nt[0]) % tg.nt[1]),
+                  tzi = (int)(t / ((int64_t)tg.nt[0] * tg.nt[1]));
+        for (int e = lane; e < len; e += 32) {
+            const int32_t v = unsorted[s0 + e];
+            int rank = 0;
+            for (int j = 0; j < len; ++j) rank += (unsorted[s0 + j] < v);
+            entries[s0 + rank] = v;
+            int L[3][kMaxTileList];
+            int c[3];
+            for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * (int64_t)v + d], tg.P, tg.N[d], tg.T[d], L[d]);
+            int ix = 0, iy = 0, iz = 0;
+            while (ix < c[0] && L[0][ix] != tx) ++ix;
+            while (iy < c[1] && L[1][iy] != ty) ++iy;
+            while (iz < c[2] && L[2][iz] != tzi) ++iz;
+            pentry[pstart[v] + ((int64_t)iz * c[1] + iy) * c[0] + ix] = (int32_t)(s0 + rank);
+        }
+    }
+}
+
+static char *carve_t(char *&p, size_t bytes) {
+    uintptr_t u = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+    p = (char *)(u + bytes);
+    return (char *)u;
+}
+
+int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s) {
+    tile_bins_free(tb);
+    if (!tiles_supported(gp, tz)) return MPS_BAD_ARG;
+    TileGeom tg;
+    tg.P = gp.P;
+    tg.T[0] = kTileX;
+    tg.T[1] = kTileY;
+    tg.T[2] = tz;
+    for (int d = 0; d < 3; ++d) {
+        tg.N[d] = gp.N[d];
+        tg.nt[d] = (gp.N[d] + tg.T[d] - 1) / tg.T[d];
+    }
+    tb.tz = tz;
+    tb.ntx = tg.nt[0];
+    tb.nty = tg.nt[1];
+    tb.ntz = tg.nt[2];
+    tb.ntiles = (int64_t)tg.nt[0] * tg.nt[1] * tg.nt[2];
+    const int64_t T = tb.ntiles;
+    // temporaries
+    int32_t *tcount = nullptr, *cursor = nullptr, *unsorted = nullptr;
+    int64_t *pcount = nullptr;
+    void *scan_tmp = nullptr;
+    size_t tmp_bytes = 256 * 5 + (size_t)T * 4 * 2 + (size_t)n * 8 + scan_workspace(std::max(T, n) + 1);
+    char *tmp = nullptr;
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, tmp_bytes, s));
+    char *p = tmp;
+    tcount = (int32_t *)carve_t(p, (size_t)T * 4);
+    cursor = (int32_t *)carve_t(p, (size_t)T * 4);
+    pcount = (int64_t *)carve_t(p, (size_t)n * 8);
+    scan_tmp = carve_t(p, scan_workspace(std::max(T, n) + 1));
+    MPS_CUDA_TRY(cudaMemsetAsync(tcount, 0, (size_t)T * 4, s));
+    MPS_CUDA_TRY(cudaMemsetAsync(cursor, 0, (size_t)T * 4, s));
+    k_tile_count<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tcount, pcount);
+    MPS_LAUNCH_CHECK();
+    // sizes: total entries
+    int64_t *tstart_tmp = nullptr, *pstart_tmp = nullptr;
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&tstart_tmp, (size_t)(T + 1) * 8, s));
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&pstart_tmp, (size_t)(n + 1) * 8, s));
+    int r = exclusive_scan_i32_to_i64(tcount, tstart_tmp, T, scan_tmp, s);
+    if (r) return r;
+    r = exclusive_scan_i64(pcount, pstart_tmp, n, scan_tmp, s);
+    if (r) return r;
+    int64_t last_t, last_c, last_p, last_pc;
+    int32_t lc;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last_t, tstart_tmp + T - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&lc, tcount + T - 1, 4, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last_p, pstart_tmp + n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last_pc, pcount + n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    last_c = lc;
+    const int64_t E = last_t + last_c;
+    tb.nentries = E;
+    (void)last_pc;
+    // persistent arrays
+    size_t bytes = 256 * 5 + (size_t)(T + 1) * 8 + (size_t)E * 4 + (size_t)(n + 1) * 8 + (size_t)E * 4 +
+                   (size_t)E * 4;
+    MPS_CUDA_TRY(cudaMalloc(&tb.mem, bytes));
+    p = (char *)tb.mem;
+    tb.tile_start = (int64_t *)carve_t(p, (size_t)(T + 1) * 8);
+    tb.entries = (int32_t *)carve_t(p, (size_t)E * 4);
+    tb.pstart = (int64_t *)carve_t(p, (size_t)(n + 1) * 8);
+    tb.pentry = (int32_t *)carve_t(p, (size_t)E * 4);
+    unsorted = (int32_t *)carve_t(p, (size_t)E * 4);
+    MPS_CUDA_TRY(cudaMemcpyAsync(tb.tile_start, tstart_tmp, (size_t)T * 8, cudaMemcpyDeviceToDevice, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(tb.tile_start + T, &E, 8, cudaMemcpyHostToDevice, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(tb.pstart, pstart_tmp, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(tb.pstart + n, &E, 8, cudaMemcpyHostToDevice, s));
+    k_tile_fill<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tb.tile_start, cursor, unsorted);
+    MPS_LAUNCH_CHECK();
+    k_tile_rank<<<grid_for(T * 32, 256), 256, 0, s>>>(unsorted, tb.tile_start, T, start, tg, tb.pstart, tb.entries,
+                                                      tb.pentry);
+    MPS_LAUNCH_CHECK();
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));  // host scalars above must outlive the copies
+    cudaFreeAsync(tstart_tmp, s);
+    cudaFreeAsync(pstart_tmp, s);
+    cudaFreeAsync(tmp, s);
+    return MPS_OK;
+}
+
+void tile_bins_free(TileBins &tb) {
+    if (tb.mem) cudaFree(tb.mem);
+    tb = TileBins();
+}
+
+// ---------------------------------------------------------------------------
+// Spread
+// ---------------------------------------------------------------------------
+template <typename T, int TZ, int NR>
+__global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__ m, int64_t n, int r0,
+                                                      const int32_t *__restrict__ start, const T *__restrict__ w,
+                                                      GridParams gp, const int64_t *__restrict__ tstart,
+                                                      const int32_t *__restrict__ entries, int ntx, int nty,
+                                                      T *__restrict__ grid) {
+    constexpr int C = 3 * NR;
+    __shared__ int3 s_off[kChunk];
+    __shared__ T s_w[kChunk][3 * kMaxP];
+    __shared__ T s_m[kChunk][C];
+    const int64_t t = blockIdx.x;
+    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
+    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
+    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    T acc[TZ][C];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[z][c] = (T)0;
+    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
+    for (int64_t cb = e0; cb < e1; cb += kChunk) {
+        const int cnt = (int)min((int64_t)kChunk, e1 - cb);
+        if (threadIdx.x < cnt) {
+            const int32_t a = entries[cb + threadIdx.x];
+            int ox = X0 - start[3 * a], oy = Y0 - start[3 * a + 1], oz = Z0 - start[3 * a + 2];
+            if (ox < 0) ox += Nx;
+            if (oy < 0) oy += Ny;
+            if (oz < 0) oz += Nz;
+            s_off[threadIdx.x] = make_int3(ox, oy, oz);
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const double *ma = m + ((int64_t)(r0 + r) * n + a) * 3;
+                s_m[threadIdx.x][3 * r + 0] = (T)ma[0];
+                s_m[threadIdx.x][3 * r + 1] = (T)ma[1];
+                s_m[threadIdx.x][3 * r + 2] = (T)ma[2];
+            }
+        }
+        for (int q = threadIdx.x; q < cnt * 3 * P; q += blockDim.x) {
+            const int pp = q / (3 * P), k = q % (3 * P);
+            const int32_t a = entries[cb + pp];
+            s_w[pp][(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+        }
+        __syncthreads();
+        for (int pp = 0; pp < cnt; ++pp) {
+            const int3 o = s_off[pp];
+            int dx = o.x + tx;
+            if (dx >= Nx) dx -= Nx;
+            int dy = o.y + ty;
+            if (dy >= Ny) dy -= Ny;
+            if (dx < P && dy < P) {
+                const T wxy = s_w[pp][dx] * s_w[pp][kMaxP + dy];
+                T mv[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) mv[c] = s_m[pp][c];
+#pragma unroll
+                for (int z = 0; z < TZ; ++z) {
+                    int dz = o.z + z;
+                    if (dz >= Nz) dz -= Nz;
+                    if (dz < P) {
+                        const T wv = wxy * s_w[pp][2 * kMaxP + dz];
+#pragma unroll
+                        for (int c = 0; c < C; ++c) acc[z][c] += wv * mv[c];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    const int gx = X0 + tx, gy = Y0 + ty;
+    if (gx < Nx && gy < Ny) {
+        const int64_t G = gp.G;
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            const int gz = Z0 + z;
+            if (gz < Nz) {
+                const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
+#pragma unroll
+                for (int c = 0; c < C; ++c) grid[(int64_t)(3 * r0 + c) * G + node] = acc[z][c];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Contract
+// ---------------------------------------------------------------------------
+template <typename T, int TZ, int NR>
+__global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ grid, int r0,
+                                                        const int32_t *__restrict__ start, const T *__restrict__ w,
+                                                        GridParams gp, const int64_t *__restrict__ tstart,
+                                                        const int32_t *__restrict__ entries, int ntx, int nty,
+                                                        T *__restrict__ partial) {
+    constexpr int C = 3 * NR;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tile = (T *)smem_raw;                                  // [C][TZ][16][16]
+    T *wbuf = tile + C * TZ * kTileX * kTileY;                // [8 warps][3*kMaxP]
+    const int64_t t = blockIdx.x;
+    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
+    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
+    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int64_t G = gp.G;
+    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
+    if (e0 == e1) return;
+    {
+        const int gx = X0 + tx, gy = Y0 + ty;
+        const bool in = gx < Nx && gy < Ny;
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            const int gz = Z0 + z;
+            const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                tile[((c * TZ + z) * kTileY + ty) * kTileX + tx] =
+                    (in && gz < Nz) ? grid[(int64_t)(3 * r0 + c) * G + node] : (T)0;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T *wb = wbuf + wid * 3 * kMaxP;
+    for (int64_t e = e0 + wid; e < e1; e += 8) {
+        const int32_t a = entries[e];
+        int ox = X0 - start[3 * a], oy = Y0 - start[3 * a + 1], oz = Z0 - start[3 * a + 2];
+        if (ox < 0) ox += Nx;
+        if (oy < 0) oy += Ny;
+        if (oz < 0) oz += Nz;
+        for (int k = lane; k < 3 * P; k += 32) wb[(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+        __syncwarp();
+        T acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = (T)0;
+        for (int idx = lane; idx < P * P; idx += 32) {
+            const int jx = idx % P, jy = idx / P;
+            int xr = jx - ox;
+            if (xr < 0) xr += Nx;
+            int yr = jy - oy;
+            if (yr < 0) yr += Ny;
+            if (xr < kTileX && yr < kTileY) {
+                const T wxy = wb[jx] * wb[kMaxP + jy];
+                for (int jz = 0; jz < P; ++jz) {
+                    int zr = jz - oz;
+                    if (zr < 0) zr += Nz;
+                    if (zr < TZ) {
+                        const T wv = wxy * wb[2 * kMaxP + jz];
+                        const T *tp = tile + (zr * kTileY + yr) * kTileX + xr;
+#pragma unroll
+                        for (int c = 0; c < C; ++c) acc[c] += wv * tp[c * TZ * kTileX * kTileY];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < C; ++c) partial[e * C + c] = acc[c];
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T, int NR>
+__global__ void k_contract_gather(const T *__restrict__ partial, int64_t n, int r0, const int64_t *__restrict__ pstart,
+                                  const int32_t *__restrict__ pentry, double hprod, double *__restrict__ out) {
+    constexpr int C = 3 * NR;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        double acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = 0.0;
+        for (int64_t k = pstart[a]; k < pstart[a + 1]; ++k) {
+            const T *pp = partial + (int64_t)pentry[k] * C;
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[c] += (double)pp[c];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) out[((int64_t)(r0 + r) * n + a) * 3 + c] = acc[3 * r + c] * hprod;
+    }
+}
+
+template <typename T, int TZ, int NR>
+static int spread_launch(const double *m, int64_t n, int r0, const int32_t *start, const T *w, const GridParams &gp,
+                         const TileBins &tb, T *grid, cudaStream_t s) {
+    k_spread_tiled<T, TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, gp, tb.tile_start, tb.entries,
+                                                                   tb.ntx, tb.nty, grid);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+template <typename T, int TZ>
+static int spread_dispatch(const double *m, int64_t n, int nrhs, const int32_t *start, const T *w,
+                           const GridParams &gp, const TileBins &tb, T *grid, cudaStream_t s) {
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        int rc = nr == 3 ? spread_launch<T, TZ, 3>(m, n, r0, start, w, gp, tb, grid, s)
+                 : nr == 2 ? spread_launch<T, TZ, 2>(m, n, r0, start, w, gp, tb, grid, s)
+                           : spread_launch<T, TZ, 1>(m, n, r0, start, w, gp, tb, grid, s);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+template <typename T>
+int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
+                 const TileBins &tb, T *grid, cudaStream_t s) {
+    if (tb.tz == 8) return spread_dispatch<T, 8>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 4) return spread_dispatch<T, 4>(m, n, nrhs, start, w, gp, tb, grid, s);
+    return MPS_BAD_ARG;
+}
+
+template <typename T, int TZ, int NR>
+static int contract_launch(const T *grid, int64_t n, int r0, const int32_t *start, const T *w, const GridParams &gp,
+                           const TileBins &tb, T *partial, double *out, cudaStream_t s) {
+    constexpr int C = 3 * NR;
+    const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileX * kTileY + 8 * 3 * kMaxP);
+    static bool attr_set = false;  // one attribute call per instantiation
+    if (!attr_set) {
+        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        attr_set = true;
+    }
+    k_contract_tiled<T, TZ, NR><<<(unsigned)tb.ntiles, 256, smem, s>>>(grid, r0, start, w, gp, tb.tile_start,
+                                                                       tb.entries, tb.ntx, tb.nty, partial);
+    MPS_LAUNCH_CHECK();
+    k_contract_gather<T, NR><<<grid_for(n, 256), 256, 0, s>>>(partial, n, r0, tb.pstart, tb.pentry, gp.hprod, out);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+template <typename T, int TZ>
+static int contract_dispatch(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w,
+                             const GridParams &gp, const TileBins &tb, T *partial, double *out, cudaStream_t s) {
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        int rc = nr == 3 ? contract_launch<T, TZ, 3>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                 : nr == 2 ? contract_launch<T, TZ, 2>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                           : contract_launch<T, TZ, 1>(grid, n, r0, start, w, gp, tb, partial, out, s);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+template <typename T>
+int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
+                   const TileBins &tb, T *partial, double *out, cudaStream_t s) {
+    if (tb.tz == 8) return contract_dispatch<T, 8>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 4) return contract_dispatch<T, 4>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    return MPS_BAD_ARG;
+}
+
+template int spread_tiled<float>(const double *, int64_t, int, const int32_t *, const float *, const GridParams &,
+                                 const TileBins &, float *, cudaStream_t);
+template int spread_tiled<double>(const double *, int64_t, int, const int32_t *, const double *, const GridParams &,
+                                  const TileBins &, double *, cudaStream_t);
+template int contract_tiled<float>(const float *, int64_t, int, const int32_t *, const float *, const GridParams &,
+                                   const TileBins &, float *, double *, cudaStream_t);
+template int contract_tiled<double>(const double *, int64_t, int, const int32_t *, const double *,
+                                    const GridParams &, const TileBins &, double *, double *, cudaStream_t);
+
+}  // namespace mps

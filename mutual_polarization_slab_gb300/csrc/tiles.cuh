@@ -1,0 +1,40 @@
+// Tile binning of particles and the tiled spread / contract kernels.
+#pragma once
+
+#include "grid.cuh"
+
+namespace mps {
+
+constexpr int kTileX = 16;
+constexpr int kTileY = 16;
+constexpr int kMaxP = 16;       // largest support handled by the tiled kernels
+constexpr int kMaxTilesPerDim = 4;
+
+// Particles binned into every grid tile their P^3 stencil touches.
+struct TileBins {
+    int tz = 0;                 // tile depth (z)
+    int ntx = 0, nty = 0, ntz = 0;
+    int64_t ntiles = 0;
+    int64_t nentries = 0;
+    int64_t *tile_start = nullptr;   // ntiles + 1
+    int32_t *entries = nullptr;      // particle id per (tile, particle) entry, tiles in order, ids ascending
+    int64_t *pstart = nullptr;       // n + 1: each particle's entries ...
+    int32_t *pentry = nullptr;       // ... listed here (entry indices), in the particle's tile order
+    void *mem = nullptr;             // single allocation backing the arrays above
+};
+
+bool tiles_supported(const GridParams &gp, int tz);
+int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s);
+void tile_bins_free(TileBins &tb);
+
+// grid[(r*3+c)][G] for r < nrhs, written completely (no zeroing needed).
+template <typename T>
+int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
+                 const TileBins &tb, T *grid, cudaStream_t s);
+
+// out[r][a][c] = hprod * sum over the stencil (overwrites); partial: nentries * 3 * min(nrhs,3) of T.
+template <typename T>
+int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
+                   const TileBins &tb, T *partial, double *out, cudaStream_t s);
+
+}  // namespace mps

@@ -175,7 +175,7 @@ class SpectralEwaldSystem:
         return torch.complex(out[0], out[1])
 
     def solve(self, b, x0=None, tol=1e-8, restart=30, maxit=100, precision="fp64", inner_tol=1e-4,
-              inner_maxit=4, diag_index=None, raise_on_fail=False):
+              inner_maxit=4, diag_index=None, raise_on_fail=False, residual_policy=0, verify=False):
         """GMRES (``precision='fp64'``) or float64 iterative refinement around a
         float32-operator GMRES (``'mixed'``) for R right-hand sides at once.
 
@@ -187,7 +187,8 @@ class SpectralEwaldSystem:
         x = torch.empty_like(b)
         x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, 3).contiguous()
         opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
-                           precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit))
+                           precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit),
+                           residual_policy=int(residual_policy), verify=1 if verify else 0)
         info = (L.SolveInfo * nrhs)()
         st = self._lib.mps_gmres(self._h, L.dptr(b), L.dptr(x0d) if x0d is not None else C.c_void_p(0), L.dptr(x),
                                  nrhs, self._diag_arg(nrhs, diag_index), C.byref(opts), info, L.stream_handle())

@@ -202,6 +202,24 @@ def test_system_matvec_fp64_fp32(golden_small, golden_c1, case):
             assert _rel(s.matvec(g["m_real"]).cpu().numpy(), g["H_real"].real) < 1e-12
 
 
+def test_tiled_kernels_odd_noncubic_grid():
+    """Partial tiles in every axis, odd axes (no Nyquist bin) and one even axis, P < tile depth mix."""
+    x, box, _ = rsa(400, 0.15, seed=8)
+    xi, rc, P = 0.7, 5.0, 8
+    Ng = np.array([25, 17, 12])
+    eps = np.where(np.arange(400) % 3 == 0, 28.0, 3.0)
+    perp, para, rv = ew.default_table(xi)
+    geo = ew.Geometry(x, eps, box, xi, rc, Ng, P, perp, para, rv, 0.5)
+    m = np.random.default_rng(4).normal(size=(3, 400, 3))
+    ref = np.stack([geo.field_real(mi) for mi in m])
+    with SpectralEwaldSystem(x, eps, box, xi, rc, Ng, P, perp, para, rv, slab_factor=0.5, max_rhs=3) as s:
+        for r in (1, 2, 3):
+            assert _rel(s.matvec(m[:r]).cpu().numpy(), ref[:r]) < 1e-12
+            assert _rel(s.matvec(m[:r], precision="fp32").cpu().numpy(), ref[:r]) < 2e-5
+        again = s.matvec(m).cpu().numpy()
+        assert np.array_equal(again, s.matvec(m).cpu().numpy())   # deterministic summation order
+
+
 # ---------------------------------------------------------------- solves
 def test_run_capacitance_matches_reference(golden_small):
     g = golden_small
@@ -251,14 +269,19 @@ def test_mixed_precision_accuracy(golden_c1):
     with SpectralEwaldSystem(g["x"], g["eps"], g["box"], float(g["xi"]), float(g["rc"]), g["Ngrid"], int(g["P"]),
                              perp, para, rv, slab_factor=0.0, max_rhs=3) as s:
         x64, i64 = s.solve(b, tol=1e-11, restart=30, maxit=50)
-        xm, im = s.solve(b, tol=1e-8, restart=30, maxit=10, precision="mixed", inner_tol=1e-4)
+        runs = [s.solve(b, tol=1e-8, restart=30, maxit=10, precision="mixed", inner_tol=1e-4, residual_policy=pol,
+                        verify=True) for pol in (0, 1)]
     x64 = x64.cpu().numpy()
-    xm = xm.cpu().numpy()
-    assert all(i.converged for i in i64) and all(i.converged for i in im)
-    for r in range(3):
-        err = np.linalg.norm(xm[r] - x64[r]) / np.linalg.norm(x64[r])
-        assert err < 1e-6, err
-    assert im[0].matvecs_fp32 > im[0].matvecs_fp64
+    assert all(i.converged for i in i64)
+    for xm, im in runs:
+        xm = xm.cpu().numpy()
+        assert all(i.converged for i in im)            # verified with a float64 true residual
+        for r in range(3):
+            err = np.linalg.norm(xm[r] - x64[r]) / np.linalg.norm(x64[r])
+            assert err < 1e-6, err
+        assert im[0].matvecs_fp32 > im[0].matvecs_fp64
+    # policy 0: one float64 residual + the verification
+    assert runs[0][1][0].matvecs_fp64 == 2
 
 
 def test_contrast_batch_diag_index(golden_small):
