@@ -24,7 +24,7 @@ EXPORTS = (
     "mps_real_space_fast", "mps_pre_calculations", "mps_grid_kernel", "mps_spread_fast", "mps_contract_fast",
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
-    "mps_system_stage_times", "mps_neighbor_list_noalloc",
+    "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
 )
 
 p = C.c_void_p
@@ -82,6 +82,7 @@ _SIGS = {
     "mps_system_profile": (C.c_int, [p, i32]),
     "mps_system_stage_times": (C.c_int, [p, PD, P64]),
     "mps_neighbor_list_noalloc": (C.c_int, [p, i64, P64, p, p, i64, P64, p]),
+    "mps_system_tuning": (C.c_int, [p, C.POINTER(i32), C.POINTER(C.c_float)]),
 }
 
 _lib = None

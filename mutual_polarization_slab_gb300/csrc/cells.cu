@@ -7,6 +7,8 @@
 // index, 27 neighbour cells with the x offset outermost, home particle, then
 // neighbour particle, both by increasing id).  Floating-point pair data use
 // explicitly rounded operations (no FMA contraction) so they match numpy's.
+#include <string.h>
+
 #include "cells.cuh"
 
 namespace mps {
@@ -163,11 +165,33 @@ __device__ __forceinline__ int64_t search_left(const double *__restrict__ rv, in
     return lo;
 }
 
+// Same index as search_left, starting from the uniform-spacing guess d * inv_dr
+// (inv_dr = (ntab-1)/rv[ntab-1]); falls back to the binary search when the
+// table is far from uniform.
+__device__ __forceinline__ int64_t search_left_guess(const double *__restrict__ rv, int64_t n, double d,
+                                                     double inv_dr) {
+    if (!(inv_dr > 0)) return search_left(rv, n, d);
+    double gf = d * inv_dr;
+    int64_t g = gf < 0 ? 0 : (gf > (double)(n - 1) ? n - 1 : (int64_t)gf);
+    for (int it = 0; it < 8; ++it) {
+        if (g < n && rv[g] < d) {
+            ++g;
+            continue;
+        }
+        if (g > 0 && rv[g - 1] >= d) {
+            --g;
+            continue;
+        }
+        return g;
+    }
+    return search_left(rv, n, d);
+}
+
 // Interpolated couplings at separation d; returns false when d is outside the table.
 __device__ __forceinline__ bool table_lerp(const double *__restrict__ perp, const double *__restrict__ para,
                                            const double *__restrict__ rv, int64_t ntab, double d, double *A,
-                                           double *B) {
-    int64_t i = search_left(rv, ntab, d);
+                                           double *B, double inv_dr = 0.0) {
+    int64_t i = search_left_guess(rv, ntab, d, inv_dr);
     if (i <= 0 || i >= ntab) return false;
     double rl = rv[i - 1], rh = rv[i];
     double t = __ddiv_rn(__dsub_rn(d, rl), __dsub_rn(rh, rl));
@@ -214,26 +238,94 @@ __global__ void k_pair_fill(const double *__restrict__ x, double Lx, double Ly, 
     }
 }
 
-// Filtered per-particle neighbour counts, slot (a, o) at a*27 + o.
-__global__ void k_csr_count(const double *__restrict__ x, double Lx, double Ly, double Lz,
-                            const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
-                            const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
-                            int64_t ncx, int64_t ncy, int64_t ncz, double rc, int64_t *__restrict__ cnt27) {
-    const double L[3] = {Lx, Ly, Lz};
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t s = t / 27;
-        int o = (int)(t % 27);
-        int32_t a = sorted[s];
-        int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
-        int64_t b0 = starts[nb], len = counts[nb];
+// Cutoff test of the solver's pair list.  A float32 screen on float32 copies
+// of the positions sorts candidates into clearly outside / clearly inside /
+// near rc (margins bound the float32 rounding); only pairs near rc (and, in
+// the fill pass, kept pairs) touch float64, which is scarce on GB300.  The kept
+// set is exactly the reference's d < rc set: the float64 path below does the
+// reference's operations (r - L trunc(2r/L) by comparisons, which give the same
+// value for |r| < L, and sqrt of the left-to-right sum of squares).
+struct PairScreen {
+    double L[3];
+    float Lf[3];
+    float rc2_lo, rc2_hi;
+    double rc;
+};
+
+enum { SCREEN_OUT = 0, SCREEN_IN = 1, SCREEN_NEAR = 2 };
+
+__device__ __forceinline__ int pair_screen(const float *__restrict__ xf, int64_t a, int64_t b, const PairScreen &ps) {
+    float s2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float v = xf[3 * a + k] - xf[3 * b + k];
+        if (!(fabsf(v) < ps.Lf[k])) return SCREEN_NEAR;  // far outside the box: exact path decides
+        if (v > 0.5f * ps.Lf[k])
+            v -= ps.Lf[k];
+        else if (v < -0.5f * ps.Lf[k])
+            v += ps.Lf[k];
+        s2 = fmaf(v, v, s2);
+    }
+    if (s2 > ps.rc2_hi) return SCREEN_OUT;
+    if (s2 < ps.rc2_lo) return SCREEN_IN;
+    return SCREEN_NEAR;
+}
+
+// Float64 minimum-image vector and distance, same values as min_image_sep for |r| < L.
+__device__ __forceinline__ double pair_exact(const double *__restrict__ x, int64_t a, int64_t b, const PairScreen &ps,
+                                             double r[3]) {
+    bool big = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = __dsub_rn(x[3 * a + k], x[3 * b + k]);
+        big = big || !(fabs(v) < ps.L[k]);
+        if (v >= 0.5 * ps.L[k])
+            v = __dsub_rn(v, ps.L[k]);
+        else if (v <= -0.5 * ps.L[k])
+            v = __dadd_rn(v, ps.L[k]);
+        r[k] = v;
+    }
+    if (big) return min_image_sep(x, a, b, ps.L, r);
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+    return __dsqrt_rn(s);
+}
+
+// Filtered per-particle neighbour counts, slot (a, o) at a*27 + o.  One warp per
+// (particle, neighbour cell): lanes take the cell's particles, a ballot counts
+// the kept ones.
+__global__ void __launch_bounds__(256) k_csr_count(const double *__restrict__ x, const float *__restrict__ xf,
+                                                   PairScreen ps,
+                                                   const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                                                   const int32_t *__restrict__ counts,
+                                                   const int64_t *__restrict__ starts, int64_t n, int64_t ncx,
+                                                   int64_t ncy, int64_t ncz, int64_t *__restrict__ cnt27) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
+        const int64_t s = t / 27;
+        const int o = (int)(t % 27);
+        const int32_t a = sorted[s];
+        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
+        const int64_t b0 = starts[nb], len = counts[nb];
         int64_t cnt = 0;
-        for (int64_t j = 0; j < len; ++j) {
-            int32_t b = sorted[b0 + j];
-            if (b == a) continue;
-            double r[3];
-            cnt += min_image_sep(x, a, b, L, r) < rc;
+        for (int64_t j0 = 0; j0 < len; j0 += 32) {
+            const int64_t j = j0 + lane;
+            bool keep = false;
+            if (j < len) {
+                const int32_t b = sorted[b0 + j];
+                if (b != a) {
+                    const int sc = pair_screen(xf, a, b, ps);
+                    if (sc == SCREEN_IN) {
+                        keep = true;
+                    } else if (sc == SCREEN_NEAR) {
+                        double r[3];
+                        keep = pair_exact(x, a, b, ps, r) < ps.rc;
+                    }
+                }
+            }
+            cnt += __popc(__ballot_sync(0xffffffffu, keep));
         }
-        cnt27[(int64_t)a * 27 + o] = cnt;
+        if (lane == 0) cnt27[(int64_t)a * 27 + o] = cnt;
     }
 }
 
@@ -248,35 +340,83 @@ __device__ __forceinline__ void store_pair(PairData<T> &pd, int64_t w, int32_t b
     pd.rz[w] = (T)rh[2];
 }
 
-__global__ void k_csr_fill(const double *__restrict__ x, double Lx, double Ly, double Lz,
-                           const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
-                           const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
-                           int64_t ncx, int64_t ncy, int64_t ncz, double rc, const int64_t *__restrict__ off27,
-                           const double *__restrict__ perp, const double *__restrict__ para,
-                           const double *__restrict__ rv, int64_t ntab, PairData<double> p64, PairData<float> p32,
-                           int *__restrict__ err) {
-    const double L[3] = {Lx, Ly, Lz};
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 27 * n; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t s = t / 27;
-        int o = (int)(t % 27);
-        int32_t a = sorted[s];
-        int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
-        int64_t b0 = starts[nb], len = counts[nb];
+// Same traversal as k_csr_count; kept lanes write at the ballot prefix, so a
+// row lists its pairs by neighbour-cell offset, then by particle id.
+__global__ void __launch_bounds__(256) k_csr_fill(const double *__restrict__ x, const float *__restrict__ xf,
+                                                  PairScreen ps,
+                                                  const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
+                                                  const int32_t *__restrict__ counts,
+                                                  const int64_t *__restrict__ starts, int64_t n, int64_t ncx,
+                                                  int64_t ncy, int64_t ncz, const int64_t *__restrict__ off27,
+                                                  const double *__restrict__ perp, const double *__restrict__ para,
+                                                  const double *__restrict__ rv, int64_t ntab, double inv_dr,
+                                                  PairData<double> p64, PairData<float> p32, int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
+        const int64_t s = t / 27;
+        const int o = (int)(t % 27);
+        const int32_t a = sorted[s];
+        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
+        const int64_t b0 = starts[nb], len = counts[nb];
         int64_t w = off27[(int64_t)a * 27 + o];
-        for (int64_t j = 0; j < len; ++j) {
-            int32_t b = sorted[b0 + j];
-            if (b == a) continue;
-            double r[3];
-            double d = min_image_sep(x, a, b, L, r);
-            if (!(d < rc)) continue;
-            double rh[3] = {__ddiv_rn(r[0], d), __ddiv_rn(r[1], d), __ddiv_rn(r[2], d)};
-            double A = 0.0, B = 0.0;
-            if (!table_lerp(perp, para, rv, ntab, d, &A, &B)) atomicExch(err, 1);
-            store_pair(p64, w, b, A, B, rh);
-            store_pair(p32, w, b, A, B, rh);
-            ++w;
+        for (int64_t j0 = 0; j0 < len; j0 += 32) {
+            const int64_t j = j0 + lane;
+            bool keep = false;
+            int32_t b = -1;
+            double r[3] = {0, 0, 0}, d = 0.0;
+            if (j < len) {
+                b = sorted[b0 + j];
+                if (b != a && pair_screen(xf, a, b, ps) != SCREEN_OUT) {
+                    d = pair_exact(x, a, b, ps, r);
+                    keep = d < ps.rc;
+                }
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int64_t wp = w + __popc(mask & ((1u << lane) - 1u));
+                const double inv = 1.0 / d;
+                const double rh[3] = {r[0] * inv, r[1] * inv, r[2] * inv};
+                double A = 0.0, B = 0.0;
+                if (!table_lerp(perp, para, rv, ntab, d, &A, &B, inv_dr)) atomicExch(err, 1);
+                store_pair(p64, wp, b, A, B, rh);
+                store_pair(p32, wp, b, A, B, rh);
+            }
+            w += __popc(mask);
         }
     }
+}
+
+static PairScreen make_screen(const double *box, double rc, double maxabs) {
+    PairScreen ps;
+    double Lmax = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        ps.L[k] = box[k];
+        ps.Lf[k] = (float)box[k];
+        Lmax = box[k] > Lmax ? box[k] : Lmax;
+    }
+    ps.rc = rc;
+    // per-component error of the float32 difference and wrap: rounding of both
+    // positions (<= 2^-24 |x| each), of the box and of the result
+    const double eps = 4.0 * 5.9604644775390625e-08 * (maxabs + Lmax);
+    const double m = 4.0 * 1.7320508075688772 * eps + 1e-6 * rc;
+    const double lo = rc > m ? rc - m : 0.0;
+    ps.rc2_lo = (float)(lo * lo * (1.0 - 1e-5));
+    ps.rc2_hi = (float)((rc + m) * (rc + m) * (1.0 + 1e-5));
+    return ps;
+}
+
+// float32 copy of the positions and the largest |coordinate| (as ordered float bits).
+__global__ void k_positions_f32(const double *__restrict__ x, int64_t m, float *__restrict__ xf,
+                                unsigned *__restrict__ maxbits) {
+    unsigned local = 0u;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = (float)x[i];
+        xf[i] = v;
+        local = max(local, __float_as_uint(fabsf(v)));
+    }
+    for (int o = 16; o > 0; o >>= 1) local = max(local, __shfl_xor_sync(0xffffffffu, local, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, local);
 }
 
 __global__ void k_row_ptr(const int64_t *__restrict__ off27, const int64_t *__restrict__ cnt27, int64_t n,
@@ -352,11 +492,24 @@ int cell_assign(const double *x, int64_t n, const double *box, const int64_t *nc
     return MPS_OK;
 }
 
-int csr_pairs_count(const double *x, const double *box, double rc, const CellBins &cb, int64_t *cnt27, int64_t *off27,
-                    void *scan_tmp, int64_t *total_host, cudaStream_t s) {
+int positions_f32(const double *x, int64_t n, float *xf, unsigned *maxbits, double *maxabs, cudaStream_t s) {
+    MPS_CUDA_TRY(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), s));
+    k_positions_f32<<<grid_for(3 * n, 256), 256, 0, s>>>(x, 3 * n, xf, maxbits);
+    MPS_LAUNCH_CHECK();
+    unsigned hb = 0;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&hb, maxbits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    float f;
+    memcpy(&f, &hb, sizeof(f));
+    *maxabs = (double)f * (1.0 + 1e-6);
+    return MPS_OK;
+}
+
+int csr_pairs_count(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
+                    int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *total_host, cudaStream_t s) {
     int64_t n = cb.n;
-    k_csr_count<<<grid_for(27 * n, 256), 256, 0, s>>>(x, box[0], box[1], box[2], cb.sorted, cb.lin, cb.counts,
-                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], rc, cnt27);
+    k_csr_count<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
+                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], cnt27);
     MPS_LAUNCH_CHECK();
     int r = exclusive_scan_i64(cnt27, off27, 27 * n, scan_tmp, s);
     if (r) return r;
@@ -368,15 +521,20 @@ int csr_pairs_count(const double *x, const double *box, double rc, const CellBin
     return MPS_OK;
 }
 
-int csr_pairs_fill(const double *x, const double *box, double rc, const CellBins &cb, const int64_t *cnt27,
+int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
+                   const int64_t *cnt27,
                    const int64_t *off27, const double *perp, const double *para, const double *rv, int64_t ntab,
                    int64_t *row_ptr, PairData<double> p64, PairData<float> p32, int *err, cudaStream_t s) {
     int64_t n = cb.n;
     k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
     MPS_LAUNCH_CHECK();
-    k_csr_fill<<<grid_for(27 * n, 256), 256, 0, s>>>(x, box[0], box[1], box[2], cb.sorted, cb.lin, cb.counts,
-                                                     cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], rc, off27,
-                                                     perp, para, rv, ntab, p64, p32, err);
+    double rv_last = 0.0;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&rv_last, rv + ntab - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    const double inv_dr = rv_last > 0 ? (double)(ntab - 1) / rv_last : 0.0;
+    k_csr_fill<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
+                                                     cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], off27,
+                                                     perp, para, rv, ntab, inv_dr, p64, p32, err);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -37,6 +38,25 @@ struct CachedPlan {
 static std::map<PlanKey, CachedPlan> g_plans;
 static std::mutex g_plan_mu;
 
+// Green's coefficients depend only on (grid, box, xi, eta): cached per process
+// (like the FFT plans) and shared by every system built on the same grid.
+struct GreenKey {
+    int N[3];
+    double box[3], xi, eta[3];
+    bool operator<(const GreenKey &o) const { return memcmp(this, &o, sizeof(GreenKey)) < 0; }
+};
+struct GreenCoef {
+    double *h64 = nullptr;
+    float *h32 = nullptr;
+    ~GreenCoef() {
+        if (h64) cudaFree(h64);
+        if (h32) cudaFree(h32);
+    }
+};
+static std::map<GreenKey, std::shared_ptr<GreenCoef>> g_green;
+static std::mutex g_green_mu;
+constexpr size_t kGreenCacheMax = 4;
+
 // Per-stage timing of the matvec (diagnostics): slab, spread, forward FFT,
 // scale, inverse FFT, contract, real space.
 constexpr int kStages = 7;
@@ -46,6 +66,7 @@ struct StageEvents {
 };
 
 struct mps_system {
+    cudaStream_t stream = nullptr;   // creation stream: stream-ordered allocations and frees
     int64_t n = 0;
     int max_rhs = 1;
     int64_t n_diag = 1;
@@ -63,8 +84,9 @@ struct mps_system {
     int32_t *start = nullptr;
     double *w64 = nullptr;
     float *w32 = nullptr;
-    double *h64 = nullptr;
+    double *h64 = nullptr;       // owned by green (shared, cached per grid)
     float *h32 = nullptr;
+    std::shared_ptr<GreenCoef> green;
     double *grid64 = nullptr;
     void *spec64 = nullptr;
     float *grid32 = nullptr;
@@ -94,23 +116,51 @@ static void free_system(mps_system *s) {
     for (auto &e : s->spare)
         for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
     void *ptrs[] = {s->x, s->diag, s->row_ptr, s->p64.nbr, s->p64.A, s->p64.BA, s->p64.rx, s->p64.ry, s->p64.rz,
-                    s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32, s->h64, s->h32,
+                    s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32,
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work};
     for (void *p : ptrs)
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
-    tile_bins_free(s->tb64);
-    tile_bins_free(s->tb32);
-    if (s->partial64) cudaFree(s->partial64);
-    if (s->partial32) cudaFree(s->partial32);
+    tile_bins_free(s->tb64, s->stream);
+    tile_bins_free(s->tb32, s->stream);
+    if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
+    if (s->partial32) cudaFreeAsync(s->partial32, s->stream);
     delete s;
 }
 
+// Device memory of a system comes from the device's default stream-ordered pool
+// with its release threshold raised, so building a system for the next
+// configuration reuses the previous one's memory instead of mapping new pages.
+static void configure_pool_once() {
+    static int done_dev = -1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    if (done_dev == dev) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done_dev = dev;
+}
+
 template <typename P>
-static int dalloc(P **p, size_t bytes) {
+static int dalloc(P **p, size_t bytes, cudaStream_t st) {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc((void **)p, bytes);
+    cudaError_t e = cudaMallocAsync((void **)p, bytes, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return e == cudaErrorMemoryAllocation ? MPS_NO_MEMORY : MPS_CUDA_ERR;
+    }
+    return MPS_OK;
+}
+
+// Persistent buffers shared between systems (cached Green's coefficients).
+template <typename P>
+static int dalloc_persistent(P **p, size_t bytes) {
+    cudaError_t e = cudaMalloc((void **)p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
@@ -156,15 +206,12 @@ static int get_plan(cufftType type, const GridParams &gp, int batch, CachedPlan 
     return MPS_OK;
 }
 
-static int ensure_work(mps_system *s, size_t need) {
+static int ensure_work(mps_system *s, size_t need, cudaStream_t st) {
     if (need <= s->fft_work_bytes) return MPS_OK;
-    if (s->fft_work) {
-        MPS_CUDA_TRY(cudaDeviceSynchronize());
-        cudaFree(s->fft_work);
-    }
+    if (s->fft_work) cudaFreeAsync(s->fft_work, st);
     s->fft_work = nullptr;
     s->fft_work_bytes = 0;
-    MPS_TRY(dalloc(&s->fft_work, need));
+    MPS_TRY(dalloc(&s->fft_work, need, st));
     s->fft_work_bytes = need;
     return MPS_OK;
 }
@@ -173,7 +220,7 @@ static int ensure_work(mps_system *s, size_t need) {
 static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *out, int dir, cudaStream_t st) {
     CachedPlan cp;
     MPS_TRY(get_plan(type, s->gp, batch, &cp));
-    MPS_TRY(ensure_work(s, cp.work));
+    MPS_TRY(ensure_work(s, cp.work, st));
     std::lock_guard<std::mutex> lk(g_plan_mu);
     CUFFT_TRY(cufftSetWorkArea(cp.h, s->fft_work));
     CUFFT_TRY(cufftSetStream(cp.h, st));
@@ -190,14 +237,14 @@ static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *o
     return MPS_OK;
 }
 
-static int ensure_grids(mps_system *s, int precision) {
+static int ensure_grids(mps_system *s, int precision, cudaStream_t st) {
     size_t nr = (size_t)s->max_rhs * 3;
     if (precision == MPS_FP64) {
-        if (!s->grid64) MPS_TRY(dalloc(&s->grid64, nr * s->gp.G * sizeof(double)));
-        if (!s->spec64) MPS_TRY(dalloc(&s->spec64, nr * s->Gc * 2 * sizeof(double)));
+        if (!s->grid64) MPS_TRY(dalloc(&s->grid64, nr * s->gp.G * sizeof(double), st));
+        if (!s->spec64) MPS_TRY(dalloc(&s->spec64, nr * s->Gc * 2 * sizeof(double), st));
     } else {
-        if (!s->grid32) MPS_TRY(dalloc(&s->grid32, nr * s->gp.G * sizeof(float)));
-        if (!s->spec32) MPS_TRY(dalloc(&s->spec32, nr * s->Gc * 2 * sizeof(float)));
+        if (!s->grid32) MPS_TRY(dalloc(&s->grid32, nr * s->gp.G * sizeof(float), st));
+        if (!s->spec32) MPS_TRY(dalloc(&s->spec32, nr * s->Gc * 2 * sizeof(float), st));
     }
     return MPS_OK;
 }
@@ -237,21 +284,127 @@ static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStrea
     } while (0)
 
 // Tile depth per precision: float64 accumulators take twice the registers.
-static int tile_depth(bool dbl) { return dbl ? 4 : 8; }
+// Autotuner for the tiled spread/contract: the tile depth (z) is timed on the
+// first system of each (grid, support, precision, batch width) and the fastest
+// is kept for the rest of the process.
+struct TuneKey {
+    int N[3];
+    int P;
+    int dbl;
+    int nrhs;
+    bool operator<(const TuneKey &o) const { return memcmp(this, &o, sizeof(TuneKey)) < 0; }
+};
+struct TuneResult {
+    int tz;
+    float ms[2];   // timings of depth 4 and 8 (spread + contract), -1 if not run
+};
+static std::map<TuneKey, TuneResult> g_tune;
+static std::mutex g_tune_mu;
+static const int kDepths[2] = {4, 8};
 
-// Lazily bins the particles for the tiled kernels of one precision.
+template <typename T>
+static int time_tiles(mps_system *s, int tz, int nrhs, const double *m, double *out, T *grid, cudaStream_t st,
+                      float *ms) {
+    TileBins tb;
+    MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
+    T *partial = nullptr;
+    const bool dbl = sizeof(T) == 8;
+    if (!dbl) MPS_TRY(dalloc(&partial, (size_t)tb.nentries * 9 * sizeof(T), st));
+    const T *w = dbl ? (const T *)s->w64 : (const T *)s->w32;
+    cudaEvent_t e0, e1;
+    MPS_CUDA_TRY(cudaEventCreate(&e0));
+    MPS_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int rc = MPS_OK;
+    for (int rep = 0; rep < 4 && rc == MPS_OK; ++rep) {
+        cudaEventRecord(e0, st);
+        rc = spread_tiled<T>(m, s->n, nrhs, s->start, w, s->gp, tb, grid, st);
+        if (rc == MPS_OK && !dbl) rc = contract_tiled<T>(grid, s->n, nrhs, s->start, w, s->gp, tb, partial, out, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && t < best) best = t;   // first repetition warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (partial) cudaFreeAsync(partial, st);
+    tile_bins_free(tb, st);
+    *ms = best;
+    return rc;
+}
+
+static int tuned_depth(mps_system *s, bool dbl, cudaStream_t st, int *tz) {
+    TuneKey key;
+    memset(&key, 0, sizeof(key));
+    for (int k = 0; k < 3; ++k) key.N[k] = s->gp.N[k];
+    key.P = s->gp.P;
+    key.dbl = dbl ? 1 : 0;
+    key.nrhs = s->max_rhs < 3 ? s->max_rhs : 3;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            *tz = it->second.tz;
+            return MPS_OK;
+        }
+    }
+    TuneResult res{0, {-1.f, -1.f}};
+    int ok = 0;
+    for (int i = 0; i < 2; ++i) ok += tiles_supported(s->gp, kDepths[i]) ? 1 : 0;
+    if (ok == 0) {
+        *tz = 0;
+        return MPS_OK;
+    }
+    const int nrhs = key.nrhs;
+    const int64_t tot = (int64_t)nrhs * 3 * s->n;
+    double *m = nullptr, *out = nullptr;
+    MPS_TRY(dalloc(&m, sizeof(double) * tot, st));
+    MPS_TRY(dalloc(&out, sizeof(double) * tot, st));
+    MPS_CUDA_TRY(cudaMemsetAsync(m, 0, sizeof(double) * tot, st));
+    float best = 1e30f;
+    for (int i = 0; i < 2; ++i) {
+        if (!tiles_supported(s->gp, kDepths[i])) continue;
+        float ms = 0.f;
+        int rc = dbl ? time_tiles<double>(s, kDepths[i], nrhs, m, out, (double *)s->grid64, st, &ms)
+                     : time_tiles<float>(s, kDepths[i], nrhs, m, out, (float *)s->grid32, st, &ms);
+        if (rc != MPS_OK) {
+            cudaFreeAsync(m, st);
+            cudaFreeAsync(out, st);
+            return rc;
+        }
+        res.ms[i] = ms;
+        if (ms < best) {
+            best = ms;
+            res.tz = kDepths[i];
+        }
+    }
+    cudaFreeAsync(m, st);
+    cudaFreeAsync(out, st);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = res;
+    }
+    *tz = res.tz;
+    return MPS_OK;
+}
+
+// Lazily bins the particles for the tiled kernels of one precision (tile depth
+// from the autotuner).
 static int ensure_tiles(mps_system *s, bool dbl, cudaStream_t st, bool *use) {
     *use = false;
-    const int tz = tile_depth(dbl);
-    if (!s->tiled || !tiles_supported(s->gp, tz)) return MPS_OK;
+    if (!s->tiled) return MPS_OK;
     TileBins &tb = dbl ? s->tb64 : s->tb32;
     if (!tb.mem) {
+        MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
+        int tz = 0;
+        MPS_TRY(tuned_depth(s, dbl, st, &tz));
+        if (tz == 0 || !tiles_supported(s->gp, tz)) {
+            s->tiled = false;
+            return MPS_OK;
+        }
         MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
-        const size_t pbytes = (size_t)tb.nentries * 9 * (dbl ? sizeof(double) : sizeof(float));
-        if (dbl)
-            MPS_TRY(dalloc(&s->partial64, pbytes));
-        else
-            MPS_TRY(dalloc(&s->partial32, pbytes));
+        if (!dbl) MPS_TRY(dalloc(&s->partial32, (size_t)tb.nentries * 9 * sizeof(float), st));
     }
     *use = true;
     return MPS_OK;
@@ -264,7 +417,7 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     MPS_TRY(ensure_tiles(s, dbl, st, &use_tiles));
     const TileBins &tb = dbl ? s->tb64 : s->tb32;
     T *partial = dbl ? (T *)s->partial64 : (T *)s->partial32;
-    MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32));
+    MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
     T *grid = dbl ? (T *)s->grid64 : (T *)s->grid32;
     void *spec = dbl ? s->spec64 : s->spec32;
     const T *w = dbl ? (const T *)s->w64 : (const T *)s->w32;
@@ -272,7 +425,7 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
-    MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
     STAGE_MARK(1);
     if (use_tiles)
         MPS_TRY(spread_tiled<T>(m, s->n, nrhs, s->start, w, s->gp, tb, grid, st));
@@ -285,7 +438,9 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     STAGE_MARK(4);
     MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 3 * nrhs, spec, grid, 0, st));
     STAGE_MARK(5);
-    if (use_tiles)
+    // float64: the warp-per-particle gather keeps more lanes busy, which is what
+    // matters at GB300's float64 issue rate; float32: the shared-memory tile.
+    if (use_tiles && !dbl)
         MPS_TRY(contract_tiled<T>(grid, s->n, nrhs, s->start, w, s->gp, tb, partial, out, st));
     else
         MPS_TRY(contract<T>(grid, s->n, nrhs, s->start, w, s->gp, out, st));
@@ -311,11 +466,16 @@ constexpr int kDotItems = 8;
 constexpr int kDotChunk = kDotThreads * kDotItems;
 constexpr int kMaxCols = 64;
 
-// partial[r][blk][c] = sum over the block's rows of V_r[c][i] * w_r[i]
+// partial[r][blk][c] = sum over the block's rows of V_r[c][i] * w_r[i]; the last
+// block of each system to finish (ticket counter, threadfence pattern) sums the
+// partials in block order and writes out[r][c]: one launch, fixed summation order.
 __global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restrict__ V, int64_t ldv, int64_t vstride,
                                                           int ncols, const double *__restrict__ w, int64_t wstride,
-                                                          int64_t n3, double *__restrict__ partial, int nblk) {
+                                                          int64_t n3, double *__restrict__ partial, int nblk,
+                                                          unsigned *__restrict__ tickets, double *__restrict__ out,
+                                                          int64_t ostride) {
     __shared__ double red[kDotThreads / 32][kMaxCols];
+    __shared__ bool last;
     const int r = blockIdx.y;
     const double *Vr = V + r * vstride;
     const double *wr = w + r * wstride;
@@ -345,16 +505,17 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restri
         for (int q = 0; q < kDotThreads / 32; ++q) s += red[q][c];
         partial[((int64_t)r * nblk + blockIdx.x) * kMaxCols + c] = s;
     }
-}
-
-__global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, int ncols, int nrhs,
-                                  double *__restrict__ out, int64_t ostride) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nrhs * ncols) return;
-    const int r = t / ncols, c = t % ncols;
-    double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += partial[((int64_t)r * nblk + b) * kMaxCols + c];
-    out[(int64_t)r * ostride + c] = s;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&tickets[r], 1u) == (unsigned)(nblk - 1);
+    __syncthreads();
+    if (!last) return;
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b) s += __ldcg(partial + ((int64_t)r * nblk + b) * kMaxCols + c);
+        out[(int64_t)r * ostride + c] = s;
+    }
+    if (threadIdx.x == 0) tickets[r] = 0u;
 }
 
 // w_r[i] -= sum_c V_r[c][i] * h_r[c]
@@ -538,15 +699,27 @@ static char *carve_ws(char *&p, size_t bytes) {
     return (char *)u;
 }
 
-// Dots of the first ncols basis vectors with w, for every system.
+// Dots of the first ncols basis vectors with w, for every system.  The scratch
+// holds nrhs * nblk * kMaxCols partials followed by nrhs zeroed tickets
+// (multidot_bytes / multidot_init).
 static int multidot(const double *V, int64_t ldv, int64_t vstride, int ncols, const double *w, int64_t wstride,
                     int64_t n3, int nrhs, double *partial, double *out, int64_t ostride, cudaStream_t s) {
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    unsigned *tickets = (unsigned *)(partial + (size_t)nrhs * nblk * kMaxCols);
     dim3 g(nblk, nrhs);
-    k_multidot<<<g, kDotThreads, 0, s>>>(V, ldv, vstride, ncols, w, wstride, n3, partial, nblk);
+    k_multidot<<<g, kDotThreads, 0, s>>>(V, ldv, vstride, ncols, w, wstride, n3, partial, nblk, tickets, out, ostride);
     MPS_LAUNCH_CHECK();
-    k_reduce_partials<<<(nrhs * ncols + 127) / 128, 128, 0, s>>>(partial, nblk, ncols, nrhs, out, ostride);
-    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+static size_t multidot_bytes(int64_t n3, int nrhs) {
+    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    return sizeof(double) * (size_t)nrhs * nblk * kMaxCols + sizeof(unsigned) * (size_t)(nrhs + 2);
+}
+
+static int multidot_init(double *partial, int64_t n3, int nrhs, cudaStream_t s) {
+    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
+    MPS_CUDA_TRY(cudaMemsetAsync(partial + (size_t)nrhs * nblk * kMaxCols, 0, sizeof(unsigned) * (size_t)nrhs, s));
     return MPS_OK;
 }
 
@@ -579,7 +752,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     bytes += 4 * (256 + sizeof(double) * (size_t)nrhs);               // nrm2 beta bnorm res
     bytes += 2 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount frozen
     bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
-    bytes += 256 + sizeof(double) * (size_t)nrhs * nblk * kMaxCols;   // partial
+    bytes += 256 + multidot_bytes(n3, nrhs);                          // partial + tickets
     bytes += 256 + sizeof(double) * (size_t)nrhs * (kMaxCols + 1);    // u
     char *base = nullptr;
     MPS_CUDA_TRY(cudaMallocAsync((void **)&base, bytes, st));
@@ -600,8 +773,15 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     S.kcount = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
     int32_t *frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
     S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
-    double *partial = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * nblk * kMaxCols);
+    double *partial = (double *)carve_ws(p, multidot_bytes(n3, nrhs));
     double *u = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * (kMaxCols + 1));
+    {
+        int e = multidot_init(partial, n3, nrhs, st);
+        if (e) {
+            cudaFreeAsync(base, st);
+            return e;
+        }
+    }
 
     std::vector<double> hres(nrhs);
     std::vector<int32_t> hfrozen(nrhs, 0);
@@ -810,10 +990,18 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
     const int inner_maxit = o->inner_maxit > 0 ? o->inner_maxit : 4;
     const bool incremental = o->residual_policy == 0;
     double *buf = nullptr;
-    const size_t bytes = sizeof(double) * (4 * (size_t)tot + 2 * nrhs + (size_t)nrhs * nblk * kMaxCols);
+    const size_t bytes = sizeof(double) * (4 * (size_t)tot + 2 * nrhs) + multidot_bytes(n3, nrhs);
     MPS_CUDA_TRY(cudaMallocAsync((void **)&buf, bytes, st));
     double *r = buf, *dx = buf + tot, *ax = buf + 2 * tot, *rn = buf + 3 * tot, *nrm = buf + 4 * tot,
            *partial = nrm + 2 * nrhs;
+    (void)nblk;
+    {
+        int e0 = multidot_init(partial, n3, nrhs, st);
+        if (e0) {
+            cudaFreeAsync(buf, st);
+            return e0;
+        }
+    }
     std::vector<double> rel(nrhs);
     std::vector<int> ic(nrhs);
     std::vector<double> ir(nrhs);
@@ -914,7 +1102,9 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         if (d->rc > d->box[k] / 2.0) return MPS_RC_GT_HALF_BOX;
     }
     if (d->P > 32) return MPS_BAD_ARG;
+    configure_pool_once();
     mps_system *s = new mps_system();
+    s->stream = st;
     s->n = d->n;
     s->max_rhs = d->max_rhs;
     s->n_diag = d->n_diag;
@@ -934,13 +1124,14 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
             return rc;             \
         }                          \
     } while (0)
-    CR_TRY(dalloc(&s->x, sizeof(double) * 3 * n));
+    CR_TRY(dalloc(&s->x, sizeof(double) * 3 * n, st));
     if (cudaMemcpyAsync(s->x, d->x, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         CR_TRY(MPS_CUDA_ERR);
-    CR_TRY(dalloc(&s->diag, sizeof(double) * n * d->n_diag));
+    CR_TRY(dalloc(&s->diag, sizeof(double) * n * d->n_diag, st));
     CR_TRY(build_diag(d->lambdap, n * d->n_diag, d->perp, s->diag, st));
-    CR_TRY(dalloc(&s->slab, sizeof(double) * d->max_rhs));
-    CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * d->max_rhs));
+    CR_TRY(dalloc(&s->slab, sizeof(double) * d->max_rhs, st));
+    if (cudaMemsetAsync(s->slab, 0, sizeof(double) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
+    CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * d->max_rhs, st));
     if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * d->max_rhs) != cudaSuccess) CR_TRY(MPS_NO_MEMORY);
     if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     // cell list + pair CSR
@@ -949,47 +1140,55 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     int64_t *cell3 = nullptr, *cnt27 = nullptr, *off27 = nullptr;
     void *bins = nullptr, *scan_tmp = nullptr;
     int *err = nullptr;
-    CR_TRY(dalloc(&cell3, sizeof(int64_t) * 3 * n));
-    CR_TRY(dalloc(&bins, cell_bins_bytes(n, ncells)));
-    CR_TRY(dalloc(&cnt27, sizeof(int64_t) * 27 * n));
-    CR_TRY(dalloc(&off27, sizeof(int64_t) * 27 * n));
-    CR_TRY(dalloc(&scan_tmp, scan_workspace(27 * n)));
-    CR_TRY(dalloc(&err, sizeof(int)));
+    float *xf = nullptr;
+    unsigned *maxbits = nullptr;
+    double maxabs = 0.0;
+    CR_TRY(dalloc(&xf, sizeof(float) * 3 * n, st));
+    CR_TRY(dalloc(&maxbits, sizeof(unsigned) * 4, st));
+    CR_TRY(dalloc(&cell3, sizeof(int64_t) * 3 * n, st));
+    CR_TRY(dalloc(&bins, cell_bins_bytes(n, ncells), st));
+    CR_TRY(dalloc(&cnt27, sizeof(int64_t) * 27 * n, st));
+    CR_TRY(dalloc(&off27, sizeof(int64_t) * 27 * n, st));
+    CR_TRY(dalloc(&scan_tmp, scan_workspace(27 * n), st));
+    CR_TRY(dalloc(&err, sizeof(int), st));
     auto tmp_free = [&]() {
-        cudaFree(cell3);
-        cudaFree(bins);
-        cudaFree(cnt27);
-        cudaFree(off27);
-        cudaFree(scan_tmp);
-        cudaFree(err);
+        cudaFreeAsync(cell3, st);
+        cudaFreeAsync(bins, st);
+        cudaFreeAsync(cnt27, st);
+        cudaFreeAsync(off27, st);
+        cudaFreeAsync(scan_tmp, st);
+        cudaFreeAsync(err, st);
+        cudaFreeAsync(xf, st);
+        cudaFreeAsync(maxbits, st);
     };
     CellBins cb;
     rc = cell_assign(s->x, n, d->box, s->ncell, cell3, st);
     if (!rc) rc = cell_bins_build(cell3, n, s->ncell, bins, cb, st);
     int64_t np = 0;
-    if (!rc) rc = csr_pairs_count(s->x, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);
+    if (!rc) rc = positions_f32(s->x, n, xf, maxbits, &maxabs, st);
+    if (!rc) rc = csr_pairs_count(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);
     if (rc) {
         tmp_free();
         free_system(s);
         return rc;
     }
     s->n_pairs = np;
-    rc = dalloc(&s->row_ptr, sizeof(int64_t) * (n + 1));
-    if (!rc) rc = dalloc(&s->p64.nbr, sizeof(int32_t) * np);
-    if (!rc) rc = dalloc(&s->p64.A, sizeof(double) * np);
-    if (!rc) rc = dalloc(&s->p64.BA, sizeof(double) * np);
-    if (!rc) rc = dalloc(&s->p64.rx, sizeof(double) * np);
-    if (!rc) rc = dalloc(&s->p64.ry, sizeof(double) * np);
-    if (!rc) rc = dalloc(&s->p64.rz, sizeof(double) * np);
-    if (!rc) rc = dalloc(&s->p32.A, sizeof(float) * np);
-    if (!rc) rc = dalloc(&s->p32.BA, sizeof(float) * np);
-    if (!rc) rc = dalloc(&s->p32.rx, sizeof(float) * np);
-    if (!rc) rc = dalloc(&s->p32.ry, sizeof(float) * np);
-    if (!rc) rc = dalloc(&s->p32.rz, sizeof(float) * np);
+    rc = dalloc(&s->row_ptr, sizeof(int64_t) * (n + 1), st);
+    if (!rc) rc = dalloc(&s->p64.nbr, sizeof(int32_t) * np, st);
+    if (!rc) rc = dalloc(&s->p64.A, sizeof(double) * np, st);
+    if (!rc) rc = dalloc(&s->p64.BA, sizeof(double) * np, st);
+    if (!rc) rc = dalloc(&s->p64.rx, sizeof(double) * np, st);
+    if (!rc) rc = dalloc(&s->p64.ry, sizeof(double) * np, st);
+    if (!rc) rc = dalloc(&s->p64.rz, sizeof(double) * np, st);
+    if (!rc) rc = dalloc(&s->p32.A, sizeof(float) * np, st);
+    if (!rc) rc = dalloc(&s->p32.BA, sizeof(float) * np, st);
+    if (!rc) rc = dalloc(&s->p32.rx, sizeof(float) * np, st);
+    if (!rc) rc = dalloc(&s->p32.ry, sizeof(float) * np, st);
+    if (!rc) rc = dalloc(&s->p32.rz, sizeof(float) * np, st);
     s->p32.nbr = s->p64.nbr;
     if (!rc && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
     if (!rc)
-        rc = csr_pairs_fill(s->x, d->box, d->rc, cb, cnt27, off27, d->perp, d->para, d->rvals, d->n_tab, s->row_ptr,
+        rc = csr_pairs_fill(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, d->perp, d->para, d->rvals, d->n_tab, s->row_ptr,
                             s->p64, s->p32, err, st);
     int herr = 0;
     if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = MPS_CUDA_ERR;
@@ -1001,13 +1200,35 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         return rc;
     }
     // grid geometry + Green's coefficients
-    CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n));
-    CR_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P));
-    CR_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P));
+    CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n, st));
+    CR_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P, st));
+    CR_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P, st));
     CR_TRY(grid_geometry(s->x, n, s->gp, s->start, s->w64, s->w32, st));
-    CR_TRY(dalloc(&s->h64, sizeof(double) * s->Gc));
-    CR_TRY(dalloc(&s->h32, sizeof(float) * s->Gc));
-    CR_TRY(green_half(s->gp, s->h64, s->h32, st));
+    {
+        GreenKey key;
+        memset(&key, 0, sizeof(key));
+        for (int k = 0; k < 3; ++k) {
+            key.N[k] = s->gp.N[k];
+            key.box[k] = d->box[k];
+            key.eta[k] = s->gp.eta[k];
+        }
+        key.xi = d->xi;
+        std::lock_guard<std::mutex> lk(g_green_mu);
+        auto it = g_green.find(key);
+        if (it != g_green.end()) {
+            s->green = it->second;
+        } else {
+            auto gc = std::make_shared<GreenCoef>();
+            CR_TRY(dalloc_persistent(&gc->h64, sizeof(double) * s->Gc));
+            CR_TRY(dalloc_persistent(&gc->h32, sizeof(float) * s->Gc));
+            CR_TRY(green_half(s->gp, gc->h64, gc->h32, st));
+            if (g_green.size() >= kGreenCacheMax) g_green.clear();  // systems keep their own reference
+            g_green[key] = gc;
+            s->green = gc;
+        }
+        s->h64 = s->green->h64;
+        s->h32 = s->green->h32;
+    }
 #undef CR_TRY
     *out = s;
     return MPS_OK;
@@ -1042,8 +1263,8 @@ extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *o
     int32_t di[2] = {diag_index, diag_index};
     MPS_TRY(upload_diag_idx(sys, di, 2, st));
     const int64_t G = sys->gp.G;
-    if (!sys->rgrid2) MPS_TRY(dalloc(&sys->rgrid2, sizeof(double) * 6 * G));
-    if (!sys->cgrid) MPS_TRY(dalloc(&sys->cgrid, sizeof(double) * 2 * 3 * G));
+    if (!sys->rgrid2) MPS_TRY(dalloc(&sys->rgrid2, sizeof(double) * 6 * G, st));
+    if (!sys->cgrid) MPS_TRY(dalloc(&sys->cgrid, sizeof(double) * 2 * 3 * G, st));
     const double vol = sys->box[0] * sys->box[1] * sys->box[2];
     MPS_TRY(slab_terms(m_ri, sys->n, 2, sys->slab_factor / vol, sys->slab, st));
     MPS_TRY(spread<double>(m_ri, sys->n, 2, sys->start, sys->w64, sys->gp, sys->rgrid2, st));
@@ -1119,6 +1340,25 @@ extern "C" int mps_system_stage_times(mps_system *sys, double *ms, int64_t *coun
         count[p] = sys->stage_count[p];
         for (int k = 0; k < kStages; ++k) sys->stage_ms[p][k] = 0.0;
         sys->stage_count[p] = 0;
+    }
+    return MPS_OK;
+}
+
+extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms) {
+    if (!sys || !tile_depth || !ms) return MPS_BAD_ARG;
+    tile_depth[0] = sys->tb64.tz;
+    tile_depth[1] = sys->tb32.tz;
+    for (int p = 0; p < 2; ++p) {
+        TuneKey key;
+        memset(&key, 0, sizeof(key));
+        for (int k = 0; k < 3; ++k) key.N[k] = sys->gp.N[k];
+        key.P = sys->gp.P;
+        key.dbl = p == 0 ? 1 : 0;
+        key.nrhs = sys->max_rhs < 3 ? sys->max_rhs : 3;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        ms[2 * p] = it != g_tune.end() ? it->second.ms[0] : -1.f;
+        ms[2 * p + 1] = it != g_tune.end() ? it->second.ms[1] : -1.f;
     }
     return MPS_OK;
 }

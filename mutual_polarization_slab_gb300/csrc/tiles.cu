@@ -115,7 +115,7 @@ static char *carve_t(char *&p, size_t bytes) {
 }
 
 int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s) {
-    tile_bins_free(tb);
+    tile_bins_free(tb, s);
     if (!tiles_supported(gp, tz)) return MPS_BAD_ARG;
     TileGeom tg;
     tg.P = gp.P;
@@ -170,7 +170,7 @@ int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int t
     // persistent arrays
     size_t bytes = 256 * 5 + (size_t)(T + 1) * 8 + (size_t)E * 4 + (size_t)(n + 1) * 8 + (size_t)E * 4 +
                    (size_t)E * 4;
-    MPS_CUDA_TRY(cudaMalloc(&tb.mem, bytes));
+    MPS_CUDA_TRY(cudaMallocAsync(&tb.mem, bytes, s));
     p = (char *)tb.mem;
     tb.tile_start = (int64_t *)carve_t(p, (size_t)(T + 1) * 8);
     tb.entries = (int32_t *)carve_t(p, (size_t)E * 4);
@@ -193,8 +193,8 @@ int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int t
     return MPS_OK;
 }
 
-void tile_bins_free(TileBins &tb) {
-    if (tb.mem) cudaFree(tb.mem);
+void tile_bins_free(TileBins &tb, cudaStream_t s) {
+    if (tb.mem) cudaFreeAsync(tb.mem, s);
     tb = TileBins();
 }
 
@@ -289,6 +289,8 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
 // ---------------------------------------------------------------------------
 // Contract
 // ---------------------------------------------------------------------------
+constexpr int kRowPad = kTileX + 1;  // padded tile row: rows y and y+2 no longer share banks
+
 template <typename T, int TZ, int NR>
 __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ grid, int r0,
                                                         const int32_t *__restrict__ start, const T *__restrict__ w,
@@ -296,9 +298,10 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
                                                         const int32_t *__restrict__ entries, int ntx, int nty,
                                                         T *__restrict__ partial) {
     constexpr int C = 3 * NR;
+    constexpr int kPlane = kTileY * kRowPad;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *tile = (T *)smem_raw;                                  // [C][TZ][16][16]
-    T *wbuf = tile + C * TZ * kTileX * kTileY;                // [8 warps][3*kMaxP]
+    T *tile = (T *)smem_raw;                                  // [C][TZ][16][17]
+    T *wbuf = tile + C * TZ * kPlane;                         // [8 warps][3*kMaxP]
     const int64_t t = blockIdx.x;
     const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
     const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
@@ -317,7 +320,7 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
             const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
 #pragma unroll
             for (int c = 0; c < C; ++c)
-                tile[((c * TZ + z) * kTileY + ty) * kTileX + tx] =
+                tile[(c * TZ + z) * kPlane + ty * kRowPad + tx] =
                     (in && gz < Nz) ? grid[(int64_t)(3 * r0 + c) * G + node] : (T)0;
         }
     }
@@ -331,28 +334,37 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
         if (oy < 0) oy += Ny;
         if (oz < 0) oz += Nz;
         for (int k = lane; k < 3 * P; k += 32) wb[(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+        // stencil columns / rows / planes of this particle that fall inside the tile (and the grid)
+        int xr = lane - ox, yr = lane - oy, zr = lane - oz;
+        if (xr < 0) xr += Nx;
+        if (yr < 0) yr += Ny;
+        if (zr < 0) zr += Nz;
+        const unsigned mx = __ballot_sync(0xffffffffu, lane < P && xr < kTileX && X0 + xr < Nx);
+        const unsigned my = __ballot_sync(0xffffffffu, lane < P && yr < kTileY && Y0 + yr < Ny);
+        unsigned mz = __ballot_sync(0xffffffffu, lane < P && zr < TZ && Z0 + zr < Nz);
         __syncwarp();
+        const int nx = __popc(mx), ny = __popc(my);
         T acc[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) acc[c] = (T)0;
-        for (int idx = lane; idx < P * P; idx += 32) {
-            const int jx = idx % P, jy = idx / P;
-            int xr = jx - ox;
-            if (xr < 0) xr += Nx;
-            int yr = jy - oy;
-            if (yr < 0) yr += Ny;
-            if (xr < kTileX && yr < kTileY) {
-                const T wxy = wb[jx] * wb[kMaxP + jy];
-                for (int jz = 0; jz < P; ++jz) {
-                    int zr = jz - oz;
-                    if (zr < 0) zr += Nz;
-                    if (zr < TZ) {
-                        const T wv = wxy * wb[2 * kMaxP + jz];
-                        const T *tp = tile + (zr * kTileY + yr) * kTileX + xr;
+        for (int q = lane; q < nx * ny; q += 32) {
+            const unsigned jxu = __fns(mx, 0, q % nx + 1), jyu = __fns(my, 0, q / nx + 1);
+            if (jxu >= (unsigned)P || jyu >= (unsigned)P) continue;  // (cannot happen: q < nx*ny)
+            const int jx = (int)jxu, jy = (int)jyu;
+            int x = jx - ox, y = jy - oy;
+            if (x < 0) x += Nx;
+            if (y < 0) y += Ny;
+            const T wxy = wb[jx] * wb[kMaxP + jy];
+            unsigned mzz = mz;
+            while (mzz) {
+                const int jz = __ffs(mzz) - 1;
+                mzz &= mzz - 1;
+                int z = jz - oz;
+                if (z < 0) z += Nz;
+                const T wv = wxy * wb[2 * kMaxP + jz];
+                const T *tp = tile + z * kPlane + y * kRowPad + x;
 #pragma unroll
-                        for (int c = 0; c < C; ++c) acc[c] += wv * tp[c * TZ * kTileX * kTileY];
-                    }
-                }
+                for (int c = 0; c < C; ++c) acc[c] += wv * tp[c * TZ * kPlane];
             }
         }
 #pragma unroll
@@ -419,7 +431,7 @@ template <typename T, int TZ, int NR>
 static int contract_launch(const T *grid, int64_t n, int r0, const int32_t *start, const T *w, const GridParams &gp,
                            const TileBins &tb, T *partial, double *out, cudaStream_t s) {
     constexpr int C = 3 * NR;
-    const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileX * kTileY + 8 * 3 * kMaxP);
+    const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileY * kRowPad + 8 * 3 * kMaxP);
     static bool attr_set = false;  // one attribute call per instantiation
     if (!attr_set) {
         MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,

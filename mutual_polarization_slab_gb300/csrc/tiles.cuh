@@ -25,7 +25,7 @@ struct TileBins {
 
 bool tiles_supported(const GridParams &gp, int tz);
 int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s);
-void tile_bins_free(TileBins &tb);
+void tile_bins_free(TileBins &tb, cudaStream_t s);
 
 // grid[(r*3+c)][G] for r < nrhs, written completely (no zeroing needed).
 template <typename T>

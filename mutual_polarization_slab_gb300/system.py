@@ -143,6 +143,14 @@ class SpectralEwaldSystem:
             out[name] = (int(cnt[p]), {s: float(ms[p * 7 + k]) for k, s in enumerate(self.STAGES)})
         return out
 
+    def tuning(self):
+        """Autotuned tile depth per precision and the timings it was chosen from (ms)."""
+        tz = (C.c_int32 * 2)()
+        ms = (C.c_float * 4)()
+        L.check(self._lib.mps_system_tuning(self._h, tz, ms))
+        return {"fp64": {"tile": [16, 16, int(tz[0])], "ms_depth4": ms[0], "ms_depth8": ms[1]},
+                "fp32": {"tile": [16, 16, int(tz[1])], "ms_depth4": ms[2], "ms_depth8": ms[3]}}
+
     # -- operator ---------------------------------------------------------
     def _diag_arg(self, nrhs, diag_index):
         if diag_index is None:
