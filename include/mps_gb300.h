@@ -215,6 +215,18 @@ int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int
               mps_stream_t stream);
 
 /* ------------------------------------------------------------------------- */
+/* Point-dipole pair forces (the HOOMD plugin's kernel)                        */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces compute_forces(pos, dip, box, r_cut, prefactor, periodic_z, use_cell_list) of
+ * "CPU - HOOMD simulation test/dipole_forces_ext/_dipole_forces_ext.cpp:119-497".
+ * pos, dip: n x 3; box: host double[3]; forces: n x 3; pe: n (half of each pair
+ * energy on each particle).  Returns MPS_RC_GT_HALF_BOX when r_cut >= L/2 in a
+ * periodic axis (the reference's RuntimeError). */
+int mps_dipole_forces(const double *pos, const double *dip, int64_t n, const double *box, double r_cut,
+                      double prefactor, int32_t periodic_z, double *forces, double *pe, mps_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
 /* Allocation-free neighbour list (no counterpart in the reference: its Python */
 /* allocates freely).  For callers that must not allocate device memory while */
 /* they run, e.g. a simulation engine that owns all device memory and calls a */

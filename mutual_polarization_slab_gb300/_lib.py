@@ -25,6 +25,7 @@ EXPORTS = (
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
     "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
+    "mps_dipole_forces",
 )
 
 p = C.c_void_p
@@ -83,6 +84,7 @@ _SIGS = {
     "mps_system_stage_times": (C.c_int, [p, PD, P64]),
     "mps_neighbor_list_noalloc": (C.c_int, [p, i64, P64, p, p, i64, P64, p]),
     "mps_system_tuning": (C.c_int, [p, C.POINTER(i32), C.POINTER(C.c_float)]),
+    "mps_dipole_forces": (C.c_int, [p, p, i64, PD, f64, f64, i32, p, p, p]),
 }
 
 _lib = None

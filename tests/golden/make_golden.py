@@ -148,12 +148,34 @@ def case_c1(ew, cap):
     )
 
 
+def case_forces(ew, cap):
+    """The reference's compiled point-dipole force extension (built from its own
+    source by oracle/build_ref.py) on seeded dipoles, periodic and open z."""
+    sys.path.insert(0, ROOT)
+    from oracle import build_ref
+    ext = build_ref.load()
+    if ext is None:
+        raise SystemExit("reference force extension unavailable (pybind11 or reference tree missing)")
+    rng = np.random.default_rng(17)
+    n = 400
+    box = np.array([22.0, 22.0, 26.0])
+    pos = rng.random((n, 3)) * box - box / 2
+    dip = rng.normal(size=(n, 3))
+    out = dict(pos=pos, dip=dip, box=box, r_cut=6.5, pref=1.7)
+    for pz in (True, False):
+        for cl in (True, False):
+            F, e = ext.compute_forces(pos, dip, box, 6.5, 1.7, pz, cl)
+            out[f"F_pz{int(pz)}_cl{int(cl)}"] = F
+            out[f"pe_pz{int(pz)}_cl{int(cl)}"] = e
+    return out
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPS_REFERENCE_ROOT")
     if not ref_root:
         raise SystemExit("usage: make_golden.py <reference root>")
     ew, cap = _import_reference(ref_root)
-    for name, fn in (("small", case_small), ("c1", case_c1)):
+    for name, fn in (("small", case_small), ("c1", case_c1), ("forces", case_forces)):
         t0 = time.perf_counter()
         d = fn(ew, cap)
         np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **d)
