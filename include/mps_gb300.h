@@ -64,6 +64,20 @@ int mps_abi_version(void);
  * each with its r = 0 self value in column 0. */
 int mps_real_space_table(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
 
+/* Replaces the dipole + quadrupole couplings of Capacitance_Quadrupole/RealSpaceTable.m:171-378.
+ * r: n separations (no zero).  tables: 7 x (n+1) float64, rows field_quad_1,
+ * field_quad_2, field_quad_3, grad_quad_1, grad_quad_2, grad_quad_3, grad_quad_4,
+ * each with its r = 0 value in column 0 (the grad_quad_2 self value, zero for
+ * the others).  field_dip_1/2 come from mps_real_space_table. */
+int mps_quad_table(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
+
+/* Replaces Capacitance_Sizes/RealSpaceTable.m:1-149 [Ep_perp, Ep_para] = RealSpaceTable(r, a, xi).
+ * r: device n separations with r[0] = 0 (row 0 holds the r -> 0 value).
+ * a_uniq: device M distinct radii.  perp, para: device M(M+1)/2 x n, column of
+ * radii pair (i <= j) at index i M - i (i - 1) / 2 + (j - i), each column contiguous. */
+int mps_sizes_table(const double *r, int64_t n, const double *a_uniq, int64_t M, double xi, double *perp,
+                    double *para, mps_stream_t stream);
+
 /* Replaces EW/ewald.py:84-111 cell_list(x, box, rmax).
  * box: host double[3].  cell: n x 3 int64.  ncell: host int64[3] (output). */
 int mps_cell_list(const double *x, int64_t n, const double *box, double rmax,
@@ -157,7 +171,23 @@ typedef struct mps_system_desc {
     int64_t n_tab;
     double slab_factor;       /* EW/ewald.py:1233-1236 (1.0 in the reference)       */
     int32_t max_rhs;          /* largest batch of vectors one matvec will take      */
+    int32_t kind;             /* MPS_DIPOLE (3 unknowns per sphere),                */
+                              /* MPS_DIPOLE_QUADRUPOLE (8: S then Q xx xy xz yy yz) */
+                              /* or MPS_POLYDISPERSE (3, spheres of radii a_i)      */
+    const double *quad_tables; /* kind MPS_DIPOLE_QUADRUPOLE: device 7 x n_tab on   */
+                              /* rvals: field_quad_1..3, grad_quad_1..4, r = 0 first */
+                              /* (CQ/RealSpaceTable.m:171-378)                       */
+    /* kind MPS_POLYDISPERSE (CS/ComputeField.m:23-57).  perp/para are unused; eta */
+    /* is the scalar P (mean(h) xi)^2 / pi in all three entries.                 */
+    const double *radius;     /* device n radii                                     */
+    const int32_t *radius_class; /* device n class of each radius (0..n_class-1), */
+                              /* or NULL: couplings in closed form per pair         */
+    int32_t n_class;          /* distinct radii M                                   */
+    const double *sizes_tables; /* device 2 x M(M+1)/2 x n_tab: Ep_perp columns then */
+                              /* Ep_para columns on rvals (rvals[0] = 0, self first) */
 } mps_system_desc;
+
+enum mps_operator_kind { MPS_DIPOLE = 0, MPS_DIPOLE_QUADRUPOLE = 1, MPS_POLYDISPERSE = 2 };
 
 /* Builds cell list, filtered CSR pair list with interpolated couplings, grid
  * geometry, Green's coefficients and FFT plans (EW/capacitance.py:369-385).

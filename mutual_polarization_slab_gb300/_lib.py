@@ -16,6 +16,7 @@ MPS_OK, MPS_BAD_ARG, MPS_RC_GT_HALF_BOX, MPS_TABLE_RANGE, MPS_NOT_CONVERGED, MPS
     MPS_NO_MEMORY, MPS_SCRATCH_LIMIT = range(9)
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 MPS_FP64, MPS_FP32 = 0, 1
+MPS_DIPOLE, MPS_DIPOLE_QUADRUPOLE, MPS_POLYDISPERSE = 0, 1, 2
 
 EXPORTS = (
     "mps_status_string", "mps_abi_version", "mps_real_space_table", "mps_cell_list",
@@ -25,7 +26,7 @@ EXPORTS = (
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
     "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
-    "mps_dipole_forces",
+    "mps_dipole_forces", "mps_quad_table", "mps_sizes_table",
 )
 
 p = C.c_void_p
@@ -41,7 +42,8 @@ class SystemDesc(C.Structure):
     _fields_ = [
         ("n", i64), ("x", p), ("lambdap", p), ("n_diag", i64), ("box", f64 * 3), ("xi", f64), ("rc", f64),
         ("Ngrid", i64 * 3), ("P", i32), ("eta", f64 * 3), ("perp", p), ("para", p), ("rvals", p),
-        ("n_tab", i64), ("slab_factor", f64), ("max_rhs", i32),
+        ("n_tab", i64), ("slab_factor", f64), ("max_rhs", i32), ("kind", i32), ("quad_tables", p),
+        ("radius", p), ("radius_class", p), ("n_class", i32), ("sizes_tables", p),
     ]
 
 
@@ -85,6 +87,8 @@ _SIGS = {
     "mps_neighbor_list_noalloc": (C.c_int, [p, i64, P64, p, p, i64, P64, p]),
     "mps_system_tuning": (C.c_int, [p, C.POINTER(i32), C.POINTER(C.c_float)]),
     "mps_dipole_forces": (C.c_int, [p, p, i64, PD, f64, f64, i32, p, p, p]),
+    "mps_quad_table": (C.c_int, [p, i64, f64, p, p]),
+    "mps_sizes_table": (C.c_int, [p, i64, p, i64, f64, p, p, p]),
 }
 
 _lib = None

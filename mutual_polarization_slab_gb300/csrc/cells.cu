@@ -331,8 +331,9 @@ __global__ void __launch_bounds__(256) k_csr_count(const double *__restrict__ x,
 
 template <typename T>
 __device__ __forceinline__ void store_pair(PairData<T> &pd, int64_t w, int32_t b, double A, double B,
-                                           const double rh[3]) {
+                                           const double rh[3], double d) {
     pd.nbr[w] = b;
+    if (pd.dist) pd.dist[w] = (T)d;
     pd.A[w] = (T)A;
     pd.BA[w] = (T)(B - A);
     pd.rx[w] = (T)rh[0];
@@ -378,9 +379,10 @@ __global__ void __launch_bounds__(256) k_csr_fill(const double *__restrict__ x, 
                 const double inv = 1.0 / d;
                 const double rh[3] = {r[0] * inv, r[1] * inv, r[2] * inv};
                 double A = 0.0, B = 0.0;
-                if (!table_lerp(perp, para, rv, ntab, d, &A, &B, inv_dr)) atomicExch(err, 1);
-                store_pair(p64, wp, b, A, B, rh);
-                store_pair(p32, wp, b, A, B, rh);
+                // ntab == 0: the couplings are filled in afterwards from the separations
+                if (ntab > 0 && !table_lerp(perp, para, rv, ntab, d, &A, &B, inv_dr)) atomicExch(err, 1);
+                store_pair(p64, wp, b, A, B, rh, d);
+                store_pair(p32, wp, b, A, B, rh, d);
             }
             w += __popc(mask);
         }
@@ -529,8 +531,10 @@ int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double
     k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
     MPS_LAUNCH_CHECK();
     double rv_last = 0.0;
-    MPS_CUDA_TRY(cudaMemcpyAsync(&rv_last, rv + ntab - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (ntab > 0) {
+        MPS_CUDA_TRY(cudaMemcpyAsync(&rv_last, rv + ntab - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+        MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    }
     const double inv_dr = rv_last > 0 ? (double)(ntab - 1) / rv_last : 0.0;
     k_csr_fill<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], off27,

@@ -25,6 +25,7 @@ struct PairData {
     T *A;           // interpolated I - rr coupling
     T *BA;          // rr coupling minus A
     T *rx, *ry, *rz;  // unit vector from b to a (minimum image)
+    T *dist;          // separation (only kept when an operator interpolates more tables)
 };
 
 void compute_ncell(const double *box, double rmax, int64_t *ncell);

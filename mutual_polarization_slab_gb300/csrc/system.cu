@@ -14,6 +14,8 @@
 #include "grid.cuh"
 #include "realspace.cuh"
 #include "tiles.cuh"
+#include "quad.cuh"
+#include "sizes.cuh"
 
 using namespace mps;
 
@@ -81,6 +83,22 @@ struct mps_system {
     int64_t *row_ptr = nullptr;
     PairData<double> p64{};
     PairData<float> p32{};
+    // dipole + quadrupole operator (kind 1): 9 couplings per pair and the
+    // gradient/quadrupole diagonal
+    int kind = 0;
+    int ndof = 3;
+    double *qcoef = nullptr;        // n_pairs x 9 (A..I) float64
+    float *qcoef32 = nullptr;
+    double *diagq = nullptr;        // n_diag x n: 15/(8 pi (eps-1)) + grad_quad_2(0)/2
+    double *qkcoef = nullptr;       // half spectrum x 4: HES, HEQ/i, HGS/i, HGQ (with 1/G)
+    float *qkcoef32 = nullptr;
+    // polydisperse operator (kind 2): one scalar grid per vector, kernel values
+    // K(d)/d of every particle's stencil, base offset node0 h - x per particle
+    double *cs_base = nullptr;      // n x 3
+    double *cs_g64 = nullptr;       // n x P^3
+    float *cs_g32 = nullptr;
+    double *cs_h64 = nullptr;       // half spectrum: exp(-(1-eta) q^2 / 4 xi^2) / q^2 / G
+    float *cs_h32 = nullptr;
     int32_t *start = nullptr;
     double *w64 = nullptr;
     float *w32 = nullptr;
@@ -118,7 +136,8 @@ static void free_system(mps_system *s) {
     void *ptrs[] = {s->x, s->diag, s->row_ptr, s->p64.nbr, s->p64.A, s->p64.BA, s->p64.rx, s->p64.ry, s->p64.rz,
                     s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32,
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
-                    s->fft_work};
+                    s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
+                    s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -238,7 +257,8 @@ static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *o
 }
 
 static int ensure_grids(mps_system *s, int precision, cudaStream_t st) {
-    size_t nr = (size_t)s->max_rhs * 3;
+    // component grids per vector: one scalar grid for the polydisperse operator
+    size_t nr = (size_t)s->max_rhs * (s->kind == MPS_POLYDISPERSE ? 1 : s->ndof);
     if (precision == MPS_FP64) {
         if (!s->grid64) MPS_TRY(dalloc(&s->grid64, nr * s->gp.G * sizeof(double), st));
         if (!s->spec64) MPS_TRY(dalloc(&s->spec64, nr * s->Gc * 2 * sizeof(double), st));
@@ -453,12 +473,81 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     return MPS_OK;
 }
 
+// Dipole + quadrupole operator (8 moments per sphere, CQ/MatrixVectorMultiply.m:31-77):
+// the same spread / FFT / scale / FFT / contract / real-space stages over 8
+// component grids per vector.
+template <typename T>
+static int matvec_quad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    const bool dbl = sizeof(T) == 8;
+    MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
+    T *grid = dbl ? (T *)s->grid64 : (T *)s->grid32;
+    void *spec = dbl ? s->spec64 : s->spec32;
+    const T *w = dbl ? (const T *)s->w64 : (const T *)s->w32;
+    const T *kc = dbl ? (const T *)s->qkcoef : (const T *)s->qkcoef32;
+    const T *pc = dbl ? (const T *)s->qcoef : (const T *)s->qcoef32;
+    const PairData<T> &pd = *(const PairData<T> *)(dbl ? (const void *)&s->p64 : (const void *)&s->p32);
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
+    STAGE_MARK(1);
+    MPS_TRY(spread_gen<T>(m, s->n, nrhs, 8, s->start, w, s->gp, grid, st));
+    STAGE_MARK(2);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, 8 * nrhs, grid, spec, 0, st));
+    STAGE_MARK(3);
+    MPS_TRY(scale_quad<T>(spec, nrhs, s->gp, kc, st));
+    STAGE_MARK(4);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 8 * nrhs, spec, grid, 0, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract_gen<T>(grid, s->n, nrhs, 8, s->start, w, s->gp, out, st));
+    STAGE_MARK(6);
+    MPS_TRY(real_space_quad<T>(m, out, s->n, nrhs, s->row_ptr, pd.nbr, pd.rx, pd.ry, pd.rz, pc, s->diag, s->diagq,
+                               s->diag_idx, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
+// Polydisperse operator (CS/ComputeField.m:23-57): scalar spread of the dipoles
+// as charges, one FFT pair per vector, vector contraction, real space with the
+// per-pair couplings of the two radii.
+template <typename T>
+static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    const bool dbl = sizeof(T) == 8;
+    MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
+    T *grid = dbl ? (T *)s->grid64 : (T *)s->grid32;
+    void *spec = dbl ? s->spec64 : s->spec32;
+    const T *g = dbl ? (const T *)s->cs_g64 : (const T *)s->cs_g32;
+    const T *hc = dbl ? (const T *)s->cs_h64 : (const T *)s->cs_h32;
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
+    STAGE_MARK(1);
+    MPS_TRY(spread_cs<T>(m, s->n, nrhs, s->start, s->cs_base, g, s->gp, grid, st));
+    STAGE_MARK(2);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, nrhs, grid, spec, 0, st));
+    STAGE_MARK(3);
+    MPS_TRY(scale_cs<T>(spec, nrhs, s->gp, hc, st));
+    STAGE_MARK(4);
+    MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, nrhs, spec, grid, 0, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract_cs<T>(grid, s->n, nrhs, s->start, s->cs_base, g, s->gp, out, st));
+    STAGE_MARK(6);
+    if (dbl)
+        MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
+    else
+        MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
 static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+    if (s->kind == MPS_POLYDISPERSE)
+        return precision == MPS_FP64 ? matvec_cs<double>(s, m, out, nrhs, st) : matvec_cs<float>(s, m, out, nrhs, st);
+    if (s->kind == MPS_DIPOLE_QUADRUPOLE)
+        return precision == MPS_FP64 ? matvec_quad<double>(s, m, out, nrhs, st)
+                                     : matvec_quad<float>(s, m, out, nrhs, st);
     return precision == MPS_FP64 ? matvec_impl<double>(s, m, out, nrhs, st) : matvec_impl<float>(s, m, out, nrhs, st);
 }
 
 // ---------------------------------------------------------------------------
-// Krylov kernels (float64).  Vectors of length n3 = 3n; nrhs independent
+// Krylov kernels (float64).  Vectors of length n3 = ndof n; nrhs independent
 // systems stacked with stride n3 (vectors) / ld (bases).
 // ---------------------------------------------------------------------------
 constexpr int kDotThreads = 256;
@@ -738,7 +827,7 @@ struct GmresFlags {
 static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, double tol, int restart, int maxit,
                       int precision, int *conv, double *relres_out, int *cycles_out, int *mv_count,
                       cudaStream_t st, GmresFlags fl = GmresFlags()) {
-    const int64_t n3 = 3 * s->n;
+    const int64_t n3 = (int64_t)s->ndof * s->n;
     const int ld = restart + 1;
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     const int64_t ldv = (int64_t)nrhs * n3;
@@ -947,7 +1036,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
 // Relative residuals ||b - A x|| / ||b|| with the float64 operator; r receives b - A x.
 static int true_residual(mps_system *s, const double *b, const double *x, double *r, double *ax, int nrhs,
                          double *partial, double *nrm, std::vector<double> &relres, cudaStream_t st) {
-    const int64_t n3 = 3 * s->n;
+    const int64_t n3 = (int64_t)s->ndof * s->n;
     MPS_TRY(matvec_any(s, x, ax, nrhs, MPS_FP64, st));
     k_sub<<<grid_for((int64_t)nrhs * n3, 256), 256, 0, st>>>(b, ax, r, (int64_t)nrhs * n3);
     MPS_LAUNCH_CHECK();
@@ -983,7 +1072,7 @@ static int rel_norms(const double *r, const double *b, int64_t n3, int nrhs, dou
 // recomputes b - A64 x.  verify != 0 adds a final float64 true residual.
 static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, const mps_solve_opts *o, int *conv,
                         double *relres_out, int *cycles_out, int *mv64, int *mv32, cudaStream_t st) {
-    const int64_t n3 = 3 * s->n;
+    const int64_t n3 = (int64_t)s->ndof * s->n;
     const int64_t tot = (int64_t)nrhs * n3;
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
@@ -1094,8 +1183,16 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     *out = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     if (d->n < 1 || !d->x || !d->lambdap || d->n_diag < 1 || !(d->xi > 0) || !(d->rc > 0) || d->P < 1 ||
-        !d->perp || !d->para || !d->rvals || d->n_tab < 2 || d->max_rhs < 1)
+        d->max_rhs < 1)
         return MPS_BAD_ARG;
+    if (d->kind != MPS_DIPOLE && d->kind != MPS_DIPOLE_QUADRUPOLE && d->kind != MPS_POLYDISPERSE) return MPS_BAD_ARG;
+    if (d->kind != MPS_POLYDISPERSE && (!d->perp || !d->para || !d->rvals || d->n_tab < 2)) return MPS_BAD_ARG;
+    if (d->kind == MPS_POLYDISPERSE) {
+        if (!d->radius || d->slab_factor != 0.0) return MPS_BAD_ARG;
+        if (d->radius_class && (!d->sizes_tables || !d->rvals || d->n_tab < 2 || d->n_class < 1)) return MPS_BAD_ARG;
+    }
+    // the quadrupole operator has no slab term (CQ/MatrixVectorMultiply.m)
+    if (d->kind == MPS_DIPOLE_QUADRUPOLE && (!d->quad_tables || d->slab_factor != 0.0)) return MPS_BAD_ARG;
     for (int k = 0; k < 3; ++k) {
         if (!(d->box[k] > 0) || d->Ngrid[k] < 1) return MPS_BAD_ARG;
         if (d->Ngrid[k] < d->P) return MPS_BAD_ARG;  // the stencil wraps at most once
@@ -1112,6 +1209,8 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     s->xi = d->xi;
     s->rc = d->rc;
     s->slab_factor = d->slab_factor;
+    s->kind = d->kind;
+    s->ndof = d->kind == MPS_DIPOLE_QUADRUPOLE ? 8 : 3;
     s->gp = make_grid_params(d->Ngrid, d->box, d->xi, d->eta, d->P);
     s->Gc = (int64_t)(s->gp.N[0] / 2 + 1) * s->gp.N[1] * s->gp.N[2];
     const int64_t n = d->n;
@@ -1128,7 +1227,11 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (cudaMemcpyAsync(s->x, d->x, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         CR_TRY(MPS_CUDA_ERR);
     CR_TRY(dalloc(&s->diag, sizeof(double) * n * d->n_diag, st));
-    CR_TRY(build_diag(d->lambdap, n * d->n_diag, d->perp, s->diag, st));
+    if (s->kind == MPS_POLYDISPERSE)
+        CR_TRY(cs_diag(d->lambdap, n, d->n_diag, d->radius, d->radius_class, d->n_class,
+                       d->radius_class ? d->sizes_tables : nullptr, d->n_tab, d->xi, s->diag, st));
+    else
+        CR_TRY(build_diag(d->lambdap, n * d->n_diag, d->perp, s->diag, st));
     CR_TRY(dalloc(&s->slab, sizeof(double) * d->max_rhs, st));
     if (cudaMemsetAsync(s->slab, 0, sizeof(double) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * d->max_rhs, st));
@@ -1186,18 +1289,75 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (!rc) rc = dalloc(&s->p32.ry, sizeof(float) * np, st);
     if (!rc) rc = dalloc(&s->p32.rz, sizeof(float) * np, st);
     s->p32.nbr = s->p64.nbr;
+    if (!rc && s->kind != MPS_DIPOLE) rc = dalloc(&s->p64.dist, sizeof(double) * np, st);
+    // the polydisperse couplings depend on the pair's radii: filled in below
+    const int64_t fill_ntab = s->kind == MPS_POLYDISPERSE ? 0 : d->n_tab;
     if (!rc && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
     if (!rc)
-        rc = csr_pairs_fill(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, d->perp, d->para, d->rvals, d->n_tab, s->row_ptr,
-                            s->p64, s->p32, err, st);
+        rc = csr_pairs_fill(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, d->perp, d->para, d->rvals, fill_ntab,
+                            s->row_ptr, s->p64, s->p32, err, st);
     int herr = 0;
     if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = MPS_CUDA_ERR;
     if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
     tmp_free();
     if (!rc && herr) rc = MPS_TABLE_RANGE;
+    if (!rc && s->kind == MPS_POLYDISPERSE) {
+        int *perr = nullptr;
+        rc = dalloc(&perr, sizeof(int), st);
+        if (!rc && cudaMemsetAsync(perr, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
+        if (!rc)
+            rc = cs_pair_coefs(s->row_ptr, s->p64.nbr, s->p64.dist, n, d->radius, d->radius_class, d->n_class,
+                               d->radius_class ? d->sizes_tables : nullptr, d->rvals, d->n_tab, d->xi, s->p64, s->p32,
+                               perr, st);
+        if (!rc && cudaMemcpyAsync(&herr, perr, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = MPS_CUDA_ERR;
+        if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+        if (perr) cudaFreeAsync(perr, st);
+        if (!rc && herr) rc = MPS_TABLE_RANGE;
+        if (s->p64.dist) cudaFreeAsync(s->p64.dist, st);
+        s->p64.dist = nullptr;
+    }
+    if (!rc && s->kind == MPS_DIPOLE_QUADRUPOLE) {
+        // nine couplings per pair from the stored separations, then the
+        // separations are dropped
+        rc = dalloc(&s->qcoef, sizeof(double) * 9 * np, st);
+        if (!rc) rc = dalloc(&s->qcoef32, sizeof(float) * 9 * np, st);
+        int *qerr = nullptr;
+        if (!rc) rc = dalloc(&qerr, sizeof(int), st);
+        if (!rc && cudaMemsetAsync(qerr, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
+        if (!rc)
+            rc = quad_pair_coefs(s->p64.dist, np, d->perp, d->para, d->quad_tables, d->rvals, d->n_tab, s->qcoef,
+                                 s->qcoef32, qerr, st);
+        if (!rc && cudaMemcpyAsync(&herr, qerr, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = MPS_CUDA_ERR;
+        if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+        if (qerr) cudaFreeAsync(qerr, st);
+        if (!rc && herr) rc = MPS_TABLE_RANGE;
+        if (s->p64.dist) cudaFreeAsync(s->p64.dist, st);
+        s->p64.dist = nullptr;
+        if (!rc) rc = dalloc(&s->diagq, sizeof(double) * n * d->n_diag, st);
+        if (!rc) rc = quad_diag(d->lambdap, n * d->n_diag, d->quad_tables + 4 * d->n_tab, s->diagq, st);
+        if (!rc) rc = dalloc(&s->qkcoef, sizeof(double) * 4 * s->Gc, st);
+        if (!rc) rc = dalloc(&s->qkcoef32, sizeof(float) * 4 * s->Gc, st);
+        if (!rc) rc = quad_kcoef(s->gp, s->qkcoef, s->qkcoef32, st);
+    }
     if (rc) {
         free_system(s);
         return rc;
+    }
+    if (s->kind == MPS_POLYDISPERSE) {
+        const int64_t P3 = (int64_t)d->P * d->P * d->P;
+        CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n, st));
+        CR_TRY(dalloc(&s->cs_base, sizeof(double) * 3 * n, st));
+        CR_TRY(dalloc(&s->cs_g64, sizeof(double) * n * P3, st));
+        CR_TRY(dalloc(&s->cs_g32, sizeof(float) * n * P3, st));
+        CR_TRY(dalloc(&s->cs_h64, sizeof(double) * s->Gc, st));
+        CR_TRY(dalloc(&s->cs_h32, sizeof(float) * s->Gc, st));
+        CR_TRY(cs_geometry(s->x, n, s->gp, d->radius, d->xi, s->gp.eta[0], s->start, s->cs_base, s->cs_g64,
+                           s->cs_g32, st));
+        CR_TRY(cs_green(s->gp, s->gp.eta[0], d->xi, s->cs_h64, s->cs_h32, st));
+        *out = s;
+        return MPS_OK;
     }
     // grid geometry + Green's coefficients
     CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n, st));
@@ -1258,7 +1418,7 @@ extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t
 
 extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *out_ri, int32_t diag_index,
                                   mps_stream_t stream) {
-    if (!sys || !m_ri || !out_ri || sys->max_rhs < 2) return MPS_BAD_ARG;
+    if (!sys || !m_ri || !out_ri || sys->max_rhs < 2 || sys->kind != MPS_DIPOLE) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     int32_t di[2] = {diag_index, diag_index};
     MPS_TRY(upload_diag_idx(sys, di, 2, st));
@@ -1286,7 +1446,7 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
     if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
-    const int64_t n3 = 3 * sys->n;
+    const int64_t n3 = (int64_t)sys->ndof * sys->n;
     const size_t vbytes = sizeof(double) * (size_t)nrhs * n3;
     if (x0 == nullptr) {
         MPS_CUDA_TRY(cudaMemsetAsync(x, 0, vbytes, st));

@@ -56,10 +56,22 @@ class SpectralEwaldSystem:
     contrast spectrum), ``box``, ``xi``, cutoff ``rc``, grid ``Ngrid``, support
     ``P``, tables ``perp``/``para`` on separations ``rvals`` (``rvals[0] = 0``,
     self value in ``perp[0]``), ``slab_factor``.
+
+    With ``quad_tables`` (a (7, n_tab) array: field_quad_1..3, grad_quad_1..4 on
+    ``rvals``) the object is the dipole + quadrupole operator of
+    ``Capacitance_Quadrupole/MatrixVectorMultiply.m``: 8 unknowns per sphere,
+    stored per particle as (Sx, Sy, Sz, Qxx, Qxy, Qxz, Qyy, Qyz); it has no slab term.
+
+    With ``radius`` (N radii) it is the polydisperse operator of
+    ``Capacitance_Sizes/ComputeField.m`` (scalar eta, no slab term; ``perp``,
+    ``para`` unused).  ``sizes_tables`` ((2, M(M+1)/2, n_tab) on ``rvals``) with
+    ``radius_class`` (class of each particle among ``n_class`` distinct radii)
+    interpolates the couplings like ``CS/RealSpace.m``; without them every pair's
+    couplings are evaluated in closed form at its separation.
     """
 
     def __init__(self, x, lambdap, box, xi, rc, Ngrid, P, perp, para, rvals, slab_factor=1.0, eta=None,
-                 max_rhs=3):
+                 max_rhs=3, quad_tables=None, radius=None, radius_class=None, n_class=0, sizes_tables=None):
         lib = L.lib()
         self._lib = lib
         self._h = C.c_void_p(0)
@@ -78,9 +90,34 @@ class SpectralEwaldSystem:
         self.P = int(P)
         self.slab_factor = float(slab_factor)
         self.max_rhs = int(max_rhs)
-        self.perp = as_device(perp)
-        self.para = as_device(para)
-        self.rvals = as_device(rvals)
+        self.perp = None if perp is None else as_device(perp)
+        self.para = None if para is None else as_device(para)
+        self.rvals = None if rvals is None else as_device(rvals)
+        self.kind = L.MPS_DIPOLE if quad_tables is None else L.MPS_DIPOLE_QUADRUPOLE
+        if radius is not None:
+            if quad_tables is not None:
+                raise ValueError("radius and quad_tables select different operators")
+            self.kind = L.MPS_POLYDISPERSE
+        self.ndof = 3 if quad_tables is None else 8
+        self.radius = None if radius is None else as_device(radius).reshape(-1).contiguous()
+        self.radius_class = None if radius_class is None else as_device(radius_class, torch.int32).reshape(-1)
+        self.sizes_tables = None if sizes_tables is None else as_device(sizes_tables).contiguous()
+        if self.kind == L.MPS_POLYDISPERSE:
+            if self.radius.numel() != self.x.shape[0]:
+                raise ValueError("radius must have N entries")
+            if self.slab_factor != 0.0:
+                raise ValueError("the polydisperse operator has no slab term (slab_factor must be 0)")
+            if (self.radius_class is None) != (self.sizes_tables is None):
+                raise ValueError("radius_class and sizes_tables go together")
+            if self.sizes_tables is not None and self.sizes_tables.shape[-1] != self.rvals.numel():
+                raise ValueError("sizes_tables must have n_tab entries per column")
+        self.quad_tables = None
+        if quad_tables is not None:
+            self.quad_tables = as_device(quad_tables).reshape(7, -1).contiguous()
+            if self.quad_tables.shape[1] != self.rvals.numel():
+                raise ValueError("quad_tables must have one row of n_tab entries per coupling")
+            if self.slab_factor != 0.0:
+                raise ValueError("the dipole + quadrupole operator has no slab term (slab_factor must be 0)")
         if np.any(self.rc > self.box / 2.0):
             raise ValueError("Real-space cutoff exceeds half the box size; tolerance unmet.")
         d = L.SystemDesc()
@@ -95,12 +132,18 @@ class SpectralEwaldSystem:
         d.P = self.P
         eta = np.zeros(3) if eta is None else np.asarray(eta, dtype=np.float64).reshape(3)
         d.eta = (C.c_double * 3)(*eta)
-        d.perp = self.perp.data_ptr()
-        d.para = self.para.data_ptr()
-        d.rvals = self.rvals.data_ptr()
-        d.n_tab = int(self.rvals.numel())
+        d.perp = self.perp.data_ptr() if self.perp is not None else None
+        d.para = self.para.data_ptr() if self.para is not None else None
+        d.rvals = self.rvals.data_ptr() if self.rvals is not None else None
+        d.n_tab = int(self.rvals.numel()) if self.rvals is not None else 0
         d.slab_factor = self.slab_factor
         d.max_rhs = self.max_rhs
+        d.kind = self.kind
+        d.quad_tables = self.quad_tables.data_ptr() if self.quad_tables is not None else None
+        d.radius = self.radius.data_ptr() if self.radius is not None else None
+        d.radius_class = self.radius_class.data_ptr() if self.radius_class is not None else None
+        d.n_class = int(n_class)
+        d.sizes_tables = self.sizes_tables.data_ptr() if self.sizes_tables is not None else None
         L.check(lib.mps_system_create(C.byref(d), C.byref(self._h), L.stream_handle()), "mps_system_create")
         np_ = C.c_int64(0)
         nc = (C.c_int64 * 3)()
@@ -159,10 +202,11 @@ class SpectralEwaldSystem:
         return arr
 
     def matvec(self, m, precision="fp64", diag_index=None, out=None) -> torch.Tensor:
-        """Field at the particles from real moments ``m`` of shape (N,3) or (R,N,3)."""
+        """Field at the particles from real moments ``m`` of shape (N,ndof) or (R,N,ndof)
+        (ndof = 3, or 8 for the dipole + quadrupole operator)."""
         m = as_device(m)
         single = m.dim() == 2
-        m = m.reshape(-1, self.n, 3).contiguous()
+        m = m.reshape(-1, self.n, self.ndof).contiguous()
         nrhs = m.shape[0]
         if out is None:
             out = torch.empty_like(m)
@@ -187,13 +231,13 @@ class SpectralEwaldSystem:
         """GMRES (``precision='fp64'``) or float64 iterative refinement around a
         float32-operator GMRES (``'mixed'``) for R right-hand sides at once.
 
-        ``b``, ``x0``: (N,3) or (R,N,3).  Returns (x, [SolveInfo] * R)."""
+        ``b``, ``x0``: (N,ndof) or (R,N,ndof).  Returns (x, [SolveInfo] * R)."""
         b = as_device(b)
         single = b.dim() == 2
-        b = b.reshape(-1, self.n, 3).contiguous()
+        b = b.reshape(-1, self.n, self.ndof).contiguous()
         nrhs = b.shape[0]
         x = torch.empty_like(b)
-        x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, 3).contiguous()
+        x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, self.ndof).contiguous()
         opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
                            precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit),
                            residual_policy=int(residual_policy), verify=1 if verify else 0)
