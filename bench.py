@@ -161,7 +161,8 @@ def run_gpu(args):
     def step_mixed(prof=False):
         s = make_system(prof)
         sol, info = s.solve(b, x0, tol=tol, restart=restart, maxit=args.maxref, precision="mixed",
-                            inner_tol=args.inner_tol, inner_maxit=args.inner_maxit)
+                            inner_tol=args.inner_tol, inner_maxit=args.inner_maxit,
+                            residual_precision=args.resid)
         return s, sol, info
 
     def step_fp64_plain():
@@ -325,7 +326,9 @@ def roofline(w, st):
             "traffic": None,
             "stage_ms_per_matvec_fp32": {k: v / cnt for k, v in ms.items()},
             "stage_ms_per_matvec_fp64": ({k: v / st["fp64"][0] for k, v in st["fp64"][1].items()}
-                                         if st["fp64"][0] else None)}
+                                         if st["fp64"][0] else None),
+            "stage_ms_per_matvec_df": ({k: v / st["df"][0] for k, v in st["df"][1].items()}
+                                       if st["df"][0] else None)}
 
 
 def run_e2e(args, w, world):
@@ -343,7 +346,7 @@ def run_e2e(args, w, world):
         C, S, info = gcap.capacitance_tensor(xh, eh, w["box"], guess, w["xi"], args.tol, rc=w["rc"],
                                              Ngrid=w["Ngrid"], P=w["P"], restart=args.restart, maxit=args.maxref,
                                              precision="mixed", inner_tol=args.inner_tol,
-                                             inner_maxit=args.inner_maxit)
+                                             inner_maxit=args.inner_maxit, residual_precision=args.resid)
         return C, S
 
     for _ in range(max(1, args.warmup - 1)):
@@ -427,6 +430,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-7)
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--maxref", type=int, default=8)
+    ap.add_argument("--resid", default="df", choices=["df", "fp64"],
+                    help="operator of the refinement residual: double-float FFTs (df) or cuFFT float64")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=3)
     ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=2000)

@@ -48,7 +48,12 @@ enum mps_status {
 
 enum mps_precision {
     MPS_FP64 = 0,             /* every stage in float64                              */
-    MPS_FP32 = 1              /* float32 matvec (grids, FFT, pair sum), float64 I/O  */
+    MPS_FP32 = 1,             /* float32 matvec (grids, FFT, pair sum), float64 I/O  */
+    MPS_DF = 2                /* float64 matvec whose FFTs and Green's scale run in  */
+                              /* double-float arithmetic (float hi + float lo,       */
+                              /* ~48-bit significand; dipole operator, grid axes of  */
+                              /* factors 2, 3, 5 up to 1024, even Nx; otherwise the  */
+                              /* float64 path)                                        */
 };
 
 const char *mps_status_string(int status);
@@ -226,6 +231,8 @@ typedef struct mps_solve_opts {
                                  the inner GMRES's Arnoldi relation; 1 = a float64
                                  residual after every correction                     */
     int32_t verify;           /* mixed: != 0 ends with a float64 true residual        */
+    int32_t residual_precision; /* mixed: operator of the refinement residuals,       */
+                              /* MPS_FP64 (0, default) or MPS_DF                      */
 } mps_solve_opts;
 
 typedef struct mps_solve_info {
@@ -296,8 +303,9 @@ uint64_t mps_kernel_launches(void);
 int mps_system_profile(mps_system *sys, int32_t enable);
 
 /* Accumulated stage times since the last call (synchronises on the recorded
- * events): ms[14] = [float64 stages 0..6, float32 stages 0..6] in milliseconds,
- * count[2] = matvecs recorded per precision.  Resets the accumulators. */
+ * events): ms[21] = [float64 stages 0..6, float32 stages 0..6, double-float
+ * stages 0..6] in milliseconds, count[3] = matvecs recorded per precision.
+ * Resets the accumulators. */
 int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count);
 
 /* Tile depth the autotuner chose for the tiled spread/contract: tile_depth[0]

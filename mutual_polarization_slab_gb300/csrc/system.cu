@@ -16,6 +16,7 @@
 #include "tiles.cuh"
 #include "quad.cuh"
 #include "sizes.cuh"
+#include "dffft.cuh"
 
 using namespace mps;
 
@@ -123,8 +124,11 @@ struct mps_system {
     bool profile = false;
     std::vector<StageEvents> pending;
     std::vector<StageEvents> spare;
-    double stage_ms[2][kStages] = {{0}};
-    int64_t stage_count[2] = {0, 0};
+    double stage_ms[3][kStages] = {{0}};   // float64, float32, double-float matvecs
+    int64_t stage_count[3] = {0, 0, 0};
+    DfPlan3 dfp;                 // double-float FFT plans of the grid
+    int df_state = 0;            // 0 not built yet, 1 usable, -1 unsupported grid
+    int resid_prec = MPS_FP64;   // operator of the refinement residuals
 };
 
 static void free_system(mps_system *s) {
@@ -473,6 +477,46 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     return MPS_OK;
 }
 
+// Float64 matvec whose FFTs and Green's scale run in double-float arithmetic
+// (dffft.cu): the spread, contraction and pair sum are the float64 kernels.
+static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    bool use_tiles = false;
+    MPS_TRY(ensure_tiles(s, true, st, &use_tiles));
+    MPS_TRY(ensure_grids(s, MPS_FP64, st));
+    double *grid = s->grid64;
+    float4 *spec = (float4 *)s->spec64;     // float4 per complex value: the size of a double2
+    const double vol = s->box[0] * s->box[1] * s->box[2];
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, MPS_DF, &ev, st));
+    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    STAGE_MARK(1);
+    if (use_tiles)
+        MPS_TRY(spread_tiled<double>(m, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, grid, st));
+    else
+        MPS_TRY(spread<double>(m, s->n, nrhs, s->start, s->w64, s->gp, grid, st));
+    STAGE_MARK(2);
+    MPS_TRY(df_forward_xy(grid, spec, 3 * nrhs, s->gp, s->dfp, st));
+    STAGE_MARK(3);
+    MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, st));
+    STAGE_MARK(4);
+    MPS_TRY(df_inverse_yx(spec, grid, 3 * nrhs, s->gp, s->dfp, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract<double>(grid, s->n, nrhs, s->start, s->w64, s->gp, out, st));
+    STAGE_MARK(6);
+    MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
+static bool df_usable(mps_system *s) {
+    if (s->kind != MPS_DIPOLE) return false;
+    if (s->df_state == 0) {
+        if (df_plan(s->gp, &s->dfp) != MPS_OK) return false;
+        s->df_state = s->dfp.ok ? 1 : -1;
+    }
+    return s->df_state == 1;
+}
+
 // Dipole + quadrupole operator (8 moments per sphere, CQ/MatrixVectorMultiply.m:31-77):
 // the same spread / FFT / scale / FFT / contract / real-space stages over 8
 // component grids per vector.
@@ -538,6 +582,10 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
 }
 
 static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+    if (precision == MPS_DF) {
+        if (df_usable(s)) return matvec_df(s, m, out, nrhs, st);
+        precision = MPS_FP64;
+    }
     if (s->kind == MPS_POLYDISPERSE)
         return precision == MPS_FP64 ? matvec_cs<double>(s, m, out, nrhs, st) : matvec_cs<float>(s, m, out, nrhs, st);
     if (s->kind == MPS_DIPOLE_QUADRUPOLE)
@@ -1037,7 +1085,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
 static int true_residual(mps_system *s, const double *b, const double *x, double *r, double *ax, int nrhs,
                          double *partial, double *nrm, std::vector<double> &relres, cudaStream_t st) {
     const int64_t n3 = (int64_t)s->ndof * s->n;
-    MPS_TRY(matvec_any(s, x, ax, nrhs, MPS_FP64, st));
+    MPS_TRY(matvec_any(s, x, ax, nrhs, s->resid_prec, st));
     k_sub<<<grid_for((int64_t)nrhs * n3, 256), 256, 0, st>>>(b, ax, r, (int64_t)nrhs * n3);
     MPS_LAUNCH_CHECK();
     MPS_TRY(multidot(r, n3, n3, 1, r, n3, n3, nrhs, partial, nrm, 1, st));
@@ -1410,7 +1458,7 @@ extern "C" int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t 
 extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t nrhs, const int32_t *diag_index,
                           int32_t precision, mps_stream_t stream) {
     if (!sys || !m || !out || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
-    if (precision != MPS_FP64 && precision != MPS_FP32) return MPS_BAD_ARG;
+    if (precision != MPS_FP64 && precision != MPS_FP32 && precision != MPS_DF) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     return matvec_any(sys, m, out, nrhs, precision, st);
@@ -1443,7 +1491,8 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
                          mps_stream_t stream) {
     if (!sys || !b || !x || !opts || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
     if (opts->restart < 1 || opts->restart >= kMaxCols || opts->maxit < 1 || !(opts->tol > 0)) return MPS_BAD_ARG;
-    if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32) return MPS_BAD_ARG;
+    if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32 && opts->precision != MPS_DF) return MPS_BAD_ARG;
+    if (opts->residual_precision != MPS_FP64 && opts->residual_precision != MPS_DF) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     const int64_t n3 = (int64_t)sys->ndof * sys->n;
@@ -1457,9 +1506,10 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
     std::vector<double> relres(nrhs, 0.0);
     int cycles = 0, mv64 = 0, mv32 = 0;
     int rc;
-    if (opts->precision == MPS_FP64) {
-        rc = gmres_core(sys, b, x, nrhs, opts->tol, opts->restart, opts->maxit, MPS_FP64, conv.data(), relres.data(),
-                        &cycles, &mv64, st);
+    sys->resid_prec = opts->residual_precision;
+    if (opts->precision == MPS_FP64 || opts->precision == MPS_DF) {
+        rc = gmres_core(sys, b, x, nrhs, opts->tol, opts->restart, opts->maxit, opts->precision, conv.data(),
+                        relres.data(), &cycles, &mv64, st);
     } else {
         rc = refine_mixed(sys, b, x, nrhs, opts, conv.data(), relres.data(), &cycles, &mv64, &mv32, st);
     }
@@ -1485,7 +1535,7 @@ extern "C" int mps_system_stage_times(mps_system *sys, double *ms, int64_t *coun
     if (!sys || !ms || !count) return MPS_BAD_ARG;
     for (auto &e : sys->pending) {
         MPS_CUDA_TRY(cudaEventSynchronize(e.ev[kStages]));
-        const int p = e.precision == MPS_FP64 ? 0 : 1;
+        const int p = e.precision == MPS_FP64 ? 0 : (e.precision == MPS_FP32 ? 1 : 2);
         for (int k = 0; k < kStages; ++k) {
             float t = 0.f;
             MPS_CUDA_TRY(cudaEventElapsedTime(&t, e.ev[k], e.ev[k + 1]));
@@ -1495,7 +1545,7 @@ extern "C" int mps_system_stage_times(mps_system *sys, double *ms, int64_t *coun
         sys->spare.push_back(e);
     }
     sys->pending.clear();
-    for (int p = 0; p < 2; ++p) {
+    for (int p = 0; p < 3; ++p) {
         for (int k = 0; k < kStages; ++k) ms[p * kStages + k] = sys->stage_ms[p][k];
         count[p] = sys->stage_count[p];
         for (int k = 0; k < kStages; ++k) sys->stage_ms[p][k] = 0.0;

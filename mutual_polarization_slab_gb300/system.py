@@ -16,7 +16,7 @@ import torch
 
 from . import _lib as L
 
-PRECISIONS = {"fp64": L.MPS_FP64, "fp32": L.MPS_FP32, "mixed": L.MPS_FP32}
+PRECISIONS = {"fp64": L.MPS_FP64, "fp32": L.MPS_FP32, "mixed": L.MPS_FP32, "df": L.MPS_DF}
 
 
 def as_device(a, dtype=torch.float64) -> torch.Tensor:
@@ -178,11 +178,11 @@ class SpectralEwaldSystem:
 
     def stage_times(self):
         """{precision: (matvec count, {stage: total ms})} since the last call."""
-        ms = (C.c_double * 14)()
-        cnt = (C.c_int64 * 2)()
+        ms = (C.c_double * 21)()
+        cnt = (C.c_int64 * 3)()
         L.check(self._lib.mps_system_stage_times(self._h, ms, cnt))
         out = {}
-        for p, name in ((0, "fp64"), (1, "fp32")):
+        for p, name in ((0, "fp64"), (1, "fp32"), (2, "df")):
             out[name] = (int(cnt[p]), {s: float(ms[p * 7 + k]) for k, s in enumerate(self.STAGES)})
         return out
 
@@ -227,9 +227,13 @@ class SpectralEwaldSystem:
         return torch.complex(out[0], out[1])
 
     def solve(self, b, x0=None, tol=1e-8, restart=30, maxit=100, precision="fp64", inner_tol=1e-4,
-              inner_maxit=4, diag_index=None, raise_on_fail=False, residual_policy=0, verify=False):
-        """GMRES (``precision='fp64'``) or float64 iterative refinement around a
-        float32-operator GMRES (``'mixed'``) for R right-hand sides at once.
+              inner_maxit=4, diag_index=None, raise_on_fail=False, residual_policy=0, verify=False,
+              residual_precision="df"):
+        """GMRES (``precision='fp64'``, or ``'df'`` for the float64 operator with
+        double-float FFTs) or float64 iterative refinement around a float32-operator
+        GMRES (``'mixed'``) for R right-hand sides at once.  The refinement
+        residuals use ``residual_precision`` ('df': double-float FFTs, the default;
+        'fp64': cuFFT float64); operators without a double-float path use float64.
 
         ``b``, ``x0``: (N,ndof) or (R,N,ndof).  Returns (x, [SolveInfo] * R)."""
         b = as_device(b)
@@ -240,7 +244,8 @@ class SpectralEwaldSystem:
         x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, self.ndof).contiguous()
         opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
                            precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit),
-                           residual_policy=int(residual_policy), verify=1 if verify else 0)
+                           residual_policy=int(residual_policy), verify=1 if verify else 0,
+                           residual_precision=PRECISIONS[residual_precision])
         info = (L.SolveInfo * nrhs)()
         st = self._lib.mps_gmres(self._h, L.dptr(b), L.dptr(x0d) if x0d is not None else C.c_void_p(0), L.dptr(x),
                                  nrhs, self._diag_arg(nrhs, diag_index), C.byref(opts), info, L.stream_handle())
