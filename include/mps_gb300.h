@@ -252,6 +252,21 @@ int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int
               mps_stream_t stream);
 
 /* ------------------------------------------------------------------------- */
+/* Adjoint forces (no counterpart in the reference, which computes forces from */
+/* fixed point dipoles only)                                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Forces F = -dE/dx of E = -1/2 m.H0 for the converged moments m (n x 3, one
+ * field) of a dipole system, using the symmetry of the operator:
+ * F_k = -1/2 m^T (dA/dx_k) m.  perp, para, rvals, n_tab: the tables the system
+ * was created with (their segment slopes are the derivative of the interpolated
+ * couplings).  forces: n x 3.  dE_deps (optional, n): dE/d eps_k of the
+ * permittivity set diag_index.  Synchronises once. */
+int mps_adjoint_forces(mps_system *sys, const double *m, const double *perp, const double *para,
+                       const double *rvals, int64_t n_tab, int32_t diag_index, double *forces, double *dE_deps,
+                       mps_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
 /* Point-dipole pair forces (the HOOMD plugin's kernel)                        */
 /* ------------------------------------------------------------------------- */
 

@@ -26,7 +26,7 @@ EXPORTS = (
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
     "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
-    "mps_dipole_forces", "mps_quad_table", "mps_sizes_table",
+    "mps_dipole_forces", "mps_quad_table", "mps_sizes_table", "mps_adjoint_forces",
 )
 
 p = C.c_void_p
@@ -89,6 +89,7 @@ _SIGS = {
     "mps_dipole_forces": (C.c_int, [p, p, i64, PD, f64, f64, i32, p, p, p]),
     "mps_quad_table": (C.c_int, [p, i64, f64, p, p]),
     "mps_sizes_table": (C.c_int, [p, i64, p, i64, f64, p, p, p]),
+    "mps_adjoint_forces": (C.c_int, [p, p, p, p, p, i64, i32, p, p, p]),
 }
 
 _lib = None

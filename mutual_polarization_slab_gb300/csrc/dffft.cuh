@@ -1,7 +1,10 @@
-// Double-float (float hi + float lo, ~48-bit significand) 3-D real FFT pipeline
-// for the float64-accurate matvec of the refinement residual: GB300 issues
-// float32 far faster than float64, and a hand-written mixed-radix Stockham FFT
-// in double-float arithmetic replaces cuFFT's float64 R2C / C2R transforms.
+// Hand-written mixed-radix 3-D real FFT pipeline with the dipole Green's scale
+// fused into its z pass, in two arithmetics:
+//   double-float (float hi + float lo, ~48-bit significand) for the
+//   float64-accurate matvec of the refinement residual -- GB300 issues float32
+//   far faster than float64, so this replaces cuFFT's float64 R2C / C2R;
+//   float32 for the float32 operator, replacing cuFFT R2C / C2R and the
+//   separate scale pass.
 #pragma once
 
 #include "grid.cuh"
@@ -40,7 +43,18 @@ int df_plan(const GridParams &gp, DfPlan3 *out);
 int df_forward_xy(const double *grid, float4 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
                   cudaStream_t s);
 int df_z_scale_dipole(float4 *spec, int nrhs, const GridParams &gp, const DfPlan3 &pl, const double *H,
-                      cudaStream_t s);
+                      const float2 *tm6, cudaStream_t s);
+// The scale tensor of the double-float z pass, 6 double-float entries per
+// half-spectrum point (6 x Gc float2), built once per grid.
+int df_scale_table(const GridParams &gp, const double *H, float2 *tm6, cudaStream_t s);
 int df_inverse_yx(float4 *spec, double *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s);
+
+// The same transforms in float32 (float2 per complex value) for the float32
+// operator: the z pass, Green's scale and inverse z pass fused as above.
+int f32_forward_xy(const float *grid, float2 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
+                   cudaStream_t s);
+int f32_z_scale_dipole(float2 *spec, int nrhs, const GridParams &gp, const DfPlan3 &pl, const float *H,
+                       cudaStream_t s);
+int f32_inverse_yx(float2 *spec, float *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s);
 
 }  // namespace mps

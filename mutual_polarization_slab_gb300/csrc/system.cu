@@ -17,6 +17,7 @@
 #include "quad.cuh"
 #include "sizes.cuh"
 #include "dffft.cuh"
+#include "adjoint.cuh"
 
 using namespace mps;
 
@@ -129,6 +130,7 @@ struct mps_system {
     DfPlan3 dfp;                 // double-float FFT plans of the grid
     int df_state = 0;            // 0 not built yet, 1 usable, -1 unsupported grid
     int resid_prec = MPS_FP64;   // operator of the refinement residuals
+    float2 *df_tm6 = nullptr;    // double-float scale tensor, 6 x Gc
 };
 
 static void free_system(mps_system *s) {
@@ -141,7 +143,7 @@ static void free_system(mps_system *s) {
                     s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32,
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
-                    s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32};
+                    s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->df_tm6};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -434,9 +436,20 @@ static int ensure_tiles(mps_system *s, bool dbl, cudaStream_t st, bool *use) {
     return MPS_OK;
 }
 
+static bool df_usable(mps_system *s);
+
+// The float32 operator runs cuFFT R2C/C2R + a scale pass; MPS_FFT32=own in the
+// environment selects the hand-written transforms of dffft.cu (scale fused into
+// the z pass) instead, where the grid allows.
+static bool own_fft32() {
+    const char *e = getenv("MPS_FFT32");
+    return e && strcmp(e, "own") == 0;
+}
+
 template <typename T>
 static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     const bool dbl = sizeof(T) == 8;
+    const bool own_fft = !dbl && own_fft32() && df_usable(s);
     bool use_tiles = false;
     MPS_TRY(ensure_tiles(s, dbl, st, &use_tiles));
     const TileBins &tb = dbl ? s->tb64 : s->tb32;
@@ -456,12 +469,21 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     else
         MPS_TRY(spread<T>(m, s->n, nrhs, s->start, w, s->gp, grid, st));
     STAGE_MARK(2);
-    MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, 3 * nrhs, grid, spec, 0, st));
-    STAGE_MARK(3);
-    MPS_TRY(scale_half<T>(spec, nrhs, s->gp, hh, st));
-    STAGE_MARK(4);
-    MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 3 * nrhs, spec, grid, 0, st));
-    STAGE_MARK(5);
+    if (own_fft) {
+        MPS_TRY(f32_forward_xy((const float *)grid, (float2 *)spec, 3 * nrhs, s->gp, s->dfp, st));
+        STAGE_MARK(3);
+        MPS_TRY(f32_z_scale_dipole((float2 *)spec, nrhs, s->gp, s->dfp, (const float *)hh, st));
+        STAGE_MARK(4);
+        MPS_TRY(f32_inverse_yx((float2 *)spec, (float *)grid, 3 * nrhs, s->gp, s->dfp, st));
+        STAGE_MARK(5);
+    } else {
+        MPS_TRY(exec_plan(s, dbl ? CUFFT_D2Z : CUFFT_R2C, 3 * nrhs, grid, spec, 0, st));
+        STAGE_MARK(3);
+        MPS_TRY(scale_half<T>(spec, nrhs, s->gp, hh, st));
+        STAGE_MARK(4);
+        MPS_TRY(exec_plan(s, dbl ? CUFFT_Z2D : CUFFT_C2R, 3 * nrhs, spec, grid, 0, st));
+        STAGE_MARK(5);
+    }
     // float64: the warp-per-particle gather keeps more lanes busy, which is what
     // matters at GB300's float64 issue rate; float32: the shared-memory tile.
     if (use_tiles && !dbl)
@@ -477,12 +499,20 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     return MPS_OK;
 }
 
-// Float64 matvec whose FFTs and Green's scale run in double-float arithmetic
-// (dffft.cu): the spread, contraction and pair sum are the float64 kernels.
+// Float64-accurate matvec without float64 issue in the wave-space stages: the
+// tiled spread and contraction accumulate in double-float arithmetic (float64
+// weights and grids), the FFTs and Green's scale are the double-float transforms
+// of dffft.cu; the pair sum is the float64 kernel.
 static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     bool use_tiles = false;
     MPS_TRY(ensure_tiles(s, true, st, &use_tiles));
     MPS_TRY(ensure_grids(s, MPS_FP64, st));
+    if (use_tiles && !s->partial64)
+        MPS_TRY(dalloc(&s->partial64, (size_t)s->tb64.nentries * 9 * sizeof(double), st));
+    if (!s->df_tm6) {
+        MPS_TRY(dalloc(&s->df_tm6, sizeof(float2) * 6 * s->Gc, st));
+        MPS_TRY(df_scale_table(s->gp, s->h64, s->df_tm6, st));
+    }
     double *grid = s->grid64;
     float4 *spec = (float4 *)s->spec64;     // float4 per complex value: the size of a double2
     const double vol = s->box[0] * s->box[1] * s->box[2];
@@ -491,17 +521,20 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
     STAGE_MARK(1);
     if (use_tiles)
-        MPS_TRY(spread_tiled<double>(m, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, grid, st));
+        MPS_TRY(spread_tiled_df(m, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, grid, st));
     else
         MPS_TRY(spread<double>(m, s->n, nrhs, s->start, s->w64, s->gp, grid, st));
     STAGE_MARK(2);
     MPS_TRY(df_forward_xy(grid, spec, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(3);
-    MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, st));
+    MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, s->df_tm6, st));
     STAGE_MARK(4);
     MPS_TRY(df_inverse_yx(spec, grid, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(5);
-    MPS_TRY(contract<double>(grid, s->n, nrhs, s->start, s->w64, s->gp, out, st));
+    if (use_tiles)
+        MPS_TRY(contract_tiled_df(grid, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, s->partial64, out, st));
+    else
+        MPS_TRY(contract<double>(grid, s->n, nrhs, s->start, s->w64, s->gp, out, st));
     STAGE_MARK(6);
     MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
     STAGE_MARK(7);
@@ -1337,7 +1370,9 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (!rc) rc = dalloc(&s->p32.ry, sizeof(float) * np, st);
     if (!rc) rc = dalloc(&s->p32.rz, sizeof(float) * np, st);
     s->p32.nbr = s->p64.nbr;
-    if (!rc && s->kind != MPS_DIPOLE) rc = dalloc(&s->p64.dist, sizeof(double) * np, st);
+    // separations: the dipole operator keeps them for its adjoint forces, the
+    // other operators derive their couplings from them
+    if (!rc) rc = dalloc(&s->p64.dist, sizeof(double) * np, st);
     // the polydisperse couplings depend on the pair's radii: filled in below
     const int64_t fill_ntab = s->kind == MPS_POLYDISPERSE ? 0 : d->n_tab;
     if (!rc && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
@@ -1571,4 +1606,39 @@ extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, flo
         ms[2 * p + 1] = it != g_tune.end() ? it->second.ms[1] : -1.f;
     }
     return MPS_OK;
+}
+
+extern "C" int mps_adjoint_forces(mps_system *sys, const double *m, const double *perp, const double *para,
+                                  const double *rvals, int64_t n_tab, int32_t diag_index, double *forces,
+                                  double *dE_deps, mps_stream_t stream) {
+    if (!sys || !m || !perp || !para || !rvals || n_tab < 2 || !forces) return MPS_BAD_ARG;
+    if (sys->kind != MPS_DIPOLE || !sys->p64.dist) return MPS_BAD_ARG;
+    if (diag_index < 0 || diag_index >= sys->n_diag) return MPS_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = sys->n;
+    int *err = nullptr;
+    MPS_TRY(dalloc(&err, sizeof(int), st));
+    int rc = MPS_OK;
+    if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (!rc) rc = rs_force(m, n, sys->row_ptr, sys->p64, perp, para, rvals, n_tab, forces, err, st);
+    // wave space: phi = IFFT(scale(FFT(spread(m)))) in float64, then the weight-gradient contraction
+    if (!rc) rc = ensure_grids(sys, MPS_FP64, st);
+    if (!rc) rc = spread<double>(m, n, 1, sys->start, sys->w64, sys->gp, sys->grid64, st);
+    if (!rc) rc = exec_plan(sys, CUFFT_D2Z, 3, sys->grid64, sys->spec64, 0, st);
+    if (!rc) rc = scale_half<double>(sys->spec64, 1, sys->gp, sys->h64, st);
+    if (!rc) rc = exec_plan(sys, CUFFT_Z2D, 3, sys->spec64, sys->grid64, 0, st);
+    if (!rc) rc = wave_force(sys->grid64, sys->x, m, n, sys->start, sys->w64, sys->gp, forces, st);
+    if (!rc && dE_deps) {
+        double self = 0.0;
+        if (cudaMemcpyAsync(&self, perp, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            rc = MPS_CUDA_ERR;
+        if (!rc) rc = eps_grad(m, sys->diag + (int64_t)diag_index * n, self, n, dE_deps, st);
+    }
+    int herr = 0;
+    if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    cudaFreeAsync(err, st);
+    if (!rc && herr) rc = MPS_TABLE_RANGE;
+    return rc;
 }

@@ -14,6 +14,7 @@
 // Both produce the same sums as the reference's per-particle loops
 // (EW/ewald.py:370-467) up to summation order.
 #include "tiles.cuh"
+#include "dfloat.cuh"
 
 namespace mps {
 
@@ -201,12 +202,14 @@ void tile_bins_free(TileBins &tb, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // Spread
 // ---------------------------------------------------------------------------
-template <typename T, int TZ, int NR>
+// T: accumulation arithmetic (float, double, or the double-float dfv);
+// TW: stored weight type; TG: grid element type.
+template <typename T, int TZ, int NR, typename TW = T, typename TG = T>
 __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__ m, int64_t n, int r0,
-                                                      const int32_t *__restrict__ start, const T *__restrict__ w,
+                                                      const int32_t *__restrict__ start, const TW *__restrict__ w,
                                                       GridParams gp, const int64_t *__restrict__ tstart,
                                                       const int32_t *__restrict__ entries, int ntx, int nty,
-                                                      T *__restrict__ grid) {
+                                                      TG *__restrict__ grid) {
     constexpr int C = 3 * NR;
     __shared__ int3 s_off[kChunk];
     __shared__ T s_w[kChunk][3 * kMaxP];
@@ -243,7 +246,7 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
         for (int q = threadIdx.x; q < cnt * 3 * P; q += blockDim.x) {
             const int pp = q / (3 * P), k = q % (3 * P);
             const int32_t a = entries[cb + pp];
-            s_w[pp][(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+            s_w[pp][(k / P) * kMaxP + (k % P)] = (T)w[(int64_t)a * 3 * P + k];
         }
         __syncthreads();
         for (int pp = 0; pp < cnt; ++pp) {
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
             if (gz < Nz) {
                 const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
 #pragma unroll
-                for (int c = 0; c < C; ++c) grid[(int64_t)(3 * r0 + c) * G + node] = acc[z][c];
+                for (int c = 0; c < C; ++c) grid[(int64_t)(3 * r0 + c) * G + node] = (TG)acc[z][c];
             }
         }
     }
@@ -291,12 +294,13 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
 // ---------------------------------------------------------------------------
 constexpr int kRowPad = kTileX + 1;  // padded tile row: rows y and y+2 no longer share banks
 
-template <typename T, int TZ, int NR>
-__global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ grid, int r0,
-                                                        const int32_t *__restrict__ start, const T *__restrict__ w,
+// T: accumulation arithmetic; TG: grid (and weight) element type; TP: partial type.
+template <typename T, int TZ, int NR, typename TG = T, typename TP = T>
+__global__ void __launch_bounds__(256) k_contract_tiled(const TG *__restrict__ grid, int r0,
+                                                        const int32_t *__restrict__ start, const TG *__restrict__ w,
                                                         GridParams gp, const int64_t *__restrict__ tstart,
                                                         const int32_t *__restrict__ entries, int ntx, int nty,
-                                                        T *__restrict__ partial) {
+                                                        TP *__restrict__ partial) {
     constexpr int C = 3 * NR;
     constexpr int kPlane = kTileY * kRowPad;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
 #pragma unroll
             for (int c = 0; c < C; ++c)
                 tile[(c * TZ + z) * kPlane + ty * kRowPad + tx] =
-                    (in && gz < Nz) ? grid[(int64_t)(3 * r0 + c) * G + node] : (T)0;
+                    (in && gz < Nz) ? (T)grid[(int64_t)(3 * r0 + c) * G + node] : (T)0;
         }
     }
     __syncthreads();
@@ -333,7 +337,7 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
         if (ox < 0) ox += Nx;
         if (oy < 0) oy += Ny;
         if (oz < 0) oz += Nz;
-        for (int k = lane; k < 3 * P; k += 32) wb[(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+        for (int k = lane; k < 3 * P; k += 32) wb[(k / P) * kMaxP + (k % P)] = (T)w[(int64_t)a * 3 * P + k];
         // stencil columns / rows / planes of this particle that fall inside the tile (and the grid)
         int xr = lane - ox, yr = lane - oy, zr = lane - oz;
         if (xr < 0) xr += Nx;
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(256) k_contract_tiled(const T *__restrict__ gr
         for (int c = 0; c < C; ++c) acc[c] = warp_sum(acc[c]);
         if (lane == 0) {
 #pragma unroll
-            for (int c = 0; c < C; ++c) partial[e * C + c] = acc[c];
+            for (int c = 0; c < C; ++c) partial[e * C + c] = (TP)acc[c];
         }
         __syncwarp();
     }
@@ -397,23 +401,23 @@ __global__ void k_contract_gather(const T *__restrict__ partial, int64_t n, int 
     }
 }
 
-template <typename T, int TZ, int NR>
-static int spread_launch(const double *m, int64_t n, int r0, const int32_t *start, const T *w, const GridParams &gp,
-                         const TileBins &tb, T *grid, cudaStream_t s) {
-    k_spread_tiled<T, TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, gp, tb.tile_start, tb.entries,
-                                                                   tb.ntx, tb.nty, grid);
+template <typename T, int TZ, int NR, typename TW, typename TG>
+static int spread_launch(const double *m, int64_t n, int r0, const int32_t *start, const TW *w, const GridParams &gp,
+                         const TileBins &tb, TG *grid, cudaStream_t s) {
+    k_spread_tiled<T, TZ, NR, TW, TG><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, gp, tb.tile_start,
+                                                                           tb.entries, tb.ntx, tb.nty, grid);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
 
-template <typename T, int TZ>
-static int spread_dispatch(const double *m, int64_t n, int nrhs, const int32_t *start, const T *w,
-                           const GridParams &gp, const TileBins &tb, T *grid, cudaStream_t s) {
+template <typename T, int TZ, typename TW, typename TG>
+static int spread_dispatch(const double *m, int64_t n, int nrhs, const int32_t *start, const TW *w,
+                           const GridParams &gp, const TileBins &tb, TG *grid, cudaStream_t s) {
     for (int r0 = 0; r0 < nrhs; r0 += 3) {
         const int nr = min(3, nrhs - r0);
-        int rc = nr == 3 ? spread_launch<T, TZ, 3>(m, n, r0, start, w, gp, tb, grid, s)
-                 : nr == 2 ? spread_launch<T, TZ, 2>(m, n, r0, start, w, gp, tb, grid, s)
-                           : spread_launch<T, TZ, 1>(m, n, r0, start, w, gp, tb, grid, s);
+        int rc = nr == 3 ? spread_launch<T, TZ, 3, TW, TG>(m, n, r0, start, w, gp, tb, grid, s)
+                 : nr == 2 ? spread_launch<T, TZ, 2, TW, TG>(m, n, r0, start, w, gp, tb, grid, s)
+                           : spread_launch<T, TZ, 1, TW, TG>(m, n, r0, start, w, gp, tb, grid, s);
         if (rc) return rc;
     }
     return MPS_OK;
@@ -422,38 +426,45 @@ static int spread_dispatch(const double *m, int64_t n, int nrhs, const int32_t *
 template <typename T>
 int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
                  const TileBins &tb, T *grid, cudaStream_t s) {
-    if (tb.tz == 8) return spread_dispatch<T, 8>(m, n, nrhs, start, w, gp, tb, grid, s);
-    if (tb.tz == 4) return spread_dispatch<T, 4>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 8) return spread_dispatch<T, 8, T, T>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 4) return spread_dispatch<T, 4, T, T>(m, n, nrhs, start, w, gp, tb, grid, s);
     return MPS_BAD_ARG;
 }
 
-template <typename T, int TZ, int NR>
-static int contract_launch(const T *grid, int64_t n, int r0, const int32_t *start, const T *w, const GridParams &gp,
-                           const TileBins &tb, T *partial, double *out, cudaStream_t s) {
+int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
+                    const TileBins &tb, double *grid, cudaStream_t s) {
+    if (tb.tz == 8) return spread_dispatch<dfv, 8, double, double>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 4) return spread_dispatch<dfv, 4, double, double>(m, n, nrhs, start, w, gp, tb, grid, s);
+    return MPS_BAD_ARG;
+}
+
+template <typename T, int TZ, int NR, typename TG, typename TP>
+static int contract_launch(const TG *grid, int64_t n, int r0, const int32_t *start, const TG *w,
+                           const GridParams &gp, const TileBins &tb, TP *partial, double *out, cudaStream_t s) {
     constexpr int C = 3 * NR;
     const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileY * kRowPad + 8 * 3 * kMaxP);
     static bool attr_set = false;  // one attribute call per instantiation
     if (!attr_set) {
-        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
+        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR, TG, TP>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    k_contract_tiled<T, TZ, NR><<<(unsigned)tb.ntiles, 256, smem, s>>>(grid, r0, start, w, gp, tb.tile_start,
-                                                                       tb.entries, tb.ntx, tb.nty, partial);
+    k_contract_tiled<T, TZ, NR, TG, TP><<<(unsigned)tb.ntiles, 256, smem, s>>>(grid, r0, start, w, gp, tb.tile_start,
+                                                                               tb.entries, tb.ntx, tb.nty, partial);
     MPS_LAUNCH_CHECK();
-    k_contract_gather<T, NR><<<grid_for(n, 256), 256, 0, s>>>(partial, n, r0, tb.pstart, tb.pentry, gp.hprod, out);
+    k_contract_gather<TP, NR><<<grid_for(n, 256), 256, 0, s>>>(partial, n, r0, tb.pstart, tb.pentry, gp.hprod, out);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
 
-template <typename T, int TZ>
-static int contract_dispatch(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w,
-                             const GridParams &gp, const TileBins &tb, T *partial, double *out, cudaStream_t s) {
+template <typename T, int TZ, typename TG, typename TP>
+static int contract_dispatch(const TG *grid, int64_t n, int nrhs, const int32_t *start, const TG *w,
+                             const GridParams &gp, const TileBins &tb, TP *partial, double *out, cudaStream_t s) {
     for (int r0 = 0; r0 < nrhs; r0 += 3) {
         const int nr = min(3, nrhs - r0);
-        int rc = nr == 3 ? contract_launch<T, TZ, 3>(grid, n, r0, start, w, gp, tb, partial, out, s)
-                 : nr == 2 ? contract_launch<T, TZ, 2>(grid, n, r0, start, w, gp, tb, partial, out, s)
-                           : contract_launch<T, TZ, 1>(grid, n, r0, start, w, gp, tb, partial, out, s);
+        int rc = nr == 3 ? contract_launch<T, TZ, 3, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                 : nr == 2 ? contract_launch<T, TZ, 2, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                           : contract_launch<T, TZ, 1, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s);
         if (rc) return rc;
     }
     return MPS_OK;
@@ -462,8 +473,15 @@ static int contract_dispatch(const T *grid, int64_t n, int nrhs, const int32_t *
 template <typename T>
 int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
                    const TileBins &tb, T *partial, double *out, cudaStream_t s) {
-    if (tb.tz == 8) return contract_dispatch<T, 8>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
-    if (tb.tz == 4) return contract_dispatch<T, 4>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 8) return contract_dispatch<T, 8, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 4) return contract_dispatch<T, 4, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    return MPS_BAD_ARG;
+}
+
+int contract_tiled_df(const double *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
+                      const GridParams &gp, const TileBins &tb, double *partial, double *out, cudaStream_t s) {
+    if (tb.tz == 8) return contract_dispatch<dfv, 8, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 4) return contract_dispatch<dfv, 4, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
     return MPS_BAD_ARG;
 }
 

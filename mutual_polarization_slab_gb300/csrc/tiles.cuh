@@ -37,4 +37,11 @@ template <typename T>
 int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
                    const TileBins &tb, T *partial, double *out, cudaStream_t s);
 
+// The same kernels with double-float accumulation (float-pair arithmetic) on
+// float64 weights and grids: the float64-accurate matvec without float64 issue.
+int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
+                    const TileBins &tb, double *grid, cudaStream_t s);
+int contract_tiled_df(const double *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
+                      const GridParams &gp, const TileBins &tb, double *partial, double *out, cudaStream_t s);
+
 }  // namespace mps

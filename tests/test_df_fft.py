@@ -1,8 +1,11 @@
-"""Double-float FFT path (precision 'df'): the float64-accurate matvec whose FFTs
-and Green's scale run in float-pair arithmetic.  Checked against the float64
+"""Hand-written FFT paths: precision 'df' (the float64-accurate matvec whose FFTs
+and Green's scale run in float-pair arithmetic) and the float32 operator (same
+transforms in float32).  Checked against the float64
 (cuFFT) operator and the oracle on grids that exercise every radix (2, 3, 4, 5),
 odd Ny / Nz (unpaired x rows), and the fallback for unsupported grids.
 Tolerance: 1e-12 relative (max-norm), the float64 operators' bar."""
+import os
+
 import numpy as np
 import pytest
 
@@ -40,6 +43,14 @@ def test_df_matvec_matches_fp64_and_oracle(config, Ngrid):
     o64 = s.matvec(m, precision="fp64").cpu().numpy()
     odf = s.matvec(m, precision="df").cpu().numpy()
     assert _rel(odf, o64) < 1e-12
+    o32 = s.matvec(m, precision="fp32").cpu().numpy()     # float32 operator, cuFFT
+    assert _rel(o32, o64) < 2e-5
+    os.environ["MPS_FFT32"] = "own"                        # float32 operator on the hand-written FFT
+    try:
+        o32own = s.matvec(m, precision="fp32").cpu().numpy()
+    finally:
+        del os.environ["MPS_FFT32"]
+    assert _rel(o32own, o64) < 2e-5
     pn, pa, rvn = ew.default_table(xi)
     g = ew.Geometry(x, eps, box, xi, rc, Ngrid, P, pn, pa, rvn, slab_factor=1.0)
     assert _rel(odf[1], g.field_real(m[1])) < 1e-12
