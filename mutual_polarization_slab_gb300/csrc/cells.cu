@@ -201,6 +201,38 @@ __device__ __forceinline__ bool table_lerp(const double *__restrict__ perp, cons
     return true;
 }
 
+// 1/sqrt(s) by Newton's method y <- y (3 - s y^2) / 2 from a float32 seed: two
+// steps take the seed's ~2^-22 relative error below float64 rounding.
+__device__ __forceinline__ double rsqrt_newton(double s) {
+    double y = (double)rsqrtf((float)s);
+    y = y * (1.5 - 0.5 * s * y * y);
+    y = y * (1.5 - 0.5 * s * y * y);
+    return y;
+}
+
+// 1/v by Newton's method y <- y (2 - v y) from a float32 seed (two steps).
+__device__ __forceinline__ double rcp_newton(double v) {
+    double y = (double)(1.0f / (float)v);
+    y = y * (2.0 - v * y);
+    y = y * (2.0 - v * y);
+    return y;
+}
+
+// table_lerp with the segment's reciprocal from Newton iterations (solver lists:
+// agreement with table_lerp to float64 rounding, not bit-exact).
+__device__ __forceinline__ bool table_lerp_fast(const double *__restrict__ perp, const double *__restrict__ para,
+                                                const double *__restrict__ rv, int64_t ntab, double d, double *A,
+                                                double *B, double inv_dr) {
+    int64_t i = search_left_guess(rv, ntab, d, inv_dr);
+    if (i <= 0 || i >= ntab) return false;
+    const double rl = rv[i - 1], rh = rv[i];
+    const double t = (d - rl) * rcp_newton(rh - rl);
+    const double omt = 1.0 - t;
+    *A = perp[i - 1] * omt + perp[i] * t;
+    *B = para[i - 1] * omt + para[i] * t;
+    return true;
+}
+
 __global__ void k_pair_flag(const double *__restrict__ x, double Lx, double Ly, double Lz,
                             const int64_t *__restrict__ p1, const int64_t *__restrict__ p2, int64_t ncand, double rc,
                             int32_t *__restrict__ flag) {
@@ -290,6 +322,26 @@ __device__ __forceinline__ double pair_exact(const double *__restrict__ x, int64
     return __dsqrt_rn(s);
 }
 
+// Minimum-image difference x_a - x_b (same rounding as pair_exact) and its
+// squared length; big = a coordinate difference of a box length or more (then
+// the caller uses pair_exact, which wraps by the general rule).
+__device__ __forceinline__ double pair_diff2(const double *__restrict__ x, int64_t a, int64_t b, const PairScreen &ps,
+                                             double r[3], bool *big) {
+    bool bg = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = __dsub_rn(x[3 * a + k], x[3 * b + k]);
+        bg = bg || !(fabs(v) < ps.L[k]);
+        if (v >= 0.5 * ps.L[k])
+            v = __dsub_rn(v, ps.L[k]);
+        else if (v <= -0.5 * ps.L[k])
+            v = __dadd_rn(v, ps.L[k]);
+        r[k] = v;
+    }
+    *big = bg;
+    return __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+}
+
 // Filtered per-particle neighbour counts, slot (a, o) at a*27 + o.  One warp per
 // (particle, neighbour cell): lanes take the cell's particles, a ballot counts
 // the kept ones.
@@ -365,22 +417,35 @@ __global__ void __launch_bounds__(256) k_csr_fill(const double *__restrict__ x, 
             const int64_t j = j0 + lane;
             bool keep = false;
             int32_t b = -1;
-            double r[3] = {0, 0, 0}, d = 0.0;
+            double r[3] = {0, 0, 0}, s2 = 0.0;
             if (j < len) {
                 b = sorted[b0 + j];
-                if (b != a && pair_screen(xf, a, b, ps) != SCREEN_OUT) {
-                    d = pair_exact(x, a, b, ps, r);
-                    keep = d < ps.rc;
+                const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
+                if (sc != SCREEN_OUT) {
+                    bool big = false;
+                    s2 = pair_diff2(x, a, b, ps, r, &big);
+                    if (big) {
+                        const double de = pair_exact(x, a, b, ps, r);
+                        s2 = __dmul_rn(de, de);
+                        keep = de < ps.rc;
+                    } else {
+                        // inside the screen's inner margin: kept for sure; near rc: the
+                        // correctly rounded separation decides, as in the count pass
+                        keep = sc == SCREEN_IN || __dsqrt_rn(s2) < ps.rc;
+                    }
                 }
             }
             const unsigned mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const int64_t wp = w + __popc(mask & ((1u << lane) - 1u));
-                const double inv = 1.0 / d;
-                const double rh[3] = {r[0] * inv, r[1] * inv, r[2] * inv};
+                // the float64 division and square root are the slow part of this
+                // kernel on GB300: Newton iterations from float32 seeds instead
+                const double y = rsqrt_newton(s2);
+                const double d = s2 * y;
+                const double rh[3] = {r[0] * y, r[1] * y, r[2] * y};
                 double A = 0.0, B = 0.0;
                 // ntab == 0: the couplings are filled in afterwards from the separations
-                if (ntab > 0 && !table_lerp(perp, para, rv, ntab, d, &A, &B, inv_dr)) atomicExch(err, 1);
+                if (ntab > 0 && !table_lerp_fast(perp, para, rv, ntab, d, &A, &B, inv_dr)) atomicExch(err, 1);
                 store_pair(p64, wp, b, A, B, rh, d);
                 store_pair(p32, wp, b, A, B, rh, d);
             }

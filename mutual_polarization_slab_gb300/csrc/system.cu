@@ -16,6 +16,7 @@
 #include "tiles.cuh"
 #include "quad.cuh"
 #include "sizes.cuh"
+#include <algorithm>
 #include "dffft.cuh"
 #include "adjoint.cuh"
 
@@ -1214,8 +1215,15 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         fl.final_check = false;
         fl.ls_restart = true;
         fl.r_out = incremental ? rn : nullptr;
+        // the correction only has to take the worst residual below the target:
+        // relative tolerance max(inner_tol, 0.3 tol / relres), at most 0.5
+        double worst = 0.0;
+        for (int q = 0; q < nrhs; ++q)
+            if (!conv[q]) worst = std::max(worst, rel[q]);
+        double step_tol = inner_tol;
+        if (worst > 0.0) step_tol = std::max(inner_tol, std::min(0.5, 0.3 * o->tol / worst));
         int icyc = 0;
-        int g = gmres_core(s, r, dx, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
+        int g = gmres_core(s, r, dx, nrhs, step_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
                            mv32, st, fl);
         if (g != MPS_OK && g != MPS_NOT_CONVERGED) {
             e = g;
