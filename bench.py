@@ -162,7 +162,7 @@ def run_gpu(args):
         s = make_system(prof)
         sol, info = s.solve(b, x0, tol=tol, restart=restart, maxit=args.maxref, precision="mixed",
                             inner_tol=args.inner_tol, inner_maxit=args.inner_maxit,
-                            residual_precision=args.resid)
+                            residual_precision=args.resid, inner_operator=args.inner)
         return s, sol, info
 
     def step_fp64_plain():
@@ -264,7 +264,8 @@ def run_gpu(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 operator + fp64 refinement", "data": "synthetic (seeded RSA)",
+        "dtype": f"fp32 inner GMRES ({args.inner} operator) + {args.resid} refinement residual",
+        "data": "synthetic (seeded RSA)",
         "config": config_dict(w, {"parallelism": f"replicas x{world}", "tol": tol, "restart": restart,
                                   "inner_tol": args.inner_tol}),
         "e2e": e2e,
@@ -346,7 +347,8 @@ def run_e2e(args, w, world):
         C, S, info = gcap.capacitance_tensor(xh, eh, w["box"], guess, w["xi"], args.tol, rc=w["rc"],
                                              Ngrid=w["Ngrid"], P=w["P"], restart=args.restart, maxit=args.maxref,
                                              precision="mixed", inner_tol=args.inner_tol,
-                                             inner_maxit=args.inner_maxit, residual_precision=args.resid)
+                                             inner_maxit=args.inner_maxit, residual_precision=args.resid,
+                                             inner_operator=args.inner)
         return C, S
 
     for _ in range(max(1, args.warmup - 1)):
@@ -419,6 +421,95 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ----------------------------------------------------------------------------- other workloads
+def run_quadrupole(args):
+    """Dipole + quadrupole (8 unknowns per sphere) on the body-centred-tetragonal
+    chain lattice: 20 x 20 x 37 face-centred cells (59,200 sites), 15% vacancies,
+    jitter 0.02 (seed 3), field (1,1,0)/sqrt(2), beta = 0.95; mixed precision vs
+    a tight float64 solve.  Prints one JSON line (not the headline metric)."""
+    import torch
+
+    from mutual_polarization_slab_gb300 import quadrupole as gq
+    from mutual_polarization_slab_gb300.workloads import bct_chain_lattice
+
+    torch.cuda.set_device(0)
+    x, box = bct_chain_lattice(20, 20, 37, vacancy=0.15, jitter=0.02, seed=3)
+    n = x.shape[0]
+    beta = 0.95
+    eps = np.full(n, (1 + 2 * beta) / (1 - beta))
+    phi = 4 * math.pi * n / (3 * float(np.prod(box)))
+    tol_sp = 1e-4
+    rc = (60.0 / phi) ** (1.0 / 3.0)
+    xi = math.sqrt(-math.log(tol_sp)) / rc
+    tables, rv = gq.default_table(xi)
+    H0 = np.array([1.0, 1.0, 0.0]) / math.sqrt(2.0)
+    b = torch.zeros((n, 8), dtype=torch.float64, device="cuda")
+    b[:, :3] = torch.as_tensor(H0, device="cuda")
+
+    def step(precision, tol):
+        s = gq.QuadrupoleSystem(x, eps, box, xi, tol_sp, tables, rv, max_rhs=1)
+        sol, info = s.solve(b, None, tol=tol, restart=30, maxit=args.maxref if precision == "mixed" else 200,
+                            precision=precision, inner_tol=args.inner_tol, inner_maxit=args.inner_maxit)
+        s.close()
+        return sol, info
+
+    def timed(precision, tol, steps, warmup):
+        for _ in range(warmup):
+            step(precision, tol)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            sol, info = step(precision, tol)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, sol, info
+
+    ms_m, sol_m, info_m = timed("mixed", args.tol, args.steps, args.warmup)
+    ms_64, sol_64, info_64 = timed("fp64", args.tol, 1, 1)
+    ref, _ = step("fp64", 1e-11)
+    rel = lambda a: float(torch.linalg.vector_norm(a - ref) / torch.linalg.vector_norm(ref))
+    S_ref = ref[:, :3].mean(dim=0)
+    print(json.dumps({
+        "workload": f"dipole+quadrupole, BCT chain lattice 20x20x37 cells, N={n}, jitter 0.02, 15% vacancies, "
+                    f"beta={beta}, field (1,1,0)/sqrt2, xi={xi:.4f}, rc={rc:.3f}, spectral tol {tol_sp}",
+        "metric": "particle-solves/s", "value": n / (ms_m / 1e3), "ms_per_step": ms_m,
+        "fp64_plain": {"value": n / (ms_64 / 1e3), "ms_per_step": ms_64, "matvecs": info_64[0].matvecs_fp64},
+        "speedup_vs_fp64_plain": ms_64 / ms_m,
+        "rel_moment_error_vs_fp64": rel(sol_m), "fp64_plain_rel_error": rel(sol_64),
+        "mean_dipole_rel_error": float(torch.linalg.vector_norm(sol_m[:, :3].mean(dim=0) - S_ref)
+                                       / torch.linalg.vector_norm(S_ref)),
+        "mixed_matvecs": {"fp64": info_m[0].matvecs_fp64, "fp32": info_m[0].matvecs_fp32},
+        "tol": args.tol, "grid": [int(v) for v in np.ceil(1 + np.asarray(box) * 2 * xi * math.sqrt(-math.log(tol_sp))
+                                                            / math.pi)]}), flush=True)
+
+
+def run_batch(args):
+    """Many configurations (polydisperse radii 0.7-1.3, per-particle beta in
+    {0.3, 0.9}, volume fraction 0.1-0.35, N log-uniform 500-20000, seed 4), each
+    with 16 contrast scalings: 48 right-hand sides per configuration in one
+    batched mixed-precision solve.  particle-solves/s = sum N x 3 x 16 / time."""
+    import torch
+
+    from mutual_polarization_slab_gb300 import batch
+
+    torch.cuda.set_device(0)
+    cfgs = batch.make_configurations(count=args.configs, seed=4)
+    scal = np.linspace(0.1, 1.0, 16)
+    batch.solve_configuration(cfgs[0], scal, tol=args.batch_tol)       # warm-up: plans, tables, tuner
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = batch.solve_configurations(cfgs, scal, tol=args.batch_tol, precision="mixed")
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    units = sum(c.n for c in cfgs) * 3 * len(scal)
+    print(json.dumps({
+        "workload": f"{len(cfgs)} polydisperse configurations (N {min(c.n for c in cfgs)}..{max(c.n for c in cfgs)}, "
+                    f"sum {sum(c.n for c in cfgs)}), 3 fields x 16 contrast scalings each, tol {args.batch_tol}",
+        "metric": "particle-solves/s", "value": units / dt, "seconds": dt,
+        "converged": sum(1 for v in res.values() if v[1]), "configs": len(cfgs)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -432,13 +523,25 @@ def main():
     ap.add_argument("--maxref", type=int, default=8)
     ap.add_argument("--resid", default="df", choices=["df", "fp64"],
                     help="operator of the refinement residual: double-float FFTs (df) or cuFFT float64")
+    ap.add_argument("--inner", default="grad", choices=["reference", "grad"],
+                    help="inner float32 operator: the reference discretisation or its gradient form")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=3)
     ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=2000)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--only-mixed", dest="only_mixed", action="store_true",
                     help="time only the mixed solve (profiling runs); prints a short JSON line")
+    ap.add_argument("--workload", default="tensor", choices=["tensor", "quadrupole", "batch"],
+                    help="tensor: the headline N=1e5 capacitance tensor; quadrupole / batch: other configurations")
+    ap.add_argument("--configs", type=int, default=16, help="batch workload: number of configurations")
+    ap.add_argument("--batch-tol", dest="batch_tol", type=float, default=1e-4)
     args = ap.parse_args()
+    if args.workload == "quadrupole" and args.impl != "reference":
+        run_quadrupole(args)
+        return
+    if args.workload == "batch" and args.impl != "reference":
+        run_batch(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

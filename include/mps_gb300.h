@@ -49,6 +49,13 @@ enum mps_status {
 enum mps_precision {
     MPS_FP64 = 0,             /* every stage in float64                              */
     MPS_FP32 = 1,             /* float32 matvec (grids, FFT, pair sum), float64 I/O  */
+    MPS_FP32_GRAD = 3,        /* float32 matvec in gradient form: the moments spread */
+                              /* as one scalar grid sum m.grad w per vector, scaled  */
+                              /* by H/|k|^2, contracted with grad w (one FFT pair per */
+                              /* vector instead of three; differs from the reference */
+                              /* operator by the derivative's sampling error, about  */
+                              /* 1e-5 relative; dipole operator with tiled kernels,  */
+                              /* else MPS_FP32)                                       */
     MPS_DF = 2                /* float64 matvec whose FFTs and Green's scale run in  */
                               /* double-float arithmetic (float hi + float lo,       */
                               /* ~48-bit significand; dipole operator, grid axes of  */
@@ -233,6 +240,8 @@ typedef struct mps_solve_opts {
     int32_t verify;           /* mixed: != 0 ends with a float64 true residual        */
     int32_t residual_precision; /* mixed: operator of the refinement residuals,       */
                               /* MPS_FP64 (0, default) or MPS_DF                      */
+    int32_t inner_operator;   /* mixed: operator of the inner GMRES: 0 = float32 of  */
+                              /* the reference discretisation, 1 = MPS_FP32_GRAD     */
 } mps_solve_opts;
 
 typedef struct mps_solve_info {

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libmps_gb300.so")
 RSA_LIB = os.path.join(HERE, "librsa_host.so")
 BUILD = os.path.join(HERE, "_build")
 
-SOURCES = ["common.cu", "cells.cu", "realspace.cu", "grid.cu", "system.cu", "tiles.cu", "quad.cu", "quadtables.cu", "sizes.cu", "dffft.cu", "adjoint.cu", "forces.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "cells.cu", "realspace.cu", "grid.cu", "system.cu", "tiles.cu", "quad.cu", "quadtables.cu", "sizes.cu", "dffft.cu", "adjoint.cu", "gradop.cu", "forces.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include")]

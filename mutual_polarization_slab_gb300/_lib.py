@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libmps_gb300.so")
 MPS_OK, MPS_BAD_ARG, MPS_RC_GT_HALF_BOX, MPS_TABLE_RANGE, MPS_NOT_CONVERGED, MPS_CUDA_ERR, MPS_CUFFT_ERR, \
     MPS_NO_MEMORY, MPS_SCRATCH_LIMIT = range(9)
 NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
-MPS_FP64, MPS_FP32, MPS_DF = 0, 1, 2
+MPS_FP64, MPS_FP32, MPS_DF, MPS_FP32_GRAD = 0, 1, 2, 3
 MPS_DIPOLE, MPS_DIPOLE_QUADRUPOLE, MPS_POLYDISPERSE = 0, 1, 2
 
 EXPORTS = (
@@ -49,7 +49,8 @@ class SystemDesc(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("tol", f64), ("restart", i32), ("maxit", i32), ("precision", i32), ("inner_tol", f64),
-                ("inner_maxit", i32), ("residual_policy", i32), ("verify", i32), ("residual_precision", i32)]
+                ("inner_maxit", i32), ("residual_policy", i32), ("verify", i32), ("residual_precision", i32),
+                ("inner_operator", i32)]
 
 
 class SolveInfo(C.Structure):

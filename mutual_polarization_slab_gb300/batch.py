@@ -1,0 +1,139 @@
+"""Many configurations, each with a contrast spectrum, solved as batches.
+
+A configuration is one periodic box of spheres (polydisperse radii, a contrast
+beta per particle).  For every configuration the 3 field directions times the
+K contrast scalings s_k (beta_i -> s_k beta_i) are 3K right-hand sides of ONE
+system: the scalings only change the diagonal, so they are permittivity sets
+of one geometry, and all 3K solves share every batched matvec
+(``capacitance_tensor_spectrum`` of the polydisperse operator, CS/).
+
+Across configurations the work is independent, so ranks take a static share
+(largest configurations first, each to the least loaded rank) and the results
+are gathered at the end -- no exchange during the solves.  With
+``torch.distributed`` initialised (NCCL on GPUs, gloo in the CPU tests) the
+gather is ``all_gather_object``; without it one process does everything.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+
+__all__ = ["Configuration", "make_configurations", "partition", "solve_configuration", "solve_configurations"]
+
+
+@dataclass
+class Configuration:
+    x: np.ndarray          # (N, 3) positions
+    radii: np.ndarray      # (N,)
+    beta: np.ndarray       # (N,) contrast of each particle
+    box: np.ndarray        # (3,)
+    index: int = 0
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self):
+        return int(self.x.shape[0])
+
+
+def make_configurations(count=256, seed=4, n_range=(500, 20000), radius_range=(0.7, 1.3), betas=(0.3, 0.9),
+                        phi_range=(0.1, 0.35), rsa=None) -> List[Configuration]:
+    """Seeded synthetic configurations: N log-uniform in n_range, radii uniform,
+    per-particle beta drawn from ``betas`` in equal shares (shuffled), volume
+    fraction uniform in phi_range, random sequential addition without overlap
+    (largest spheres placed first)."""
+    if rsa is None:
+        from .workloads import rsa as rsa_fn
+        rsa = rsa_fn
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+        radii = np.sort(rng.uniform(radius_range[0], radius_range[1], n))[::-1].copy()
+        phi = float(rng.uniform(*phi_range))
+        x, box, _ = rsa(n, phi, seed=int(rng.integers(1 << 31)), radii=radii)
+        perm = rng.permutation(n)
+        beta = np.resize(np.asarray(betas, dtype=np.float64), n)
+        rng.shuffle(beta)
+        out.append(Configuration(x[perm], radii[perm], beta, np.asarray(box, dtype=np.float64), c,
+                                 {"phi": phi}))
+    return out
+
+
+def partition(sizes: Sequence[int], world: int) -> List[List[int]]:
+    """Static longest-processing-time partition of items with the given sizes
+    (cost ~ N) over ``world`` ranks; every rank's list is in ascending index order."""
+    load = [0] * world
+    parts: List[List[int]] = [[] for _ in range(world)]
+    for i in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += int(sizes[i])
+    return [sorted(p) for p in parts]
+
+
+def _eps(beta):
+    return (1.0 + 2.0 * beta) / (1.0 - beta)
+
+
+def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None):
+    """C (K, 3, 3) (row i = mean dipole for the unit field along i) of one
+    configuration for every contrast scaling, all 3K solves in one batch."""
+    import torch
+
+    from .sizes import PolydisperseSystem, spectral_parameters
+
+    s = np.asarray(scalings, dtype=np.float64).reshape(-1)
+    K = s.size
+    box = np.asarray(cfg.box, dtype=np.float64).reshape(3)
+    lt = math.sqrt(-math.log(tol))
+    if xi is None:
+        # real-space cutoff about 60 neighbours' worth, at most just under half the box
+        phi = cfg.meta.get("phi", 4 * math.pi * float(np.sum(cfg.radii ** 3)) / (3 * float(np.prod(box))))
+        rc = min((60.0 / phi) ** (1.0 / 3.0), 0.49 * float(box.min()))
+        xi = lt / rc
+    eps_sets = np.stack([_eps(cfg.beta * sk) for sk in s])           # (K, N)
+    n = cfg.n
+    sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, box, xi, tol, max_rhs=3 * K)
+    try:
+        b = torch.zeros((3 * K, n, 3), dtype=torch.float64, device="cuda")
+        x0 = torch.zeros_like(b)
+        phi_v = 4 * math.pi * float(np.sum(cfg.radii ** 3)) / (3 * float(np.prod(box)))
+        diag_index = []
+        for k in range(K):
+            beta = cfg.beta * s[k]
+            amp = torch.as_tensor(4 * math.pi * cfg.radii ** 3 * beta / (1 - beta * phi_v), device="cuda")
+            for i in range(3):
+                b[3 * k + i, :, i] = 1.0
+                x0[3 * k + i, :, i] = amp
+                diag_index.append(k)
+        sol, info = sysm.solve(b, x0, tol=tol, restart=min(3 * n, 30), maxit=100 if precision != "mixed" else 8,
+                               precision=precision, diag_index=diag_index)
+        C = sol.reshape(K, 3, n, 3).mean(dim=2).cpu().numpy()
+        conv = all(i.converged for i in info)
+    finally:
+        sysm.close()
+    return C, conv
+
+
+def solve_configurations(configs: Sequence[Configuration], scalings, tol=1e-4, precision="mixed",
+                         solver: Optional[Callable] = None, gather=True):
+    """Solve this rank's share of ``configs``; returns {index: (C, converged)} for
+    all configurations when gathered, else for this rank's share."""
+    import torch.distributed as dist
+
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    rank = dist.get_rank() if world > 1 else 0
+    parts = partition([c.n for c in configs], world)
+    solve = solver or (lambda cfg: solve_configuration(cfg, scalings, tol=tol, precision=precision))
+    mine = {configs[i].index: solve(configs[i]) for i in parts[rank]}
+    if world == 1 or not gather:
+        return mine
+    everything: List[Optional[dict]] = [None] * world
+    dist.all_gather_object(everything, mine)
+    merged = {}
+    for part in everything:
+        merged.update(part)
+    return merged

@@ -223,7 +223,7 @@ def run_capacitance(x, box, eps_p, xi, H0, errortol=1e-5, slab_factor=1.0, use_s
 def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None, dipoletable2=None, rtable=None,
                        offset=None, offsetxyz=None, *, slab_factor=0.0, rc=None, Ngrid=None, P=None, restart=None,
                        maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4, batched=True, system=None,
-                       residual_precision="df"):
+                       residual_precision="df", inner_operator="grad"):
     """3x3 capacitance tensor for unit fields along x, y, z (Capacitance_Hetero/Capacitance_Tensor.m:23-59).
 
     ``batched=True`` solves the three directions together (one batched matvec
@@ -252,7 +252,8 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
         amp = g0[:, 0:1]
         x0 = torch.stack([amp * eye[i] for i in range(3)]).contiguous()
         S3, infos = sysm.solve(b, x0, tol=float(errortol), restart=restart, maxit=maxit, precision=precision,
-                               inner_tol=inner_tol, inner_maxit=inner_maxit, residual_precision=residual_precision)
+                               inner_tol=inner_tol, inner_maxit=inner_maxit, residual_precision=residual_precision,
+                               inner_operator=inner_operator)
     else:
         sols = []
         guess = g0
@@ -260,7 +261,7 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
             b = eye[i].repeat(N, 1)
             Si, inf = sysm.solve(b, guess, tol=float(errortol), restart=restart, maxit=maxit, precision=precision,
                                  inner_tol=inner_tol, inner_maxit=inner_maxit,
-                                 residual_precision=residual_precision)
+                                 residual_precision=residual_precision, inner_operator=inner_operator)
             sols.append(Si)
             infos += inf
             guess = Si[:, [2, 0, 1]].contiguous()

@@ -1,0 +1,344 @@
+// Gradient form of the float32 wave-space operator (inner operator of the
+// mixed-precision solve).
+//
+// The reference operator spreads the three moment components onto three grids
+// and scales their spectra by H k k^T / |k|^2.  Since k k^T = (ik)(ik)^*, the same
+// operator (up to the sampling error of the Gaussian's derivative) is
+//   rho(n) = sum_a m_a . grad_r w_a(n)              one scalar grid per vector
+//   phi    = IFFT( H / |k|^2 FFT(rho) )
+//   E_a    = h^3 sum_n grad_r w_a(n) phi(n)
+// with r = node - x_a and grad_r w = -(4 xi^2 / eta_d) r_d w per axis (separable:
+// the per-axis factors w_d and g_d = dw_d/dr_d).  One FFT pair per vector instead
+// of three, a third of the grid traffic.  It differs from the reference operator
+// by the discretisation error of the derivative (about 1e-5 relative at the
+// configurations measured), which the float64-accurate refinement residual
+// removes: the mixed solve still converges to the reference operator's solution.
+//
+// The kernels follow the tiled spread / contract of tiles.cu (one CTA per
+// 16 x 16 x TZ tile, deterministic, no atomics).
+#include "gradop.cuh"
+
+namespace mps {
+
+constexpr int kGChunk = 32;
+
+// g[a][d][j] = dw_d/dr at stencil node j of axis d (float32).
+__global__ void k_grad_factors(const double *__restrict__ x, int64_t n, GridParams gp, const double *__restrict__ w64,
+                               float *__restrict__ g32) {
+    const int P = gp.P;
+    const int lo = (P - 1) / 2;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * 3; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = t / 3;
+        const int d = (int)(t % 3);
+        const double h = gp.h[d];
+        const double xv = x[3 * a + d];
+        const double v = __ddiv_rn(xv, h);
+        const double af = floor(fabs(v) + 0.5);
+        const double node0 = v > 0 ? af : (v < 0 ? -af : 0.0 * af);
+        const double base = __dsub_rn(__dmul_rn(node0, h), xv);
+        const double c = -4.0 * gp.xi * gp.xi / gp.eta[d];
+        for (int j = 0; j < P; ++j) {
+            const double r = base + (double)(j - lo) * h;
+            g32[(a * 3 + d) * P + j] = (float)(c * r * w64[(a * 3 + d) * P + j]);
+        }
+    }
+}
+
+// H / |k|^2 on the half spectrum (float32), H including 1/G; zero at k = 0.
+__global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, float *__restrict__ hs) {
+    const int Nxh = gp.N[0] / 2 + 1;
+    const int64_t Gc = (int64_t)Nxh * gp.N[1] * gp.N[2];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc; t += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(t % Nxh);
+        const int iy = (int)((t / Nxh) % gp.N[1]);
+        const int iz = (int)(t / ((int64_t)Nxh * gp.N[1]));
+        const double kx = fft_freq(ix, gp.N[0]) * gp.kfac[0];
+        const double ky = fft_freq(iy, gp.N[1]) * gp.kfac[1];
+        const double kz = fft_freq(iz, gp.N[2]) * gp.kfac[2];
+        const double k2 = kx * kx + ky * ky + kz * kz;
+        hs[t] = k2 > 0 ? (float)(H[t] / k2) : 0.f;
+    }
+}
+
+template <int TZ, int NR>
+__global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
+                                                           const int32_t *__restrict__ start,
+                                                           const float *__restrict__ w, const float *__restrict__ g,
+                                                           GridParams gp, const int64_t *__restrict__ tstart,
+                                                           const int32_t *__restrict__ entries, int ntx, int nty,
+                                                           float *__restrict__ grid) {
+    __shared__ int3 s_off[kGChunk];
+    __shared__ float s_w[kGChunk][3 * kMaxP];
+    __shared__ float s_g[kGChunk][3 * kMaxP];
+    __shared__ float s_m[kGChunk][3 * NR];
+    const int64_t t = blockIdx.x;
+    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
+    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
+    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    float acc[TZ][NR];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z)
+#pragma unroll
+        for (int r = 0; r < NR; ++r) acc[z][r] = 0.f;
+    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
+    for (int64_t cb = e0; cb < e1; cb += kGChunk) {
+        const int cnt = (int)min((int64_t)kGChunk, e1 - cb);
+        if (threadIdx.x < cnt) {
+            const int32_t a = entries[cb + threadIdx.x];
+            int ox = X0 - start[3 * a], oy = Y0 - start[3 * a + 1], oz = Z0 - start[3 * a + 2];
+            if (ox < 0) ox += Nx;
+            if (oy < 0) oy += Ny;
+            if (oz < 0) oz += Nz;
+            s_off[threadIdx.x] = make_int3(ox, oy, oz);
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const double *ma = m + ((int64_t)(r0 + r) * n + a) * 3;
+                s_m[threadIdx.x][3 * r + 0] = (float)ma[0];
+                s_m[threadIdx.x][3 * r + 1] = (float)ma[1];
+                s_m[threadIdx.x][3 * r + 2] = (float)ma[2];
+            }
+        }
+        for (int q = threadIdx.x; q < cnt * 3 * P; q += blockDim.x) {
+            const int pp = q / (3 * P), k = q % (3 * P);
+            const int32_t a = entries[cb + pp];
+            s_w[pp][(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+            s_g[pp][(k / P) * kMaxP + (k % P)] = g[(int64_t)a * 3 * P + k];
+        }
+        __syncthreads();
+        for (int pp = 0; pp < cnt; ++pp) {
+            const int3 o = s_off[pp];
+            int dx = o.x + tx;
+            if (dx >= Nx) dx -= Nx;
+            int dy = o.y + ty;
+            if (dy >= Ny) dy -= Ny;
+            if (dx < P && dy < P) {
+                const float wx = s_w[pp][dx], wy = s_w[pp][kMaxP + dy];
+                const float gx = s_g[pp][dx], gy = s_g[pp][kMaxP + dy];
+                const float wxy = wx * wy;
+                float cA[NR], cB[NR];
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    // column parts: (m_x gx wy + m_y wx gy) multiplies w_z, m_z wx wy multiplies g_z
+                    cA[r] = s_m[pp][3 * r] * gx * wy + s_m[pp][3 * r + 1] * wx * gy;
+                    cB[r] = s_m[pp][3 * r + 2] * wxy;
+                }
+#pragma unroll
+                for (int z = 0; z < TZ; ++z) {
+                    int dz = o.z + z;
+                    if (dz >= Nz) dz -= Nz;
+                    if (dz < P) {
+                        const float wz = s_w[pp][2 * kMaxP + dz], gz = s_g[pp][2 * kMaxP + dz];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) acc[z][r] += cA[r] * wz + cB[r] * gz;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    const int gxn = X0 + tx, gyn = Y0 + ty;
+    if (gxn < Nx && gyn < Ny) {
+        const int64_t G = gp.G;
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            const int gz = Z0 + z;
+            if (gz < Nz) {
+                const int64_t node = ((int64_t)gz * Ny + gyn) * Nx + gxn;
+#pragma unroll
+                for (int r = 0; r < NR; ++r) grid[(int64_t)(r0 + r) * G + node] = acc[z][r];
+            }
+        }
+    }
+}
+
+constexpr int kGRowPad = kTileX + 1;
+
+template <int TZ, int NR>
+__global__ void __launch_bounds__(256) k_contract_grad_tiled(const float *__restrict__ grid, int r0,
+                                                             const int32_t *__restrict__ start,
+                                                             const float *__restrict__ w, const float *__restrict__ g,
+                                                             GridParams gp, const int64_t *__restrict__ tstart,
+                                                             const int32_t *__restrict__ entries, int ntx, int nty,
+                                                             float *__restrict__ partial) {
+    constexpr int kPlane = kTileY * kGRowPad;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *tile = (float *)smem_raw;                        // [NR][TZ][16][17]
+    float *wbuf = tile + NR * TZ * kPlane;                  // [8 warps][2][3*kMaxP]
+    const int64_t t = blockIdx.x;
+    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
+    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
+    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int64_t G = gp.G;
+    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
+    if (e0 == e1) return;
+    {
+        const int gxn = X0 + tx, gyn = Y0 + ty;
+        const bool in = gxn < Nx && gyn < Ny;
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            const int gz = Z0 + z;
+            const int64_t node = ((int64_t)gz * Ny + gyn) * Nx + gxn;
+#pragma unroll
+            for (int r = 0; r < NR; ++r)
+                tile[(r * TZ + z) * kPlane + ty * kGRowPad + tx] =
+                    (in && gz < Nz) ? grid[(int64_t)(r0 + r) * G + node] : 0.f;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float *wb = wbuf + wid * 2 * 3 * kMaxP;
+    float *gb = wb + 3 * kMaxP;
+    for (int64_t e = e0 + wid; e < e1; e += 8) {
+        const int32_t a = entries[e];
+        int ox = X0 - start[3 * a], oy = Y0 - start[3 * a + 1], oz = Z0 - start[3 * a + 2];
+        if (ox < 0) ox += Nx;
+        if (oy < 0) oy += Ny;
+        if (oz < 0) oz += Nz;
+        for (int k = lane; k < 3 * P; k += 32) {
+            wb[(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
+            gb[(k / P) * kMaxP + (k % P)] = g[(int64_t)a * 3 * P + k];
+        }
+        int xr = lane - ox, yr = lane - oy, zr = lane - oz;
+        if (xr < 0) xr += Nx;
+        if (yr < 0) yr += Ny;
+        if (zr < 0) zr += Nz;
+        const unsigned mx = __ballot_sync(0xffffffffu, lane < P && xr < kTileX && X0 + xr < Nx);
+        const unsigned my = __ballot_sync(0xffffffffu, lane < P && yr < kTileY && Y0 + yr < Ny);
+        const unsigned mz = __ballot_sync(0xffffffffu, lane < P && zr < TZ && Z0 + zr < Nz);
+        __syncwarp();
+        const int nx = __popc(mx), ny = __popc(my);
+        float acc[3 * NR];
+#pragma unroll
+        for (int c = 0; c < 3 * NR; ++c) acc[c] = 0.f;
+        for (int q = lane; q < nx * ny; q += 32) {
+            const int jx = (int)__fns(mx, 0, q % nx + 1), jy = (int)__fns(my, 0, q / nx + 1);
+            int xx = jx - ox, yy = jy - oy;
+            if (xx < 0) xx += Nx;
+            if (yy < 0) yy += Ny;
+            float s0[NR], s1[NR];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) s0[r] = s1[r] = 0.f;
+            unsigned mzz = mz;
+            while (mzz) {
+                const int jz = __ffs(mzz) - 1;
+                mzz &= mzz - 1;
+                int zz = jz - oz;
+                if (zz < 0) zz += Nz;
+                const float wz = wb[2 * kMaxP + jz], gz = gb[2 * kMaxP + jz];
+                const float *tp = tile + zz * kPlane + yy * kGRowPad + xx;
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    const float v = tp[r * TZ * kPlane];
+                    s0[r] += v * wz;
+                    s1[r] += v * gz;
+                }
+            }
+            const float wx = wb[jx], wy = wb[kMaxP + jy], gx = gb[jx], gy = gb[kMaxP + jy];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                acc[3 * r + 0] += gx * wy * s0[r];
+                acc[3 * r + 1] += wx * gy * s0[r];
+                acc[3 * r + 2] += wx * wy * s1[r];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3 * NR; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 3 * NR; ++c) partial[e * 3 * NR + c] = acc[c];
+        }
+        __syncwarp();
+    }
+}
+
+// Each particle's partials summed in its fixed tile order (float64 accumulation).
+template <int NR>
+__global__ void k_contract_grad_gather(const float *__restrict__ partial, int64_t n, int r0,
+                                       const int64_t *__restrict__ pstart, const int32_t *__restrict__ pentry,
+                                       double hprod, double *__restrict__ out) {
+    constexpr int C = 3 * NR;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        double acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = 0.0;
+        for (int64_t k = pstart[a]; k < pstart[a + 1]; ++k) {
+            const float *pp = partial + (int64_t)pentry[k] * C;
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[c] += (double)pp[c];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) out[((int64_t)(r0 + r) * n + a) * 3 + c] = acc[3 * r + c] * hprod;
+    }
+}
+
+int grad_factors(const double *x, int64_t n, const GridParams &gp, const double *w64, float *g32, cudaStream_t s) {
+    k_grad_factors<<<grid_for(3 * n, 256), 256, 0, s>>>(x, n, gp, w64, g32);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int grad_scale_coef(const GridParams &gp, const double *H, float *hs, cudaStream_t s) {
+    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
+    k_grad_scale_coef<<<grid_for(Gc, 256), 256, 0, s>>>(gp, H, hs);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+template <int TZ, int NR>
+static int grad_launch(const double *m, int64_t n, int r0, const int32_t *start, const float *w, const float *g,
+                       const GridParams &gp, const TileBins &tb, float *grid, float *partial, double *out,
+                       bool spread_phase, cudaStream_t s) {
+    if (spread_phase) {
+        k_spread_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start,
+                                                                         tb.entries, tb.ntx, tb.nty, grid);
+        MPS_LAUNCH_CHECK();
+        return MPS_OK;
+    }
+    const size_t smem = sizeof(float) * ((size_t)NR * TZ * kTileY * kGRowPad + 8 * 2 * 3 * kMaxP);
+    if (smem > 48 * 1024)
+        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_grad_tiled<TZ, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+    k_contract_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, smem, s>>>(grid, r0, start, w, g, gp, tb.tile_start,
+                                                                          tb.entries, tb.ntx, tb.nty, partial);
+    MPS_LAUNCH_CHECK();
+    k_contract_grad_gather<NR><<<grid_for(n, 256), 256, 0, s>>>(partial, n, r0, tb.pstart, tb.pentry, gp.hprod, out);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+template <int TZ>
+static int grad_dispatch(const double *m, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                         const GridParams &gp, const TileBins &tb, float *grid, float *partial, double *out,
+                         bool spread_phase, cudaStream_t s) {
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        int rc = nr == 3   ? grad_launch<TZ, 3>(m, n, r0, start, w, g, gp, tb, grid, partial, out, spread_phase, s)
+                 : nr == 2 ? grad_launch<TZ, 2>(m, n, r0, start, w, g, gp, tb, grid, partial, out, spread_phase, s)
+                           : grad_launch<TZ, 1>(m, n, r0, start, w, g, gp, tb, grid, partial, out, spread_phase, s);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+int spread_grad_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                      const GridParams &gp, const TileBins &tb, float *grid, cudaStream_t s) {
+    if (tb.tz == 8) return grad_dispatch<8>(m, n, nrhs, start, w, g, gp, tb, grid, nullptr, nullptr, true, s);
+    if (tb.tz == 4) return grad_dispatch<4>(m, n, nrhs, start, w, g, gp, tb, grid, nullptr, nullptr, true, s);
+    return MPS_BAD_ARG;
+}
+
+int contract_grad_tiled(const float *grid, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                        const GridParams &gp, const TileBins &tb, float *partial, double *out, cudaStream_t s) {
+    float *gr = const_cast<float *>(grid);
+    if (tb.tz == 8) return grad_dispatch<8>(nullptr, n, nrhs, start, w, g, gp, tb, gr, partial, out, false, s);
+    if (tb.tz == 4) return grad_dispatch<4>(nullptr, n, nrhs, start, w, g, gp, tb, gr, partial, out, false, s);
+    return MPS_BAD_ARG;
+}
+
+}  // namespace mps

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include "dffft.cuh"
 #include "adjoint.cuh"
+#include "gradop.cuh"
 
 using namespace mps;
 
@@ -53,9 +54,13 @@ struct GreenKey {
 struct GreenCoef {
     double *h64 = nullptr;
     float *h32 = nullptr;
+    float *hs32 = nullptr;   // H / |k|^2 of the gradient-form float32 operator (built on first use)
+    float2 *tm6 = nullptr;   // double-float scale tensor H q q^T, 6 x Gc (built on first use)
     ~GreenCoef() {
         if (h64) cudaFree(h64);
         if (h32) cudaFree(h32);
+        if (hs32) cudaFree(hs32);
+        if (tm6) cudaFree(tm6);
     }
 };
 static std::map<GreenKey, std::shared_ptr<GreenCoef>> g_green;
@@ -131,7 +136,8 @@ struct mps_system {
     DfPlan3 dfp;                 // double-float FFT plans of the grid
     int df_state = 0;            // 0 not built yet, 1 usable, -1 unsupported grid
     int resid_prec = MPS_FP64;   // operator of the refinement residuals
-    float2 *df_tm6 = nullptr;    // double-float scale tensor, 6 x Gc
+    float *g32 = nullptr;        // gradient factors dw_d/dr of the gradient-form operator, n x 3 x P
+    int inner_prec = MPS_FP32;   // operator of the mixed solve's inner GMRES
 };
 
 static void free_system(mps_system *s) {
@@ -144,7 +150,7 @@ static void free_system(mps_system *s) {
                     s->p32.A, s->p32.BA, s->p32.rx, s->p32.ry, s->p32.rz, s->start, s->w64, s->w32,
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
-                    s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->df_tm6};
+                    s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->g32};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -510,9 +516,14 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     MPS_TRY(ensure_grids(s, MPS_FP64, st));
     if (use_tiles && !s->partial64)
         MPS_TRY(dalloc(&s->partial64, (size_t)s->tb64.nentries * 9 * sizeof(double), st));
-    if (!s->df_tm6) {
-        MPS_TRY(dalloc(&s->df_tm6, sizeof(float2) * 6 * s->Gc, st));
-        MPS_TRY(df_scale_table(s->gp, s->h64, s->df_tm6, st));
+    {
+        std::lock_guard<std::mutex> lk(g_green_mu);
+        if (!s->green->tm6) {
+            float2 *tm = nullptr;
+            MPS_TRY(dalloc_persistent(&tm, sizeof(float2) * 6 * s->Gc));
+            MPS_TRY(df_scale_table(s->gp, s->green->h64, tm, st));
+            s->green->tm6 = tm;
+        }
     }
     double *grid = s->grid64;
     float4 *spec = (float4 *)s->spec64;     // float4 per complex value: the size of a double2
@@ -528,7 +539,7 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(2);
     MPS_TRY(df_forward_xy(grid, spec, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(3);
-    MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, s->df_tm6, st));
+    MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, s->green->tm6, st));
     STAGE_MARK(4);
     MPS_TRY(df_inverse_yx(spec, grid, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(5);
@@ -615,7 +626,48 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
     return MPS_OK;
 }
 
+// Gradient form of the float32 operator (gradop.cu): one scalar grid per vector.
+static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    bool use_tiles = false;
+    MPS_TRY(ensure_tiles(s, false, st, &use_tiles));
+    if (!use_tiles || s->kind != MPS_DIPOLE) return matvec_impl<float>(s, m, out, nrhs, st);
+    MPS_TRY(ensure_grids(s, MPS_FP32, st));
+    if (!s->g32) {
+        MPS_TRY(dalloc(&s->g32, sizeof(float) * 3 * s->n * s->gp.P, st));
+        MPS_TRY(grad_factors(s->x, s->n, s->gp, s->w64, s->g32, st));
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_green_mu);
+        if (!s->green->hs32) {
+            float *hs = nullptr;
+            MPS_TRY(dalloc_persistent(&hs, sizeof(float) * s->Gc));
+            MPS_TRY(grad_scale_coef(s->gp, s->green->h64, hs, st));
+            s->green->hs32 = hs;
+        }
+    }
+    const double vol = s->box[0] * s->box[1] * s->box[2];
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
+    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    STAGE_MARK(1);
+    MPS_TRY(spread_grad_tiled(m, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->grid32, st));
+    STAGE_MARK(2);
+    MPS_TRY(exec_plan(s, CUFFT_R2C, nrhs, s->grid32, s->spec32, 0, st));
+    STAGE_MARK(3);
+    MPS_TRY(scale_cs<float>(s->spec32, nrhs, s->gp, s->green->hs32, st));
+    STAGE_MARK(4);
+    MPS_TRY(exec_plan(s, CUFFT_C2R, nrhs, s->spec32, s->grid32, 0, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->partial32, out,
+                                st));
+    STAGE_MARK(6);
+    MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
 static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+    if (precision == MPS_FP32_GRAD) return matvec_grad(s, m, out, nrhs, st);
     if (precision == MPS_DF) {
         if (df_usable(s)) return matvec_df(s, m, out, nrhs, st);
         precision = MPS_FP64;
@@ -1184,7 +1236,7 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         f0.final_check = false;
         f0.ls_restart = true;
         int icyc = 0;
-        e = gmres_core(s, b, x, nrhs, inner_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc, mv32,
+        e = gmres_core(s, b, x, nrhs, inner_tol, o->restart, inner_maxit, s->inner_prec, ic.data(), ir.data(), &icyc, mv32,
                        st, f0);
     }
     if (e == MPS_OK || e == MPS_NOT_CONVERGED) {
@@ -1223,7 +1275,7 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         double step_tol = inner_tol;
         if (worst > 0.0) step_tol = std::max(inner_tol, std::min(0.5, 0.3 * o->tol / worst));
         int icyc = 0;
-        int g = gmres_core(s, r, dx, nrhs, step_tol, o->restart, inner_maxit, MPS_FP32, ic.data(), ir.data(), &icyc,
+        int g = gmres_core(s, r, dx, nrhs, step_tol, o->restart, inner_maxit, s->inner_prec, ic.data(), ir.data(), &icyc,
                            mv32, st, fl);
         if (g != MPS_OK && g != MPS_NOT_CONVERGED) {
             e = g;
@@ -1501,7 +1553,8 @@ extern "C" int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t 
 extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t nrhs, const int32_t *diag_index,
                           int32_t precision, mps_stream_t stream) {
     if (!sys || !m || !out || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
-    if (precision != MPS_FP64 && precision != MPS_FP32 && precision != MPS_DF) return MPS_BAD_ARG;
+    if (precision != MPS_FP64 && precision != MPS_FP32 && precision != MPS_DF && precision != MPS_FP32_GRAD)
+        return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     return matvec_any(sys, m, out, nrhs, precision, st);
@@ -1536,6 +1589,7 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
     if (opts->restart < 1 || opts->restart >= kMaxCols || opts->maxit < 1 || !(opts->tol > 0)) return MPS_BAD_ARG;
     if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32 && opts->precision != MPS_DF) return MPS_BAD_ARG;
     if (opts->residual_precision != MPS_FP64 && opts->residual_precision != MPS_DF) return MPS_BAD_ARG;
+    if (opts->inner_operator != 0 && opts->inner_operator != 1) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     const int64_t n3 = (int64_t)sys->ndof * sys->n;
@@ -1550,6 +1604,7 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
     int cycles = 0, mv64 = 0, mv32 = 0;
     int rc;
     sys->resid_prec = opts->residual_precision;
+    sys->inner_prec = opts->inner_operator == 1 ? MPS_FP32_GRAD : MPS_FP32;
     if (opts->precision == MPS_FP64 || opts->precision == MPS_DF) {
         rc = gmres_core(sys, b, x, nrhs, opts->tol, opts->restart, opts->maxit, opts->precision, conv.data(),
                         relres.data(), &cycles, &mv64, st);

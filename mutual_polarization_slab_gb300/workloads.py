@@ -56,12 +56,16 @@ def rsa(n: int, phi: float, seed: int, radii=None, max_tries: int = 10_000_000):
 def bct_chain_lattice(ncx: int, ncy: int, ncz: int, vacancy: float, jitter: float, seed: int):
     """Body-centred-tetragonal chain lattice of touching unit spheres (c = 2,
     a = sqrt(6)), written in its face-centred setting: a sqrt(12) x sqrt(12) x 2
-    cell with a 4-site basis, seeded Gaussian jitter and random vacancies."""
+    cell with the 4-site basis (0,0,0), (0,1/2,1/2), (1/2,0,1/2), (1/2,1/2,0) in
+    cell units, sites listed basis-major then by cell (x outer, z inner) as
+    ``CPU - Ewald test/test_driver_BCT110.py:74-95`` does, then seeded random
+    vacancies and Gaussian jitter.  Returns (positions wrapped into the box, box)."""
     rng = np.random.default_rng(seed)
     a = math.sqrt(12.0)
-    basis = np.array([[0.0, 0.0, 0.0], [a / 2, a / 2, 0.0], [a / 2, 0.0, 1.0], [0.0, a / 2, 1.0]])
+    cell = np.array([a, a, 2.0])
+    basis = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
     cells = np.stack(np.meshgrid(np.arange(ncx), np.arange(ncy), np.arange(ncz), indexing="ij"), -1).reshape(-1, 3)
-    x = (cells[:, None, :] * np.array([a, a, 2.0]) + basis[None]).reshape(-1, 3)
+    x = ((cells[None, :, :] + basis[:, None, :]) * cell).reshape(-1, 3)
     keep = rng.random(x.shape[0]) >= vacancy
     x = x[keep] + rng.normal(0.0, jitter, size=(int(keep.sum()), 3))
     box = np.array([ncx * a, ncy * a, ncz * 2.0])
