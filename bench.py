@@ -242,7 +242,7 @@ def run_gpu(args):
     st = s_prof.stage_times()
     tuning = s_prof.tuning()
     s_prof.close()
-    roof = roofline(w, st)
+    roof = roofline(w, st, args.inner)
 
     # --- plain float64 GMRES drop-in (reference solver structure) + accuracy of the mixed result
     ms_fp64, _, (sol_64, info_64), _ = timed(step_fp64_plain, max(1, min(args.steps, 2)), 1)
@@ -290,8 +290,12 @@ def run_gpu(args):
         print(json.dumps(out), flush=True)
 
 
-def roofline(w, st):
-    """Dominant kernel (largest stage time of this library's kernels in the fp32 matvec) vs HBM peak."""
+def roofline(w, st, inner="grad"):
+    """Dominant kernel (largest stage time of this library's kernels in the fp32 matvec) vs HBM peak.
+    Algorithmic bytes per launch, R = 3 vectors, s = 4 bytes: the grids written or read once
+    (3R grids for the reference discretisation, R for the gradient form), plus per particle its
+    moments / fields (24 R), stencil start (12) and separable factors (3P s; twice for the gradient
+    form, which also reads dw/dr)."""
     n, P = w["n"], w["P"]
     G = int(np.prod(w["Ngrid"]))
     nx = int(w["Ngrid"][0])
@@ -304,12 +308,12 @@ def roofline(w, st):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     cnt, ms = st["fp32"]
     R = 3
-    # algorithmic bytes per launch (one batched fp32 matvec, R = 3 vectors, s = 4 bytes)
-    per_particle_geom = 3 * P * 4 + 12
+    grids = R if inner == "grad" else 3 * R
+    per_particle_geom = (2 if inner == "grad" else 1) * 3 * P * 4 + 12
     algo = {
-        "spread": 3 * R * G * 4 + n * (R * 3 * 8 + per_particle_geom),
-        "contract": 3 * R * G * 4 + n * (per_particle_geom + R * 3 * 8),
-        "scale": 2 * 3 * R * Gc * 8 + Gc * 4,
+        "spread": grids * G * 4 + n * (R * 3 * 8 + per_particle_geom),
+        "contract": grids * G * 4 + n * (per_particle_geom + R * 3 * 8),
+        "scale": 2 * grids * Gc * 8 + Gc * 4,
         "real_space": None,
     }
     cand = {k: v for k, v in ms.items() if k in ("spread", "contract", "scale", "real_space")}
@@ -321,7 +325,10 @@ def roofline(w, st):
         top = max((k for k in cand if algo.get(k)), key=cand.get)
         avg_ms = cand[top] / cnt
     achieved = algo[top] / (avg_ms / 1e3) / 1e9
-    return {"bound": "hbm", "kernel": f"k_{top} (fp32, 3 vectors)", "achieved": achieved, "peak": peak,
+    kname = {"spread": "k_spread_grad_tiled" if inner == "grad" else "k_spread_tiled",
+             "contract": "k_contract_grad_tiled + gather" if inner == "grad" else "k_contract_tiled + gather",
+             "scale": "k_scale_cs" if inner == "grad" else "k_scale_half"}.get(top, top)
+    return {"bound": "hbm", "kernel": f"{kname} (fp32, 3 vectors)", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
             "algorithmic_bytes_per_launch": algo[top], "avg_launch_ms": avg_ms, "launches": cnt,
             "traffic": None,

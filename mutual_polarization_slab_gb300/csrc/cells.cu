@@ -454,6 +454,190 @@ __global__ void __launch_bounds__(256) k_csr_fill(const double *__restrict__ x, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float pair list
+// ---------------------------------------------------------------------------
+__global__ void k_positions_df(const double *__restrict__ x, int64_t m, float2 *__restrict__ xdf) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const dfv v(x[i]);
+        xdf[i] = make_float2(v.hi, v.lo);
+    }
+}
+
+__global__ void k_df_tab(const double *__restrict__ perp, const double *__restrict__ para,
+                         const double *__restrict__ rv, int64_t ntab, float *__restrict__ rvf,
+                         float4 *__restrict__ seg_r, float4 *__restrict__ seg_perp, float4 *__restrict__ seg_para) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ntab; i += (int64_t)gridDim.x * blockDim.x) {
+        rvf[i] = (float)rv[i];
+        if (i == 0) {
+            seg_r[0] = seg_perp[0] = seg_para[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        const dfv rl(rv[i - 1]), inv(1.0 / (rv[i] - rv[i - 1]));
+        const dfv p0(perp[i - 1]), dp(perp[i] - perp[i - 1]), q0(para[i - 1]), dq(para[i] - para[i - 1]);
+        seg_r[i] = make_float4(rl.hi, rl.lo, inv.hi, inv.lo);
+        seg_perp[i] = make_float4(p0.hi, p0.lo, dp.hi, dp.lo);
+        seg_para[i] = make_float4(q0.hi, q0.lo, dq.hi, dq.lo);
+    }
+}
+
+__device__ __forceinline__ dfv df_lo(float4 v) { return dfv(v.x, v.y); }
+__device__ __forceinline__ dfv df_hi(float4 v) { return dfv(v.z, v.w); }
+
+// 1/sqrt(s) in double-float by Newton's method y <- y (3 - s y^2) / 2 from the
+// float32 reciprocal square root (two steps).
+__device__ __forceinline__ dfv df_rsqrt(dfv s) {
+    dfv y(rsqrtf(s.hi), 0.f);
+    const dfv three_half(1.5f, 0.f);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        dfv h = s * y * y;
+        h.hi = __fmul_rn(h.hi, 0.5f);
+        h.lo = __fmul_rn(h.lo, 0.5f);
+        y = y * (three_half - h);
+    }
+    return y;
+}
+
+// First table index with rvf[i] >= d from the uniform-spacing guess (float).
+__device__ __forceinline__ int64_t df_search(const float *__restrict__ rvf, int64_t n, float d, float inv_dr) {
+    int64_t g = (int64_t)(d * inv_dr);
+    g = g < 0 ? 0 : (g > n - 1 ? n - 1 : g);
+    for (int it = 0; it < 8; ++it) {
+        if (g < n && rvf[g] < d) {
+            ++g;
+            continue;
+        }
+        if (g > 0 && rvf[g - 1] >= d) {
+            --g;
+            continue;
+        }
+        return g;
+    }
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (rvf[mid] < d)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void store_pair_df(PairData<dfv> &pd, PairData<float> &pf, int64_t w, int32_t b, dfv A,
+                                              dfv B, const dfv rh[3], dfv d) {
+    const dfv BA = B - A;
+    pd.nbr[w] = b;
+    pd.A[w] = A;
+    pd.BA[w] = BA;
+    pd.rx[w] = rh[0];
+    pd.ry[w] = rh[1];
+    pd.rz[w] = rh[2];
+    pd.dist[w] = d;
+    pf.A[w] = A.hi;
+    pf.BA[w] = BA.hi;
+    pf.rx[w] = rh[0].hi;
+    pf.ry[w] = rh[1].hi;
+    pf.rz[w] = rh[2].hi;
+}
+
+// Same traversal and pair order as k_csr_fill.
+__global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ x, const float *__restrict__ xf,
+                                                     const float2 *__restrict__ xdf, PairScreen ps,
+                                                     const int32_t *__restrict__ sorted,
+                                                     const int32_t *__restrict__ lin,
+                                                     const int32_t *__restrict__ counts,
+                                                     const int64_t *__restrict__ starts, int64_t n, int64_t ncx,
+                                                     int64_t ncy, int64_t ncz, const int64_t *__restrict__ off27,
+                                                     DfTab tab, PairData<dfv> pdf, PairData<float> p32,
+                                                     int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    dfv L[3], halfL[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        L[k] = dfv(ps.L[k]);
+        halfL[k] = dfv(0.5 * ps.L[k]);
+    }
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
+        const int64_t s = t / 27;
+        const int o = (int)(t % 27);
+        const int32_t a = sorted[s];
+        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
+        const int64_t b0 = starts[nb], len = counts[nb];
+        int64_t w = off27[(int64_t)a * 27 + o];
+        for (int64_t j0 = 0; j0 < len; j0 += 32) {
+            const int64_t j = j0 + lane;
+            bool keep = false, exact = false;
+            int32_t b = -1;
+            dfv r[3];
+            double r64[3] = {0, 0, 0};
+            if (j < len) {
+                b = sorted[b0 + j];
+                const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
+                if (sc != SCREEN_OUT) {
+                    bool big = false;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const float2 pa = xdf[3 * a + k], pb = xdf[3 * b + k];
+                        dfv v = dfv_two_diff(pa.x, pb.x) + dfv_two_diff(pa.y, pb.y);
+                        big = big || !(fabsf(v.hi) < ps.Lf[k] * 0.999f);
+                        // minimum image with the float64 path's rule: v >= L/2 -> v - L, v <= -L/2 -> v + L
+                        const dfv up = v - halfL[k], dn = v + halfL[k];
+                        if (up.hi > 0.f || (up.hi == 0.f && up.lo >= 0.f))
+                            v = v - L[k];
+                        else if (dn.hi < 0.f || (dn.hi == 0.f && dn.lo <= 0.f))
+                            v = v + L[k];
+                        r[k] = v;
+                    }
+                    if (big || sc == SCREEN_NEAR) {
+                        // float64 decides (and, for far-wrapped pairs, supplies the vector)
+                        const double de = pair_exact(x, a, b, ps, r64);
+                        keep = de < ps.rc;
+                        exact = big;
+                    } else {
+                        keep = true;
+                    }
+                }
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int64_t wp = w + __popc(mask & ((1u << lane) - 1u));
+                if (exact)
+                    for (int k = 0; k < 3; ++k) r[k] = dfv(r64[k]);
+                const dfv s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+                const dfv y = df_rsqrt(s2);
+                const dfv d = s2 * y;
+                const dfv rh[3] = {r[0] * y, r[1] * y, r[2] * y};
+                dfv A(0.f, 0.f), B(0.f, 0.f);
+                const int64_t i = df_search(tab.rvf, tab.ntab, d.hi, tab.inv_dr);
+                if (i <= 0 || i >= tab.ntab) {
+                    atomicExch(err, 1);
+                } else {
+                    const float4 sr = tab.seg_r[i], sp = tab.seg_perp[i], sq = tab.seg_para[i];
+                    const dfv tt = (d - df_lo(sr)) * df_hi(sr);
+                    A = df_lo(sp) + tt * df_hi(sp);
+                    B = df_lo(sq) + tt * df_hi(sq);
+                }
+                store_pair_df(pdf, p32, wp, b, A, B, rh, d);
+            }
+            w += __popc(mask);
+        }
+    }
+}
+
+__global__ void k_pairs_df_to_f64(PairData<dfv> pd, int64_t np, PairData<double> p64) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < np; e += (int64_t)gridDim.x * blockDim.x) {
+        p64.A[e] = (double)pd.A[e];
+        p64.BA[e] = (double)pd.BA[e];
+        p64.rx[e] = (double)pd.rx[e];
+        p64.ry[e] = (double)pd.ry[e];
+        p64.rz[e] = (double)pd.rz[e];
+        p64.dist[e] = (double)pd.dist[e];
+    }
+}
+
 static PairScreen make_screen(const double *box, double rc, double maxabs) {
     PairScreen ps;
     double Lmax = 0.0;
@@ -604,6 +788,60 @@ int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double
     k_csr_fill<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], off27,
                                                      perp, para, rv, ntab, inv_dr, p64, p32, err);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+size_t df_tab_bytes(int64_t ntab) { return 256 * 4 + (size_t)ntab * (sizeof(float) + 3 * sizeof(float4)); }
+
+int df_tab_build(const double *perp, const double *para, const double *rv, int64_t ntab, void *buf, DfTab &t,
+                 cudaStream_t s) {
+    char *p = (char *)buf;
+    auto carve = [&](size_t bytes) {
+        uintptr_t u = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+        p = (char *)(u + bytes);
+        return (void *)u;
+    };
+    float *rvf = (float *)carve(sizeof(float) * ntab);
+    float4 *sr = (float4 *)carve(sizeof(float4) * ntab);
+    float4 *sp = (float4 *)carve(sizeof(float4) * ntab);
+    float4 *sq = (float4 *)carve(sizeof(float4) * ntab);
+    k_df_tab<<<grid_for(ntab, 256), 256, 0, s>>>(perp, para, rv, ntab, rvf, sr, sp, sq);
+    MPS_LAUNCH_CHECK();
+    double rv_last = 0.0;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&rv_last, rv + ntab - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    t.rvf = rvf;
+    t.seg_r = sr;
+    t.seg_perp = sp;
+    t.seg_para = sq;
+    t.ntab = ntab;
+    t.inv_dr = rv_last > 0 ? (float)((double)(ntab - 1) / rv_last) : 0.f;
+    return MPS_OK;
+}
+
+int positions_df(const double *x, int64_t n, float2 *xdf, cudaStream_t s) {
+    k_positions_df<<<grid_for(3 * n, 256), 256, 0, s>>>(x, 3 * n, xdf);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int csr_pairs_fill_df(const double *x, const float *xf, const float2 *xdf, double maxabs, const double *box, double rc,
+                      const CellBins &cb, const int64_t *cnt27, const int64_t *off27, const DfTab &tab,
+                      int64_t *row_ptr, PairData<dfv> pdf, PairData<float> p32, int *err, cudaStream_t s) {
+    const int64_t n = cb.n;
+    k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
+    MPS_LAUNCH_CHECK();
+    k_csr_fill_df<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(
+        x, xf, xdf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts, cb.starts, n, cb.ncell[0],
+        cb.ncell[1], cb.ncell[2], off27, tab, pdf, p32, err);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int pairs_df_to_f64(const PairData<dfv> &pdf, int64_t np, PairData<double> p64, cudaStream_t s) {
+    if (np == 0) return MPS_OK;
+    k_pairs_df_to_f64<<<grid_for(np, 256), 256, 0, s>>>(pdf, np, p64);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

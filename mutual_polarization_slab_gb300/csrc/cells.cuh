@@ -3,6 +3,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace mps {
 
@@ -39,5 +40,28 @@ int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double
                    const int64_t *cnt27,
                    const int64_t *off27, const double *perp, const double *para, const double *rv, int64_t ntab,
                    int64_t *row_ptr, PairData<double> p64, PairData<float> p32, int *err, cudaStream_t s);
+
+// Double-float form of the solver's pair list (the dipole operator): positions as
+// float pairs, the interpolation table per segment as double-float values.
+struct DfTab {
+    const float *rvf = nullptr;       // ntab table separations (float, for the index search)
+    const float4 *seg_r = nullptr;    // segment i: (r_{i-1}, 1/(r_i - r_{i-1})) double-float
+    const float4 *seg_perp = nullptr; // (perp_{i-1}, perp_i - perp_{i-1})
+    const float4 *seg_para = nullptr; // (para_{i-1}, para_i - para_{i-1})
+    int64_t ntab = 0;
+    float inv_dr = 0.f;               // (ntab - 1) / r_last: uniform-spacing index guess
+};
+size_t df_tab_bytes(int64_t ntab);
+int df_tab_build(const double *perp, const double *para, const double *rv, int64_t ntab, void *buf, DfTab &t,
+                 cudaStream_t s);
+int positions_df(const double *x, int64_t n, float2 *xdf, cudaStream_t s);
+// Same pair set and order as csr_pairs_fill; couplings, unit vectors and
+// separations in double-float (pdf) and float32 (p32); float64 only for the
+// keep decision of pairs in the screen's margin band.
+int csr_pairs_fill_df(const double *x, const float *xf, const float2 *xdf, double maxabs, const double *box, double rc,
+                      const CellBins &cb, const int64_t *cnt27, const int64_t *off27, const DfTab &tab,
+                      int64_t *row_ptr, PairData<dfv> pdf, PairData<float> p32, int *err, cudaStream_t s);
+// p64 = pdf converted to float64 (the float64 operator's pair data, built on demand).
+int pairs_df_to_f64(const PairData<dfv> &pdf, int64_t np, PairData<double> p64, cudaStream_t s);
 
 }  // namespace mps

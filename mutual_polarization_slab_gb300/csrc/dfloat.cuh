@@ -40,6 +40,17 @@ __device__ __forceinline__ dfv operator*(dfv a, dfv b) {
     return dfv_fast_two_sum(p, e);
 }
 
+__device__ __forceinline__ dfv operator-(dfv a) { return dfv(-a.hi, -a.lo); }
+__device__ __forceinline__ dfv operator-(dfv a, dfv b) { return a + (-b); }
+
+// Exact difference of two floats as a double-float (two-sum).
+__device__ __forceinline__ dfv dfv_two_diff(float a, float b) {
+    const float s = __fsub_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(-b, bb));
+    return dfv(s, e);
+}
+
 __device__ __forceinline__ dfv &operator+=(dfv &a, dfv b) {
     a = a + b;
     return a;

@@ -179,12 +179,24 @@ __global__ void k_rs_pairs(const double *__restrict__ m, int64_t n, int64_t nvec
 // pair data are read once and applied to every vector of the batch.
 //   out[r][a] = beta*out[r][a] + diag[r][a] m[r][a] + sum_b [A m_b + (B-A)(m_b.rhat) rhat] + slab[r] z
 // ---------------------------------------------------------------------------
-template <typename T, int G, int R>
+template <typename T>
+__device__ __forceinline__ T group_xor(T v, int o, int G) {
+    return __shfl_xor_sync(0xffffffffu, v, o, G);
+}
+template <>
+__device__ __forceinline__ dfv group_xor<dfv>(dfv v, int o, int G) {
+    return dfv(__shfl_xor_sync(0xffffffffu, v.hi, o, G), __shfl_xor_sync(0xffffffffu, v.lo, o, G));
+}
+
+// T: pair arithmetic (float, double or double-float dfv); mT: the moments read
+// by the pair loop in type TM (float64 m itself, or its double-float copy).
+template <typename T, int G, int R, typename TM = double>
 __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, double *__restrict__ out, int64_t n,
                                                 int nrhs, int r0, const int64_t *__restrict__ row_ptr,
                                                 PairData<T> pd, const double *__restrict__ diag,
                                                 const int32_t *__restrict__ diag_of_rhs,
-                                                const double *__restrict__ slab, int accumulate) {
+                                                const double *__restrict__ slab, int accumulate,
+                                                const TM *__restrict__ mT) {
     const int lane = threadIdx.x % G;
     const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
@@ -201,7 +213,7 @@ __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, do
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 if (r < nr) {
-                    const double *mb = m + ((int64_t)(r0 + r) * n + b) * 3;
+                    const TM *mb = mT + ((int64_t)(r0 + r) * n + b) * 3;
                     const T mx = (T)mb[0], my = (T)mb[1], mz = (T)mb[2];
                     const T s = ba * (mx * rx + my * ry + mz * rz);
                     acc[r][0] += av * mx + s * rx;
@@ -215,7 +227,7 @@ __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, do
 #pragma unroll
             for (int c = 0; c < 3; ++c)
 #pragma unroll
-                for (int o = G / 2; o > 0; o >>= 1) acc[r][c] += __shfl_xor_sync(0xffffffffu, acc[r][c], o, G);
+                for (int o = G / 2; o > 0; o >>= 1) acc[r][c] += group_xor(acc[r][c], o, G);
         if (lane == 0) {
             for (int r = 0; r < nr; ++r) {
                 const int rr = r0 + r;
@@ -248,13 +260,13 @@ int real_space_csr(const double *m, double *out, int64_t n, int nrhs, const int6
     for (int r0 = 0; r0 < nrhs; r0 += 4) {
         int nr = nrhs - r0;
         if (nr >= 4)
-            k_rs_csr<T, G, 4><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate);
+            k_rs_csr<T, G, 4><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
         else if (nr == 3)
-            k_rs_csr<T, G, 3><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate);
+            k_rs_csr<T, G, 3><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
         else if (nr == 2)
-            k_rs_csr<T, G, 2><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate);
+            k_rs_csr<T, G, 2><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
         else
-            k_rs_csr<T, G, 1><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate);
+            k_rs_csr<T, G, 1><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
         MPS_LAUNCH_CHECK();
     }
     return MPS_OK;
@@ -264,6 +276,34 @@ template int real_space_csr<double>(const double *, double *, int64_t, int, cons
                                     const double *, const int32_t *, const double *, bool, cudaStream_t);
 template int real_space_csr<float>(const double *, double *, int64_t, int, const int64_t *, PairData<float>,
                                    const double *, const int32_t *, const double *, bool, cudaStream_t);
+
+__global__ void k_to_dfv(const double *__restrict__ m, int64_t total, dfv *__restrict__ md) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        md[i] = dfv(m[i]);
+}
+
+int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
+                      PairData<dfv> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
+                      bool accumulate, cudaStream_t s) {
+    k_to_dfv<<<grid_for((int64_t)nrhs * n * 3, 256), 256, 0, s>>>(m, (int64_t)nrhs * n * 3, mdf);
+    MPS_LAUNCH_CHECK();
+    constexpr int G = 8;
+    const unsigned grid = grid_for(n * G, 256, 152 * 64);
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = nrhs - r0;
+        if (nr >= 3)
+            k_rs_csr<dfv, G, 3, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                          accumulate, mdf);
+        else if (nr == 2)
+            k_rs_csr<dfv, G, 2, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                          accumulate, mdf);
+        else
+            k_rs_csr<dfv, G, 1, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                          accumulate, mdf);
+        MPS_LAUNCH_CHECK();
+    }
+    return MPS_OK;
+}
 
 // Diagonal (dielectric + self) per particle and permittivity set.
 __global__ void k_diag(const double *__restrict__ lam, int64_t total, double self_perp, double *__restrict__ diag) {

@@ -270,7 +270,8 @@ def test_mixed_precision_accuracy(golden_c1):
                              perp, para, rv, slab_factor=0.0, max_rhs=3) as s:
         x64, i64 = s.solve(b, tol=1e-11, restart=30, maxit=50)
         runs = [s.solve(b, tol=1e-8, restart=30, maxit=10, precision="mixed", inner_tol=1e-4, residual_policy=pol,
-                        verify=True) for pol in (0, 1)]
+                        verify=True, inner_operator=inner)
+                for pol, inner in ((0, "reference"), (1, "reference"), (0, "grad"))]
     x64 = x64.cpu().numpy()
     assert all(i.converged for i in i64)
     for xm, im in runs:
@@ -280,8 +281,10 @@ def test_mixed_precision_accuracy(golden_c1):
             err = np.linalg.norm(xm[r] - x64[r]) / np.linalg.norm(x64[r])
             assert err < 1e-6, err
         assert im[0].matvecs_fp32 > im[0].matvecs_fp64
-    # policy 0: one float64 residual + the verification
+    # policy 0 with the reference-discretisation inner operator: one float64 residual + the verification;
+    # with the gradient form at most one more true residual (the drift check)
     assert runs[0][1][0].matvecs_fp64 == 2
+    assert runs[2][1][0].matvecs_fp64 <= 3
 
 
 def test_contrast_batch_diag_index(golden_small):
