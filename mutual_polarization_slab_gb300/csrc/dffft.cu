@@ -99,6 +99,10 @@ struct ArithDF {
     __device__ static __forceinline__ V conj(V a) { return cconj(a); }
     __device__ static __forceinline__ V zero() { return czero(); }
     __device__ static __forceinline__ V make(double re, double im) { return {dfrom(re), dfrom(im)}; }
+    // grids stored as (hi, lo) pairs
+    __device__ static __forceinline__ V make(float2 re, float2 im) { return {{re.x, re.y}, {im.x, im.y}}; }
+    __device__ static __forceinline__ float2 re_s(V a) { return make_float2(a.re.hi, a.re.lo); }
+    __device__ static __forceinline__ float2 nim_s(V a) { return make_float2(-a.im.hi, -a.im.lo); }
     __device__ static __forceinline__ double re(V a) { return dto(a.re); }
     __device__ static __forceinline__ double im(V a) { return dto(a.im); }
     __device__ static __forceinline__ V zero_im(V a) { return {a.re, {0.f, 0.f}}; }
@@ -128,6 +132,8 @@ struct ArithF32 {
     __device__ static __forceinline__ V conj(V a) { return make_float2(a.x, -a.y); }
     __device__ static __forceinline__ V zero() { return make_float2(0.f, 0.f); }
     __device__ static __forceinline__ V make(float re, float im) { return make_float2(re, im); }
+    __device__ static __forceinline__ float re_s(V a) { return a.x; }
+    __device__ static __forceinline__ float nim_s(V a) { return -a.y; }
     __device__ static __forceinline__ float re(V a) { return a.x; }
     __device__ static __forceinline__ float im(V a) { return a.y; }
     __device__ static __forceinline__ V zero_im(V a) { return make_float2(a.x, 0.f); }
@@ -278,7 +284,7 @@ __global__ void __launch_bounds__(128) k_fft_x_fwd(const Rl *__restrict__ grid, 
         const bool has1 = y0 + 1 < Ny;
         const Rl *r0 = grid + (cz * Ny + y0) * (int64_t)Nx;
         const Rl *r1 = r0 + Nx;
-        for (int n = lane; n < Nx; n += 32) Ab[n] = A::st(A::make(r0[n], has1 ? r1[n] : (Rl)0));
+        for (int n = lane; n < Nx; n += 32) Ab[n] = A::st(A::make(r0[n], has1 ? r1[n] : Rl{}));
         __syncwarp();
         const S *Z = fft_line<A>(Ab, Bb, px, sm, lane);
         S *o0 = spec + (cz * Ny + y0) * (int64_t)Nxh;
@@ -333,8 +339,8 @@ __global__ void __launch_bounds__(128) k_fft_x_inv(const typename A::S *__restri
         Rl *r1 = r0 + Nx;
         for (int n = lane; n < Nx; n += 32) {
             const auto z = A::ld(Z[n]);   // conj of the inverse: re as is, im negated
-            r0[n] = (Rl)A::re(z);
-            if (has1) r1[n] = -(Rl)A::im(z);
+            r0[n] = A::re_s(z);
+            if (has1) r1[n] = A::nim_s(z);
         }
         __syncwarp();
     }
@@ -660,17 +666,17 @@ static int launch_z_scale(typename A::S *spec, int nrhs, const GridParams &gp, c
     return MPS_OK;
 }
 
-int df_forward_xy(const double *grid, float4 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
+int df_forward_xy(const float2 *grid, float4 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
                   cudaStream_t s) {
     if (!pl.ok) return MPS_BAD_ARG;
-    MPS_TRY_STATUS((launch_x<ArithDF, double>(true, grid, nullptr, spec, ncomp, gp, pl.ax[0], s)));
+    MPS_TRY_STATUS((launch_x<ArithDF, float2>(true, grid, nullptr, spec, ncomp, gp, pl.ax[0], s)));
     return launch_y<ArithDF>(spec, ncomp, gp, pl.ax[1], 0, s);
 }
 
-int df_inverse_yx(float4 *spec, double *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s) {
+int df_inverse_yx(float4 *spec, float2 *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s) {
     if (!pl.ok) return MPS_BAD_ARG;
     MPS_TRY_STATUS(launch_y<ArithDF>(spec, ncomp, gp, pl.ax[1], 1, s));
-    return launch_x<ArithDF, double>(false, nullptr, grid, spec, ncomp, gp, pl.ax[0], s);
+    return launch_x<ArithDF, float2>(false, nullptr, grid, spec, ncomp, gp, pl.ax[0], s);
 }
 
 int df_z_scale_dipole(float4 *spec, int nrhs, const GridParams &gp, const DfPlan3 &pl, const double *H,

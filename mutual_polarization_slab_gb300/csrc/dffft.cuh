@@ -35,19 +35,19 @@ struct DfPlan3 {
 // axis is longer than 1024.
 int df_plan(const GridParams &gp, DfPlan3 *out);
 
-// Forward: float64 real grids (ncomp x [Nz][Ny][Nx]) -> double-float half
+// Forward: double-float real grids ((hi, lo) float pairs, ncomp x [Nz][Ny][Nx]) -> double-float half
 // spectra (ncomp x [Nz][Ny][Nx/2+1], float4 per complex value) in spec.
 // Inverse: the reverse, unnormalised.  For the dipole operator the z pass of the
 // forward transform, the Green's scale and the z pass of the inverse run in one
 // kernel (scale_dipole): spec then never holds the unscaled z-transformed data.
-int df_forward_xy(const double *grid, float4 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
+int df_forward_xy(const float2 *grid, float4 *spec, int ncomp, const GridParams &gp, const DfPlan3 &pl,
                   cudaStream_t s);
 int df_z_scale_dipole(float4 *spec, int nrhs, const GridParams &gp, const DfPlan3 &pl, const double *H,
                       const float2 *tm6, cudaStream_t s);
 // The scale tensor of the double-float z pass, 6 double-float entries per
 // half-spectrum point (6 x Gc float2), built once per grid.
 int df_scale_table(const GridParams &gp, const double *H, float2 *tm6, cudaStream_t s);
-int df_inverse_yx(float4 *spec, double *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s);
+int df_inverse_yx(float4 *spec, float2 *grid, int ncomp, const GridParams &gp, const DfPlan3 &pl, cudaStream_t s);
 
 // The same transforms in float32 (float2 per complex value) for the float32
 // operator: the z pass, Green's scale and inverse z pass fused as above.

@@ -8,7 +8,7 @@
 
 namespace mps {
 
-struct dfv {
+struct __align__(8) dfv {
     float hi, lo;
     dfv() = default;
     __device__ __forceinline__ dfv(float h, float l) : hi(h), lo(l) {}

@@ -18,6 +18,9 @@
 // 16 x 16 x TZ tile, deterministic, no atomics).
 #include "gradop.cuh"
 
+#include <cstdlib>
+#include <cstring>
+
 namespace mps {
 
 constexpr int kGChunk = 32;
@@ -153,6 +156,172 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     }
 }
 
+// Spread of the gradient form by scatter into private tile copies.  The CTA owns
+// a 16 x 16 x TZ tile; the tile's particle list (fixed order) is dealt to the NW
+// warps round-robin; each warp adds its particles' overlap with the tile into its
+// own copy of the tile in shared memory (lanes over the overlap's (x, y) columns,
+// the z range inside), so no two lanes or warps ever update one word at once.  The
+// copies are then summed in warp order: deterministic, no atomics, and every lane
+// slot works on a node of the stencil (the owner-computes kernel above visits the
+// whole tile for every particle).  Needs N >= tile + P on every axis, so that a
+// stencil's overlap with a tile is one interval (otherwise the kernel above runs).
+constexpr int kSRow = kTileX + 1;
+
+template <int TZ, int NR>
+struct ScatterShape {
+    // plane stride = 24 mod 32 words: lanes on planes z..z+3 of one row start 8 banks apart
+    static constexpr int kPlane = kTileY * kSRow + 8;
+    static constexpr int kCopy = NR * TZ * kPlane;       // one tile copy (floats)
+    static constexpr int kStage = 2 * 3 * kMaxP + 4 * NR;  // w, g of the 3 axes + moments (padded)
+    static constexpr int kWarps = TZ >= 8 ? 4 : 8;
+    static constexpr size_t kSmem = sizeof(float) * (size_t)kWarps * (kCopy + kStage);
+};
+
+// Interval of tile-local coordinates [lo, lo + cnt) covered by a stencil whose
+// first node is s, and the stencil index of its first covered node.
+__device__ __forceinline__ void tile_interval(int s, int T0, int Tn, int P, int N, int &lo, int &cnt, int &j0) {
+    int o = T0 - s;   // stencil index of tile node 0
+    if (o < 0) o += N;
+    if (o < P) {
+        lo = 0;
+        j0 = o;
+    } else {
+        lo = N - o;
+        j0 = 0;
+    }
+    cnt = min(lo + (P - j0), Tn) - lo;
+}
+
+template <int TZ, int NR>
+__global__ void __launch_bounds__(ScatterShape<TZ, NR>::kWarps * 32)
+    k_spread_grad_scatter(const double *__restrict__ m, int64_t n, int r0, const int32_t *__restrict__ start,
+                          const float *__restrict__ w, const float *__restrict__ g, GridParams gp,
+                          const int64_t *__restrict__ tstart, const int32_t *__restrict__ entries, int ntx, int nty,
+                          float *__restrict__ grid) {
+    using S = ScatterShape<TZ, NR>;
+    constexpr int NW = S::kWarps;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *copies = (float *)smem_raw;                 // [NW][NR][TZ][16][kSRow]
+    float *stage = copies + NW * S::kCopy;             // [NW][kStage]
+    const int64_t t = blockIdx.x;
+    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
+    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int Tx = min(kTileX, Nx - X0), Ty = min(kTileY, Ny - Y0), Tz = min(TZ, Nz - Z0);
+    const int P = gp.P;
+    const int64_t G = gp.G;
+    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
+    if (e0 == e1) {
+        for (int idx = threadIdx.x; idx < NR * TZ * kTileX * kTileY; idx += NW * 32) {
+            const int x = idx & (kTileX - 1), y = (idx >> 4) & (kTileY - 1), zr = idx >> 8;
+            const int z = zr % TZ, r = zr / TZ;
+            if (x < Tx && y < Ty && z < Tz)
+                grid[(int64_t)(r0 + r) * G + ((int64_t)(Z0 + z) * Ny + (Y0 + y)) * Nx + (X0 + x)] = 0.f;
+        }
+        return;
+    }
+    for (int i = threadIdx.x; i < NW * S::kCopy / 4; i += NW * 32)
+        reinterpret_cast<float4 *>(copies)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float *acc = copies + wid * S::kCopy;
+    float *wb = stage + wid * S::kStage;   // w of the 3 axes, flat (axis * P + j)
+    float *gb = wb + 3 * kMaxP;
+    // Software pipeline over this warp's particles: entry ids two visits ahead,
+    // the particle's factors, moments and stencil start one visit ahead, so the
+    // global loads overlap the previous particle's scatter.
+    const unsigned FULL = 0xffffffffu;
+    auto entry_at = [&](int64_t e) -> int32_t { return e < e1 ? entries[e] : -1; };
+    float pw0 = 0.f, pw1 = 0.f, pg0 = 0.f, pg1 = 0.f, pm = 0.f;
+    int ps = 0;
+    auto fetch = [&](int32_t a) {
+        if (a < 0) return;
+        const int64_t b = (int64_t)a * 3 * P;
+        if (lane < 3 * P) {
+            pw0 = w[b + lane];
+            pg0 = g[b + lane];
+        }
+        if (lane + 32 < 3 * P) {
+            pw1 = w[b + lane + 32];
+            pg1 = g[b + lane + 32];
+        }
+        if (lane < 3 * NR) pm = (float)m[((int64_t)(r0 + lane / 3) * n + a) * 3 + lane % 3];
+        if (lane < 3) ps = start[3 * (int64_t)a + lane];
+    };
+    int64_t e = e0 + wid;
+    fetch(entry_at(e));
+    int32_t a_next = entry_at(e + NW);
+    for (; e < e1; e += NW) {
+        // commit the prefetched particle
+        if (lane < 3 * P) {
+            wb[lane] = pw0;
+            gb[lane] = pg0;
+        }
+        if (lane + 32 < 3 * P) {
+            wb[lane + 32] = pw1;
+            gb[lane + 32] = pg1;
+        }
+        float mr[3 * NR];
+#pragma unroll
+        for (int c = 0; c < 3 * NR; ++c) mr[c] = __shfl_sync(FULL, pm, c);
+        const int sx = __shfl_sync(FULL, ps, 0), sy = __shfl_sync(FULL, ps, 1), sz = __shfl_sync(FULL, ps, 2);
+        // prefetch the next particle, and the entry id after it
+        fetch(a_next);
+        a_next = entry_at(e + 2 * NW);
+        int xlo, nx, jx0, ylo, ny, jy0, zlo, nz, jz0;
+        tile_interval(sx, X0, Tx, P, Nx, xlo, nx, jx0);
+        tile_interval(sy, Y0, Ty, P, Ny, ylo, ny, jy0);
+        tile_interval(sz, Z0, Tz, P, Nz, zlo, nz, jz0);
+        __syncwarp();
+        if (nx > 0 && ny > 0 && nz > 0) {
+            // lanes over the overlap's (x, z) columns, the y range inside:
+            // value = wy (mx gx wz + mz wx gz) + gy (my wx wz)
+            const float rnx = __frcp_rn((float)nx);
+            const int ncol = nx * nz;
+            for (int q = lane; q < ncol; q += 32) {
+                const int jz = __float2int_rz(((float)q + 0.5f) * rnx);
+                const int jx = q - jz * nx;
+                const float wx = wb[jx0 + jx], gx = gb[jx0 + jx];
+                const float wz = wb[2 * P + jz0 + jz], gz = gb[2 * P + jz0 + jz];
+                const float gxwz = gx * wz, wxgz = wx * gz, wxwz = wx * wz;
+                float al[NR], be[NR];
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    al[r] = mr[3 * r] * gxwz + mr[3 * r + 2] * wxgz;
+                    be[r] = mr[3 * r + 1] * wxwz;
+                }
+                float *col = acc + (zlo + jz) * S::kPlane + ylo * kSRow + (xlo + jx);
+                const float *wyp = wb + P + jy0, *gyp = gb + P + jy0;
+                for (int jy = 0; jy < ny; ++jy) {
+                    const float wy = wyp[jy], gy = gyp[jy];
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) {
+                        float *pr = col + jy * kSRow + r * TZ * S::kPlane;
+                        *pr += wy * al[r] + gy * be[r];
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < NR * TZ * kTileX * kTileY; idx += NW * 32) {
+        const int x = idx & (kTileX - 1), y = (idx >> 4) & (kTileY - 1), zr = idx >> 8;
+        const int z = zr % TZ, r = zr / TZ;
+        if (x < Tx && y < Ty && z < Tz) {
+            const int off = (r * TZ + z) * S::kPlane + y * kSRow + x;
+            float v = copies[off];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) v += copies[q * S::kCopy + off];
+            grid[(int64_t)(r0 + r) * G + ((int64_t)(Z0 + z) * Ny + (Y0 + y)) * Nx + (X0 + x)] = v;
+        }
+    }
+}
+
+bool scatter_supported(const GridParams &gp, int tz) {
+    return gp.N[0] >= kTileX + gp.P && gp.N[1] >= kTileY + gp.P && gp.N[2] >= tz + gp.P;
+}
+
 constexpr int kGRowPad = kTileX + 1;
 
 template <int TZ, int NR>
@@ -277,6 +446,89 @@ __global__ void k_contract_grad_gather(const float *__restrict__ partial, int64_
     }
 }
 
+// Contraction as a warp-per-particle gather: the grids of the gradient form (one
+// per vector) are small enough to be read mostly from L2.  Lanes take the (x, y)
+// columns of the stencil, each runs its z column; fixed summation order.  Warps
+// visit particles in `order` (spatially sorted: the warps of one CTA read
+// overlapping stencils, so much of it comes from L1); null = input order.
+template <int NR>
+__global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__restrict__ grid, int64_t n, int r0,
+                                                            const int32_t *__restrict__ order,
+                                                            const int32_t *__restrict__ start,
+                                                            const float *__restrict__ w, const float *__restrict__ g,
+                                                            GridParams gp, double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int64_t G = gp.G;
+    for (int64_t i = warp; i < n; i += nw) {
+        const int64_t a = order ? order[i] : i;
+        const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
+        const float *wa = w + a * 3 * P, *ga = g + a * 3 * P;
+        float acc[3 * NR];
+#pragma unroll
+        for (int c = 0; c < 3 * NR; ++c) acc[c] = 0.f;
+        for (int idx = lane; idx < P * P; idx += 32) {
+            const int jx = idx % P, jy = idx / P;
+            int ix = sx + jx;
+            if (ix >= Nx) ix -= Nx;
+            int iy = sy + jy;
+            if (iy >= Ny) iy -= Ny;
+            const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
+            float s0[NR], s1[NR];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) s0[r] = s1[r] = 0.f;
+            // unrolled so that 5 x NR loads are in flight per lane
+#pragma unroll 5
+            for (int jz = 0; jz < P; ++jz) {
+                int iz = sz + jz;
+                if (iz >= Nz) iz -= Nz;
+                const int64_t node = rowb + (int64_t)Nx * Ny * iz;
+                const float wz = wa[2 * P + jz], gz = ga[2 * P + jz];
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    const float v = __ldg(grid + (int64_t)(r0 + r) * G + node);
+                    s0[r] += v * wz;
+                    s1[r] += v * gz;
+                }
+            }
+            const float wx = wa[jx], wy = wa[P + jy], gx = ga[jx], gy = ga[P + jy];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                acc[3 * r + 0] += gx * wy * s0[r];
+                acc[3 * r + 1] += wx * gy * s0[r];
+                acc[3 * r + 2] += wx * wy * s1[r];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3 * NR; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane == 0)
+#pragma unroll
+            for (int r = 0; r < NR; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    out[((int64_t)(r0 + r) * n + a) * 3 + c] = (double)acc[3 * r + c] * gp.hprod;
+    }
+}
+
+int contract_grad_warp(const float *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start,
+                       const float *w, const float *g, const GridParams &gp, double *out, cudaStream_t s) {
+    const unsigned blocks = grid_for(n * 32, 256, 152 * 64);
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        if (nr == 3)
+            k_contract_grad_warp<3><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, g, gp, out);
+        else if (nr == 2)
+            k_contract_grad_warp<2><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, g, gp, out);
+        else
+            k_contract_grad_warp<1><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, g, gp, out);
+        MPS_LAUNCH_CHECK();
+    }
+    return MPS_OK;
+}
+
 int grad_factors(const double *x, int64_t n, const GridParams &gp, const double *w64, float *g32, cudaStream_t s) {
     k_grad_factors<<<grid_for(3 * n, 256), 256, 0, s>>>(x, n, gp, w64, g32);
     MPS_LAUNCH_CHECK();
@@ -295,8 +547,20 @@ static int grad_launch(const double *m, int64_t n, int r0, const int32_t *start,
                        const GridParams &gp, const TileBins &tb, float *grid, float *partial, double *out,
                        bool spread_phase, cudaStream_t s) {
     if (spread_phase) {
-        k_spread_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start,
-                                                                         tb.entries, tb.ntx, tb.nty, grid);
+        // MPS_GRAD_SPREAD=scatter selects the private-copy scatter (A/B timing; it is
+        // limited by shared-memory occupancy and measured no faster than the tiled one)
+        const char *e = getenv("MPS_GRAD_SPREAD");
+        if (scatter_supported(gp, TZ) && e && strcmp(e, "scatter") == 0) {
+            using S = ScatterShape<TZ, NR>;
+            if (S::kSmem > 48 * 1024)
+                MPS_CUDA_TRY(cudaFuncSetAttribute(k_spread_grad_scatter<TZ, NR>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::kSmem));
+            k_spread_grad_scatter<TZ, NR><<<(unsigned)tb.ntiles, S::kWarps * 32, S::kSmem, s>>>(
+                m, n, r0, start, w, g, gp, tb.tile_start, tb.entries, tb.ntx, tb.nty, grid);
+        } else {
+            k_spread_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start,
+                                                                             tb.entries, tb.ntx, tb.nty, grid);
+        }
         MPS_LAUNCH_CHECK();
         return MPS_OK;
     }

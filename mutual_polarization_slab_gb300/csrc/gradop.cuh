@@ -15,4 +15,8 @@ int spread_grad_tiled(const double *m, int64_t n, int nrhs, const int32_t *start
 int contract_grad_tiled(const float *grid, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
                         const GridParams &gp, const TileBins &tb, float *partial, double *out, cudaStream_t s);
 
+// The same contraction as one warp per particle gathering from the grids (no tiles).
+int contract_grad_warp(const float *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start,
+                       const float *w, const float *g, const GridParams &gp, double *out, cudaStream_t s);
+
 }  // namespace mps

@@ -110,6 +110,7 @@ struct mps_system {
     double *cs_h64 = nullptr;       // half spectrum: exp(-(1-eta) q^2 / 4 xi^2) / q^2 / G
     float *cs_h32 = nullptr;
     int32_t *start = nullptr;
+    int32_t *order = nullptr;        // particle ids sorted by (cell, id): spatial visiting order
     double *w64 = nullptr;
     float *w32 = nullptr;
     double *h64 = nullptr;       // owned by green (shared, cached per grid)
@@ -153,7 +154,7 @@ static void free_system(mps_system *s) {
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
                     s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->g32, s->pdf.A, s->pdf.BA,
-                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf};
+                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -545,28 +546,33 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
             s->green->tm6 = tm;
         }
     }
-    double *grid = s->grid64;
+    dfv *grid = (dfv *)s->grid64;           // (hi, lo) float pairs: the size of a double
     float4 *spec = (float4 *)s->spec64;     // float4 per complex value: the size of a double2
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, MPS_DF, &ev, st));
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
     STAGE_MARK(1);
-    if (use_tiles)
+    const int64_t gvals = (int64_t)3 * nrhs * s->gp.G;
+    if (use_tiles) {
         MPS_TRY(spread_tiled_df(m, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, grid, st));
-    else
-        MPS_TRY(spread<double>(m, s->n, nrhs, s->start, s->w64, s->gp, grid, st));
+    } else {
+        MPS_TRY(spread<double>(m, s->n, nrhs, s->start, s->w64, s->gp, s->grid64, st));
+        MPS_TRY(f64_to_dfv_inplace(s->grid64, gvals, st));
+    }
     STAGE_MARK(2);
-    MPS_TRY(df_forward_xy(grid, spec, 3 * nrhs, s->gp, s->dfp, st));
+    MPS_TRY(df_forward_xy((const float2 *)grid, spec, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(3);
     MPS_TRY(df_z_scale_dipole(spec, nrhs, s->gp, s->dfp, s->h64, s->green->tm6, st));
     STAGE_MARK(4);
-    MPS_TRY(df_inverse_yx(spec, grid, 3 * nrhs, s->gp, s->dfp, st));
+    MPS_TRY(df_inverse_yx(spec, (float2 *)grid, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(5);
-    if (use_tiles)
+    if (use_tiles) {
         MPS_TRY(contract_tiled_df(grid, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, s->partial64, out, st));
-    else
-        MPS_TRY(contract<double>(grid, s->n, nrhs, s->start, s->w64, s->gp, out, st));
+    } else {
+        MPS_TRY(dfv_to_f64_inplace(s->grid64, gvals, st));
+        MPS_TRY(contract<double>(s->grid64, s->n, nrhs, s->start, s->w64, s->gp, out, st));
+    }
     STAGE_MARK(6);
     if (!s->mdf) MPS_TRY(dalloc(&s->mdf, sizeof(dfv) * 3 * (size_t)s->n * s->max_rhs, st));
     MPS_TRY(real_space_csr_df(m, s->mdf, out, s->n, nrhs, s->row_ptr, s->pdf, s->diag, s->diag_idx, s->slab, true,
@@ -683,8 +689,15 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     STAGE_MARK(4);
     MPS_TRY(exec_plan(s, CUFFT_C2R, nrhs, s->spec32, s->grid32, 0, st));
     STAGE_MARK(5);
-    MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->partial32, out,
-                                st));
+    {
+        // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing); default: warp gather
+        const char *e = getenv("MPS_GRAD_CONTRACT");
+        if (e && strcmp(e, "tiled") == 0)
+            MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->partial32,
+                                        out, st));
+        else
+            MPS_TRY(contract_grad_warp(s->grid32, s->n, nrhs, s->order, s->start, s->w32, s->g32, s->gp, out, st));
+    }
     STAGE_MARK(6);
     MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
     STAGE_MARK(7);
@@ -1463,6 +1476,10 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CellBins cb;
     rc = cell_assign(s->x, n, d->box, s->ncell, cell3, st);
     if (!rc) rc = cell_bins_build(cell3, n, s->ncell, bins, cb, st);
+    if (!rc) rc = dalloc(&s->order, sizeof(int32_t) * n, st);
+    if (!rc && n > 0 && cudaMemcpyAsync(s->order, cb.sorted, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st) !=
+                            cudaSuccess)
+        rc = MPS_CUDA_ERR;
     int64_t np = 0;
     if (!rc) rc = positions_f32(s->x, n, xf, maxbits, &maxabs, st);
     if (!rc) rc = csr_pairs_count(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);

@@ -294,10 +294,10 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
 // ---------------------------------------------------------------------------
 constexpr int kRowPad = kTileX + 1;  // padded tile row: rows y and y+2 no longer share banks
 
-// T: accumulation arithmetic; TG: grid (and weight) element type; TP: partial type.
-template <typename T, int TZ, int NR, typename TG = T, typename TP = T>
+// T: accumulation arithmetic; TG: grid element type; TP: partial type; TW: weight type.
+template <typename T, int TZ, int NR, typename TG = T, typename TP = T, typename TW = TG>
 __global__ void __launch_bounds__(256) k_contract_tiled(const TG *__restrict__ grid, int r0,
-                                                        const int32_t *__restrict__ start, const TG *__restrict__ w,
+                                                        const int32_t *__restrict__ start, const TW *__restrict__ w,
                                                         GridParams gp, const int64_t *__restrict__ tstart,
                                                         const int32_t *__restrict__ entries, int ntx, int nty,
                                                         TP *__restrict__ partial) {
@@ -432,39 +432,39 @@ int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, con
 }
 
 int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
-                    const TileBins &tb, double *grid, cudaStream_t s) {
-    if (tb.tz == 8) return spread_dispatch<dfv, 8, double, double>(m, n, nrhs, start, w, gp, tb, grid, s);
-    if (tb.tz == 4) return spread_dispatch<dfv, 4, double, double>(m, n, nrhs, start, w, gp, tb, grid, s);
+                    const TileBins &tb, dfv *grid, cudaStream_t s) {
+    if (tb.tz == 8) return spread_dispatch<dfv, 8, double, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 4) return spread_dispatch<dfv, 4, double, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
     return MPS_BAD_ARG;
 }
 
-template <typename T, int TZ, int NR, typename TG, typename TP>
-static int contract_launch(const TG *grid, int64_t n, int r0, const int32_t *start, const TG *w,
+template <typename T, int TZ, int NR, typename TG, typename TP, typename TW>
+static int contract_launch(const TG *grid, int64_t n, int r0, const int32_t *start, const TW *w,
                            const GridParams &gp, const TileBins &tb, TP *partial, double *out, cudaStream_t s) {
     constexpr int C = 3 * NR;
     const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileY * kRowPad + 8 * 3 * kMaxP);
     static bool attr_set = false;  // one attribute call per instantiation
     if (!attr_set) {
-        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR, TG, TP>,
+        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR, TG, TP, TW>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    k_contract_tiled<T, TZ, NR, TG, TP><<<(unsigned)tb.ntiles, 256, smem, s>>>(grid, r0, start, w, gp, tb.tile_start,
-                                                                               tb.entries, tb.ntx, tb.nty, partial);
+    k_contract_tiled<T, TZ, NR, TG, TP, TW><<<(unsigned)tb.ntiles, 256, smem, s>>>(
+        grid, r0, start, w, gp, tb.tile_start, tb.entries, tb.ntx, tb.nty, partial);
     MPS_LAUNCH_CHECK();
     k_contract_gather<TP, NR><<<grid_for(n, 256), 256, 0, s>>>(partial, n, r0, tb.pstart, tb.pentry, gp.hprod, out);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
 
-template <typename T, int TZ, typename TG, typename TP>
-static int contract_dispatch(const TG *grid, int64_t n, int nrhs, const int32_t *start, const TG *w,
+template <typename T, int TZ, typename TG, typename TP, typename TW>
+static int contract_dispatch(const TG *grid, int64_t n, int nrhs, const int32_t *start, const TW *w,
                              const GridParams &gp, const TileBins &tb, TP *partial, double *out, cudaStream_t s) {
     for (int r0 = 0; r0 < nrhs; r0 += 3) {
         const int nr = min(3, nrhs - r0);
-        int rc = nr == 3 ? contract_launch<T, TZ, 3, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s)
-                 : nr == 2 ? contract_launch<T, TZ, 2, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s)
-                           : contract_launch<T, TZ, 1, TG, TP>(grid, n, r0, start, w, gp, tb, partial, out, s);
+        int rc = nr == 3   ? contract_launch<T, TZ, 3, TG, TP, TW>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                 : nr == 2 ? contract_launch<T, TZ, 2, TG, TP, TW>(grid, n, r0, start, w, gp, tb, partial, out, s)
+                           : contract_launch<T, TZ, 1, TG, TP, TW>(grid, n, r0, start, w, gp, tb, partial, out, s);
         if (rc) return rc;
     }
     return MPS_OK;
@@ -473,16 +473,45 @@ static int contract_dispatch(const TG *grid, int64_t n, int nrhs, const int32_t 
 template <typename T>
 int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, const T *w, const GridParams &gp,
                    const TileBins &tb, T *partial, double *out, cudaStream_t s) {
-    if (tb.tz == 8) return contract_dispatch<T, 8, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
-    if (tb.tz == 4) return contract_dispatch<T, 4, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 8) return contract_dispatch<T, 8, T, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 4) return contract_dispatch<T, 4, T, T, T>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
     return MPS_BAD_ARG;
 }
 
-int contract_tiled_df(const double *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
+int contract_tiled_df(const dfv *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
                       const GridParams &gp, const TileBins &tb, double *partial, double *out, cudaStream_t s) {
-    if (tb.tz == 8) return contract_dispatch<dfv, 8, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
-    if (tb.tz == 4) return contract_dispatch<dfv, 4, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 8)
+        return contract_dispatch<dfv, 8, dfv, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
+    if (tb.tz == 4)
+        return contract_dispatch<dfv, 4, dfv, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
     return MPS_BAD_ARG;
+}
+
+// In-place reinterpretation of a grid between float64 values and (hi, lo) pairs
+// (same 8 bytes per value; each thread reads and writes only its own element).
+__global__ void k_f64_to_dfv(double *__restrict__ g, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const dfv v(g[i]);
+        reinterpret_cast<dfv *>(g)[i] = v;
+    }
+}
+__global__ void k_dfv_to_f64(double *__restrict__ g, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const dfv v = reinterpret_cast<const dfv *>(g)[i];
+        g[i] = (double)v;
+    }
+}
+
+int f64_to_dfv_inplace(double *g, int64_t total, cudaStream_t s) {
+    k_f64_to_dfv<<<grid_for(total, 256), 256, 0, s>>>(g, total);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+int dfv_to_f64_inplace(double *g, int64_t total, cudaStream_t s) {
+    k_dfv_to_f64<<<grid_for(total, 256), 256, 0, s>>>(g, total);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
 }
 
 template int spread_tiled<float>(const double *, int64_t, int, const int32_t *, const float *, const GridParams &,

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "grid.cuh"
+#include "dfloat.cuh"
 
 namespace mps {
 
@@ -38,10 +39,14 @@ int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, con
                    const TileBins &tb, T *partial, double *out, cudaStream_t s);
 
 // The same kernels with double-float accumulation (float-pair arithmetic) on
-// float64 weights and grids: the float64-accurate matvec without float64 issue.
+// float64 weights, the grids stored as (hi, lo) float pairs: the float64-accurate
+// matvec without float64 issue (no conversion to or from float64 between stages).
 int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
-                    const TileBins &tb, double *grid, cudaStream_t s);
-int contract_tiled_df(const double *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
+                    const TileBins &tb, dfv *grid, cudaStream_t s);
+int contract_tiled_df(const dfv *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
                       const GridParams &gp, const TileBins &tb, double *partial, double *out, cudaStream_t s);
+// Grid storage conversions in place (float64 <-> (hi, lo) pairs), for the untiled kernels.
+int f64_to_dfv_inplace(double *g, int64_t total, cudaStream_t s);
+int dfv_to_f64_inplace(double *g, int64_t total, cudaStream_t s);
 
 }  // namespace mps
