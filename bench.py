@@ -230,7 +230,8 @@ def run_gpu(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     s_setup = make_system()
-    s_setup.matvec(b[:1], precision="fp32")     # first matvec of a system bins the particles into tiles
+    # first matvec of a system bins the particles into tiles (the inner operator of the solve)
+    s_setup.matvec(b[:1], precision="fp32grad" if args.inner == "grad" else "fp32")
     e1.record()
     torch.cuda.synchronize()
     setup_ms = e0.elapsed_time(e1)
@@ -290,6 +291,20 @@ def run_gpu(args):
         print(json.dumps(out), flush=True)
 
 
+def measured_traffic(kernel, n, ngrid):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of ``kernel``
+    from the committed ncu capture of this workload (profiles/dram_traffic_*.txt:
+    lines "kernel n nx ny nz bytes_per_launch"), or None when no capture matches."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "dram_traffic_*.txt"))):
+        for line in open(path):
+            f = line.split()
+            if len(f) == 6 and not line.startswith("#") and f[0] == kernel and int(f[1]) == n \
+                    and [int(v) for v in f[2:5]] == [int(v) for v in ngrid]:
+                return float(f[5])
+    return None
+
+
 def roofline(w, st, inner="grad"):
     """Dominant kernel (largest stage time of this library's kernels in the fp32 matvec) vs HBM peak.
     Algorithmic bytes per launch, R = 3 vectors, s = 4 bytes: the grids written or read once
@@ -326,12 +341,13 @@ def roofline(w, st, inner="grad"):
         avg_ms = cand[top] / cnt
     achieved = algo[top] / (avg_ms / 1e3) / 1e9
     kname = {"spread": "k_spread_grad_tiled" if inner == "grad" else "k_spread_tiled",
-             "contract": "k_contract_grad_tiled + gather" if inner == "grad" else "k_contract_tiled + gather",
+             "contract": "k_contract_grad_warp" if inner == "grad" else "k_contract_tiled + gather",
              "scale": "k_scale_cs" if inner == "grad" else "k_scale_half"}.get(top, top)
+    traffic = measured_traffic(kname, n, w["Ngrid"])
     return {"bound": "hbm", "kernel": f"{kname} (fp32, 3 vectors)", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
             "algorithmic_bytes_per_launch": algo[top], "avg_launch_ms": avg_ms, "launches": cnt,
-            "traffic": None,
+            "traffic": traffic,
             "stage_ms_per_matvec_fp32": {k: v / cnt for k, v in ms.items()},
             "stage_ms_per_matvec_fp64": ({k: v / st["fp64"][0] for k, v in st["fp64"][1].items()}
                                          if st["fp64"][0] else None),
@@ -453,10 +469,16 @@ def run_quadrupole(args):
     b = torch.zeros((n, 8), dtype=torch.float64, device="cuda")
     b[:, :3] = torch.as_tensor(H0, device="cuda")
 
-    def step(precision, tol):
+    def step(precision, tol, stages=None):
         s = gq.QuadrupoleSystem(x, eps, box, xi, tol_sp, tables, rv, max_rhs=1)
+        if stages is not None:
+            s.profile(True)
         sol, info = s.solve(b, None, tol=tol, restart=30, maxit=args.maxref if precision == "mixed" else 200,
                             precision=precision, inner_tol=args.inner_tol, inner_maxit=args.inner_maxit)
+        if stages is not None:
+            for prec, (cnt, ms) in s.stage_times().items():
+                if cnt:
+                    stages[prec] = {k: v / cnt for k, v in ms.items()}
         s.close()
         return sol, info
 
@@ -475,6 +497,8 @@ def run_quadrupole(args):
     ms_m, sol_m, info_m = timed("mixed", args.tol, args.steps, args.warmup)
     ms_64, sol_64, info_64 = timed("fp64", args.tol, 1, 1)
     ref, _ = step("fp64", 1e-11)
+    stages = {}
+    step("mixed", args.tol, stages)       # one profiled step: per-matvec stage times (CUDA events)
     rel = lambda a: float(torch.linalg.vector_norm(a - ref) / torch.linalg.vector_norm(ref))
     S_ref = ref[:, :3].mean(dim=0)
     print(json.dumps({
@@ -487,6 +511,7 @@ def run_quadrupole(args):
         "mean_dipole_rel_error": float(torch.linalg.vector_norm(sol_m[:, :3].mean(dim=0) - S_ref)
                                        / torch.linalg.vector_norm(S_ref)),
         "mixed_matvecs": {"fp64": info_m[0].matvecs_fp64, "fp32": info_m[0].matvecs_fp32},
+        "stage_ms_per_matvec": stages,
         "tol": args.tol, "grid": [int(v) for v in np.ceil(1 + np.asarray(box) * 2 * xi * math.sqrt(-math.log(tol_sp))
                                                             / math.pi)]}), flush=True)
 

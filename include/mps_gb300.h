@@ -332,9 +332,11 @@ int mps_system_profile(mps_system *sys, int32_t enable);
  * Resets the accumulators. */
 int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count);
 
-/* Tile depth the autotuner chose for the tiled spread/contract: tile_depth[0]
- * float64, [1] float32 (0 = not used yet); ms[4] = timed candidates (depth 4,
- * depth 8) for float64 then float32, -1 where not timed. */
+/* Tile depth the autotuner chose for the tiled kernels: tile_depth[0] for the
+ * float64-width tiles (float64 or double-float spread, whichever ran first),
+ * [1] for the float32 tiles (gradient-form spread, or the reference-form spread
+ * + contract) (0 = not used yet); ms[4] = the timed candidates (depth 4, depth 8)
+ * of those kernels, float64-width then float32, -1 where not timed. */
 int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms);
 
 #ifdef __cplusplus

@@ -99,6 +99,53 @@ __device__ __forceinline__ int32_t nb_cell(int32_t c, int o, int64_t ncx, int64_
     return (int32_t)(cx + ncx * (cy + ncy * cz));
 }
 
+// Warp-per-particle walk over the candidates of the 27 neighbour cells in (cell
+// offset, position in the cell) order.  Lane o < 27 holds neighbour cell o's first
+// sorted position and the exclusive prefix of the cell counts; candidate j is
+// located by a binary search over those lanes.  One warp per particle keeps the
+// dependent loads (particle, cells, candidates) to a few per particle instead of a
+// few per (particle, cell).
+struct CellWalk {
+    int64_t cstart;   // lane o < 27: sorted position of neighbour cell o's first particle
+    int pre;          // lane o < 27: candidates in cells 0..o-1
+    int total;        // candidates of all 27 cells (warp-uniform)
+};
+
+__device__ __forceinline__ CellWalk cell_walk(int32_t c, int lane, const int32_t *__restrict__ counts,
+                                              const int64_t *__restrict__ starts, int64_t ncx, int64_t ncy,
+                                              int64_t ncz) {
+    CellWalk cw;
+    cw.cstart = 0;
+    int cnt = 0;
+    if (lane < 27) {
+        const int32_t nb = nb_cell(c, lane, ncx, ncy, ncz);
+        cw.cstart = starts[nb];
+        cnt = counts[nb];
+    }
+    int v = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += u;
+    }
+    cw.pre = v - cnt;
+    cw.total = __shfl_sync(0xffffffffu, v, 31);
+    return cw;
+}
+
+// Cell offset o and sorted position of candidate j (0 <= j < total); all lanes call it.
+__device__ __forceinline__ void walk_at(const CellWalk &cw, int j, int &o, int64_t &pos) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const int mid = lo + step;
+        const int p = __shfl_sync(0xffffffffu, cw.pre, mid < 27 ? mid : 26);
+        if (mid < 27 && p <= j) lo = mid;
+    }
+    o = lo;
+    pos = __shfl_sync(0xffffffffu, cw.cstart, lo) + (j - __shfl_sync(0xffffffffu, cw.pre, lo));
+}
+
 // Candidate counts in emission-slot order: slot(s,o) = 27*start[c] + o*count[c] + (s - start[c]).
 __global__ void k_candidate_slots(const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
                                   const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
@@ -351,20 +398,22 @@ __global__ void __launch_bounds__(256) k_csr_count(const double *__restrict__ x,
                                                    const int32_t *__restrict__ counts,
                                                    const int64_t *__restrict__ starts, int64_t n, int64_t ncx,
                                                    int64_t ncy, int64_t ncz, int64_t *__restrict__ cnt27) {
-    const int lane = threadIdx.x & 31;
+    __shared__ int hist[8][27];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
-        const int64_t s = t / 27;
-        const int o = (int)(t % 27);
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
         const int32_t a = sorted[s];
-        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
-        const int64_t b0 = starts[nb], len = counts[nb];
-        int64_t cnt = 0;
-        for (int64_t j0 = 0; j0 < len; j0 += 32) {
-            const int64_t j = j0 + lane;
+        const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
+        if (lane < 27) hist[wid][lane] = 0;
+        __syncwarp();
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
             bool keep = false;
-            if (j < len) {
-                const int32_t b = sorted[b0 + j];
+            if (j < cw.total) {
+                const int32_t b = sorted[pos];
                 if (b != a) {
                     const int sc = pair_screen(xf, a, b, ps);
                     if (sc == SCREEN_IN) {
@@ -375,9 +424,11 @@ __global__ void __launch_bounds__(256) k_csr_count(const double *__restrict__ x,
                     }
                 }
             }
-            cnt += __popc(__ballot_sync(0xffffffffu, keep));
+            if (keep) atomicAdd(&hist[wid][o], 1);
         }
-        if (lane == 0) cnt27[(int64_t)a * 27 + o] = cnt;
+        __syncwarp();
+        if (lane < 27) cnt27[(int64_t)a * 27 + lane] = hist[wid][lane];
+        __syncwarp();
     }
 }
 
@@ -406,20 +457,21 @@ __global__ void __launch_bounds__(256) k_csr_fill(const double *__restrict__ x, 
                                                   PairData<double> p64, PairData<float> p32, int *__restrict__ err) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
-        const int64_t s = t / 27;
-        const int o = (int)(t % 27);
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
         const int32_t a = sorted[s];
-        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
-        const int64_t b0 = starts[nb], len = counts[nb];
-        int64_t w = off27[(int64_t)a * 27 + o];
-        for (int64_t j0 = 0; j0 < len; j0 += 32) {
-            const int64_t j = j0 + lane;
+        const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
+        int64_t w = off27[(int64_t)a * 27];   // the row's pairs follow in (cell offset, position) order
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+            (void)o;
             bool keep = false;
             int32_t b = -1;
             double r[3] = {0, 0, 0}, s2 = 0.0;
-            if (j < len) {
-                b = sorted[b0 + j];
+            if (j < cw.total) {
+                b = sorted[pos];
                 const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
                 if (sc != SCREEN_OUT) {
                     bool big = false;
@@ -560,21 +612,22 @@ __global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ 
         L[k] = dfv(ps.L[k]);
         halfL[k] = dfv(0.5 * ps.L[k]);
     }
-    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < 27 * n; t += nw) {
-        const int64_t s = t / 27;
-        const int o = (int)(t % 27);
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
         const int32_t a = sorted[s];
-        const int32_t nb = nb_cell(lin[a], o, ncx, ncy, ncz);
-        const int64_t b0 = starts[nb], len = counts[nb];
-        int64_t w = off27[(int64_t)a * 27 + o];
-        for (int64_t j0 = 0; j0 < len; j0 += 32) {
-            const int64_t j = j0 + lane;
+        const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
+        int64_t w = off27[(int64_t)a * 27];   // the row's pairs follow in (cell offset, position) order
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+            (void)o;
             bool keep = false, exact = false;
             int32_t b = -1;
             dfv r[3];
             double r64[3] = {0, 0, 0};
-            if (j < len) {
-                b = sorted[b0 + j];
+            if (j < cw.total) {
+                b = sorted[pos];
                 const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
                 if (sc != SCREEN_OUT) {
                     bool big = false;
@@ -759,7 +812,7 @@ int positions_f32(const double *x, int64_t n, float *xf, unsigned *maxbits, doub
 int csr_pairs_count(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
                     int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *total_host, cudaStream_t s) {
     int64_t n = cb.n;
-    k_csr_count<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
+    k_csr_count<<<grid_for(n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
                                                       cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], cnt27);
     MPS_LAUNCH_CHECK();
     int r = exclusive_scan_i64(cnt27, off27, 27 * n, scan_tmp, s);
@@ -785,7 +838,7 @@ int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double
         MPS_CUDA_TRY(cudaStreamSynchronize(s));
     }
     const double inv_dr = rv_last > 0 ? (double)(ntab - 1) / rv_last : 0.0;
-    k_csr_fill<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
+    k_csr_fill<<<grid_for(n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
                                                      cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], off27,
                                                      perp, para, rv, ntab, inv_dr, p64, p32, err);
     MPS_LAUNCH_CHECK();
@@ -832,7 +885,7 @@ int csr_pairs_fill_df(const double *x, const float *xf, const float2 *xdf, doubl
     const int64_t n = cb.n;
     k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
     MPS_LAUNCH_CHECK();
-    k_csr_fill_df<<<grid_for(27 * n * 32, 256, 152 * 64), 256, 0, s>>>(
+    k_csr_fill_df<<<grid_for(n * 32, 256, 152 * 64), 256, 0, s>>>(
         x, xf, xdf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts, cb.starts, n, cb.ncell[0],
         cb.ncell[1], cb.ncell[2], off27, tab, pdf, p32, err);
     MPS_LAUNCH_CHECK();

@@ -23,7 +23,6 @@
 
 namespace mps {
 
-constexpr int kGChunk = 32;
 
 // g[a][d][j] = dw_d/dr at stencil node j of axis d (float32).
 __global__ void k_grad_factors(const double *__restrict__ x, int64_t n, GridParams gp, const double *__restrict__ w64,
@@ -63,6 +62,16 @@ __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, f
     }
 }
 
+// Owner-computes spread: thread (tx, ty) of the CTA owns the column (X0+tx,
+// Y0+ty, Z0..Z0+TZ-1) of the tile and accumulates it in registers over the
+// tile's particle list (fixed order: deterministic, no atomics).  Particles are
+// staged in chunks with their per-axis factors already aligned to the tile --
+// w and dw/dr at every tile column, row and plane, zero where the stencil does
+// not reach -- plus a mask of the tile rows they cover, so a warp (two rows)
+// skips a particle with one uniform test and otherwise runs a branch-free
+// update: value(x,y,z) = (mx gx wy + my wx gy) wz + mz wx wy gz.
+constexpr int kGChunk = 32;
+
 template <int TZ, int NR>
 __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
                                                            const int32_t *__restrict__ start,
@@ -70,14 +79,15 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
                                                            GridParams gp, const int64_t *__restrict__ tstart,
                                                            const int32_t *__restrict__ entries, int ntx, int nty,
                                                            float *__restrict__ grid) {
-    __shared__ int3 s_off[kGChunk];
-    __shared__ float s_w[kGChunk][3 * kMaxP];
-    __shared__ float s_g[kGChunk][3 * kMaxP];
-    __shared__ float s_m[kGChunk][3 * NR];
+    constexpr int kPos = kTileX + kTileY + TZ;   // aligned positions per particle
+    constexpr int kMS = (3 * NR + 3) & ~3;       // moments, padded to a float4 multiple
+    __shared__ float2 s_f[kGChunk][kPos];        // (w, dw/dr) at tile columns, rows, planes
+    __shared__ __align__(16) float s_m[kGChunk][kMS];
+    __shared__ unsigned s_rows[kGChunk];
     const int64_t t = blockIdx.x;
     const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
     const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
-    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4, wid = threadIdx.x >> 5;
     const int P = gp.P;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     float acc[TZ][NR];
@@ -88,13 +98,9 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     const int64_t e0 = tstart[t], e1 = tstart[t + 1];
     for (int64_t cb = e0; cb < e1; cb += kGChunk) {
         const int cnt = (int)min((int64_t)kGChunk, e1 - cb);
+        if (threadIdx.x < kGChunk) s_rows[threadIdx.x] = 0u;
         if (threadIdx.x < cnt) {
             const int32_t a = entries[cb + threadIdx.x];
-            int ox = X0 - start[3 * a], oy = Y0 - start[3 * a + 1], oz = Z0 - start[3 * a + 2];
-            if (ox < 0) ox += Nx;
-            if (oy < 0) oy += Ny;
-            if (oz < 0) oz += Nz;
-            s_off[threadIdx.x] = make_int3(ox, oy, oz);
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
                 const double *ma = m + ((int64_t)(r0 + r) * n + a) * 3;
@@ -103,40 +109,41 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
                 s_m[threadIdx.x][3 * r + 2] = (float)ma[2];
             }
         }
-        for (int q = threadIdx.x; q < cnt * 3 * P; q += blockDim.x) {
-            const int pp = q / (3 * P), k = q % (3 * P);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt * kPos; q += blockDim.x) {
+            const int pp = q / kPos, k = q - (q / kPos) * kPos;
             const int32_t a = entries[cb + pp];
-            s_w[pp][(k / P) * kMaxP + (k % P)] = w[(int64_t)a * 3 * P + k];
-            s_g[pp][(k / P) * kMaxP + (k % P)] = g[(int64_t)a * 3 * P + k];
+            const int d = k < kTileX ? 0 : (k < kTileX + kTileY ? 1 : 2);
+            const int tpos = k - (d == 0 ? 0 : (d == 1 ? kTileX : kTileX + kTileY));
+            const int origin = d == 0 ? X0 : (d == 1 ? Y0 : Z0);
+            const int Nd = d == 0 ? Nx : (d == 1 ? Ny : Nz);
+            const int node = origin + tpos;
+            int j = node - start[3 * (int64_t)a + d];   // stencil index of this tile position
+            if (j < 0) j += Nd;
+            float2 f = make_float2(0.f, 0.f);
+            if (node < Nd && j < P) {
+                const int64_t o = (int64_t)a * 3 * P + d * P + j;
+                f = make_float2(w[o], g[o]);
+                if (d == 1) atomicOr(&s_rows[pp], 1u << tpos);
+            }
+            s_f[pp][k] = f;
         }
         __syncthreads();
         for (int pp = 0; pp < cnt; ++pp) {
-            const int3 o = s_off[pp];
-            int dx = o.x + tx;
-            if (dx >= Nx) dx -= Nx;
-            int dy = o.y + ty;
-            if (dy >= Ny) dy -= Ny;
-            if (dx < P && dy < P) {
-                const float wx = s_w[pp][dx], wy = s_w[pp][kMaxP + dy];
-                const float gx = s_g[pp][dx], gy = s_g[pp][kMaxP + dy];
-                const float wxy = wx * wy;
-                float cA[NR], cB[NR];
+            if (((s_rows[pp] >> (2 * wid)) & 3u) == 0u) continue;   // neither row of this warp is covered
+            const float2 fx = s_f[pp][tx], fy = s_f[pp][kTileX + ty];
+            const float gxwy = fx.y * fy.x, wxgy = fx.x * fy.y, wxwy = fx.x * fy.x;
+            float cA[NR], cB[NR];
 #pragma unroll
-                for (int r = 0; r < NR; ++r) {
-                    // column parts: (m_x gx wy + m_y wx gy) multiplies w_z, m_z wx wy multiplies g_z
-                    cA[r] = s_m[pp][3 * r] * gx * wy + s_m[pp][3 * r + 1] * wx * gy;
-                    cB[r] = s_m[pp][3 * r + 2] * wxy;
-                }
+            for (int r = 0; r < NR; ++r) {
+                cA[r] = s_m[pp][3 * r] * gxwy + s_m[pp][3 * r + 1] * wxgy;
+                cB[r] = s_m[pp][3 * r + 2] * wxwy;
+            }
 #pragma unroll
-                for (int z = 0; z < TZ; ++z) {
-                    int dz = o.z + z;
-                    if (dz >= Nz) dz -= Nz;
-                    if (dz < P) {
-                        const float wz = s_w[pp][2 * kMaxP + dz], gz = s_g[pp][2 * kMaxP + dz];
+            for (int z = 0; z < TZ; ++z) {
+                const float2 fz = s_f[pp][kTileX + kTileY + z];
 #pragma unroll
-                        for (int r = 0; r < NR; ++r) acc[z][r] += cA[r] * wz + cB[r] * gz;
-                    }
-                }
+                for (int r = 0; r < NR; ++r) acc[z][r] += cA[r] * fz.x + cB[r] * fz.y;
             }
         }
         __syncthreads();
@@ -156,171 +163,6 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     }
 }
 
-// Spread of the gradient form by scatter into private tile copies.  The CTA owns
-// a 16 x 16 x TZ tile; the tile's particle list (fixed order) is dealt to the NW
-// warps round-robin; each warp adds its particles' overlap with the tile into its
-// own copy of the tile in shared memory (lanes over the overlap's (x, y) columns,
-// the z range inside), so no two lanes or warps ever update one word at once.  The
-// copies are then summed in warp order: deterministic, no atomics, and every lane
-// slot works on a node of the stencil (the owner-computes kernel above visits the
-// whole tile for every particle).  Needs N >= tile + P on every axis, so that a
-// stencil's overlap with a tile is one interval (otherwise the kernel above runs).
-constexpr int kSRow = kTileX + 1;
-
-template <int TZ, int NR>
-struct ScatterShape {
-    // plane stride = 24 mod 32 words: lanes on planes z..z+3 of one row start 8 banks apart
-    static constexpr int kPlane = kTileY * kSRow + 8;
-    static constexpr int kCopy = NR * TZ * kPlane;       // one tile copy (floats)
-    static constexpr int kStage = 2 * 3 * kMaxP + 4 * NR;  // w, g of the 3 axes + moments (padded)
-    static constexpr int kWarps = TZ >= 8 ? 4 : 8;
-    static constexpr size_t kSmem = sizeof(float) * (size_t)kWarps * (kCopy + kStage);
-};
-
-// Interval of tile-local coordinates [lo, lo + cnt) covered by a stencil whose
-// first node is s, and the stencil index of its first covered node.
-__device__ __forceinline__ void tile_interval(int s, int T0, int Tn, int P, int N, int &lo, int &cnt, int &j0) {
-    int o = T0 - s;   // stencil index of tile node 0
-    if (o < 0) o += N;
-    if (o < P) {
-        lo = 0;
-        j0 = o;
-    } else {
-        lo = N - o;
-        j0 = 0;
-    }
-    cnt = min(lo + (P - j0), Tn) - lo;
-}
-
-template <int TZ, int NR>
-__global__ void __launch_bounds__(ScatterShape<TZ, NR>::kWarps * 32)
-    k_spread_grad_scatter(const double *__restrict__ m, int64_t n, int r0, const int32_t *__restrict__ start,
-                          const float *__restrict__ w, const float *__restrict__ g, GridParams gp,
-                          const int64_t *__restrict__ tstart, const int32_t *__restrict__ entries, int ntx, int nty,
-                          float *__restrict__ grid) {
-    using S = ScatterShape<TZ, NR>;
-    constexpr int NW = S::kWarps;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *copies = (float *)smem_raw;                 // [NW][NR][TZ][16][kSRow]
-    float *stage = copies + NW * S::kCopy;             // [NW][kStage]
-    const int64_t t = blockIdx.x;
-    const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
-    const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
-    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
-    const int Tx = min(kTileX, Nx - X0), Ty = min(kTileY, Ny - Y0), Tz = min(TZ, Nz - Z0);
-    const int P = gp.P;
-    const int64_t G = gp.G;
-    const int64_t e0 = tstart[t], e1 = tstart[t + 1];
-    if (e0 == e1) {
-        for (int idx = threadIdx.x; idx < NR * TZ * kTileX * kTileY; idx += NW * 32) {
-            const int x = idx & (kTileX - 1), y = (idx >> 4) & (kTileY - 1), zr = idx >> 8;
-            const int z = zr % TZ, r = zr / TZ;
-            if (x < Tx && y < Ty && z < Tz)
-                grid[(int64_t)(r0 + r) * G + ((int64_t)(Z0 + z) * Ny + (Y0 + y)) * Nx + (X0 + x)] = 0.f;
-        }
-        return;
-    }
-    for (int i = threadIdx.x; i < NW * S::kCopy / 4; i += NW * 32)
-        reinterpret_cast<float4 *>(copies)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float *acc = copies + wid * S::kCopy;
-    float *wb = stage + wid * S::kStage;   // w of the 3 axes, flat (axis * P + j)
-    float *gb = wb + 3 * kMaxP;
-    // Software pipeline over this warp's particles: entry ids two visits ahead,
-    // the particle's factors, moments and stencil start one visit ahead, so the
-    // global loads overlap the previous particle's scatter.
-    const unsigned FULL = 0xffffffffu;
-    auto entry_at = [&](int64_t e) -> int32_t { return e < e1 ? entries[e] : -1; };
-    float pw0 = 0.f, pw1 = 0.f, pg0 = 0.f, pg1 = 0.f, pm = 0.f;
-    int ps = 0;
-    auto fetch = [&](int32_t a) {
-        if (a < 0) return;
-        const int64_t b = (int64_t)a * 3 * P;
-        if (lane < 3 * P) {
-            pw0 = w[b + lane];
-            pg0 = g[b + lane];
-        }
-        if (lane + 32 < 3 * P) {
-            pw1 = w[b + lane + 32];
-            pg1 = g[b + lane + 32];
-        }
-        if (lane < 3 * NR) pm = (float)m[((int64_t)(r0 + lane / 3) * n + a) * 3 + lane % 3];
-        if (lane < 3) ps = start[3 * (int64_t)a + lane];
-    };
-    int64_t e = e0 + wid;
-    fetch(entry_at(e));
-    int32_t a_next = entry_at(e + NW);
-    for (; e < e1; e += NW) {
-        // commit the prefetched particle
-        if (lane < 3 * P) {
-            wb[lane] = pw0;
-            gb[lane] = pg0;
-        }
-        if (lane + 32 < 3 * P) {
-            wb[lane + 32] = pw1;
-            gb[lane + 32] = pg1;
-        }
-        float mr[3 * NR];
-#pragma unroll
-        for (int c = 0; c < 3 * NR; ++c) mr[c] = __shfl_sync(FULL, pm, c);
-        const int sx = __shfl_sync(FULL, ps, 0), sy = __shfl_sync(FULL, ps, 1), sz = __shfl_sync(FULL, ps, 2);
-        // prefetch the next particle, and the entry id after it
-        fetch(a_next);
-        a_next = entry_at(e + 2 * NW);
-        int xlo, nx, jx0, ylo, ny, jy0, zlo, nz, jz0;
-        tile_interval(sx, X0, Tx, P, Nx, xlo, nx, jx0);
-        tile_interval(sy, Y0, Ty, P, Ny, ylo, ny, jy0);
-        tile_interval(sz, Z0, Tz, P, Nz, zlo, nz, jz0);
-        __syncwarp();
-        if (nx > 0 && ny > 0 && nz > 0) {
-            // lanes over the overlap's (x, z) columns, the y range inside:
-            // value = wy (mx gx wz + mz wx gz) + gy (my wx wz)
-            const float rnx = __frcp_rn((float)nx);
-            const int ncol = nx * nz;
-            for (int q = lane; q < ncol; q += 32) {
-                const int jz = __float2int_rz(((float)q + 0.5f) * rnx);
-                const int jx = q - jz * nx;
-                const float wx = wb[jx0 + jx], gx = gb[jx0 + jx];
-                const float wz = wb[2 * P + jz0 + jz], gz = gb[2 * P + jz0 + jz];
-                const float gxwz = gx * wz, wxgz = wx * gz, wxwz = wx * wz;
-                float al[NR], be[NR];
-#pragma unroll
-                for (int r = 0; r < NR; ++r) {
-                    al[r] = mr[3 * r] * gxwz + mr[3 * r + 2] * wxgz;
-                    be[r] = mr[3 * r + 1] * wxwz;
-                }
-                float *col = acc + (zlo + jz) * S::kPlane + ylo * kSRow + (xlo + jx);
-                const float *wyp = wb + P + jy0, *gyp = gb + P + jy0;
-                for (int jy = 0; jy < ny; ++jy) {
-                    const float wy = wyp[jy], gy = gyp[jy];
-#pragma unroll
-                    for (int r = 0; r < NR; ++r) {
-                        float *pr = col + jy * kSRow + r * TZ * S::kPlane;
-                        *pr += wy * al[r] + gy * be[r];
-                    }
-                }
-            }
-        }
-        __syncwarp();
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < NR * TZ * kTileX * kTileY; idx += NW * 32) {
-        const int x = idx & (kTileX - 1), y = (idx >> 4) & (kTileY - 1), zr = idx >> 8;
-        const int z = zr % TZ, r = zr / TZ;
-        if (x < Tx && y < Ty && z < Tz) {
-            const int off = (r * TZ + z) * S::kPlane + y * kSRow + x;
-            float v = copies[off];
-#pragma unroll
-            for (int q = 1; q < NW; ++q) v += copies[q * S::kCopy + off];
-            grid[(int64_t)(r0 + r) * G + ((int64_t)(Z0 + z) * Ny + (Y0 + y)) * Nx + (X0 + x)] = v;
-        }
-    }
-}
-
-bool scatter_supported(const GridParams &gp, int tz) {
-    return gp.N[0] >= kTileX + gp.P && gp.N[1] >= kTileY + gp.P && gp.N[2] >= tz + gp.P;
-}
 
 constexpr int kGRowPad = kTileX + 1;
 
@@ -547,20 +389,8 @@ static int grad_launch(const double *m, int64_t n, int r0, const int32_t *start,
                        const GridParams &gp, const TileBins &tb, float *grid, float *partial, double *out,
                        bool spread_phase, cudaStream_t s) {
     if (spread_phase) {
-        // MPS_GRAD_SPREAD=scatter selects the private-copy scatter (A/B timing; it is
-        // limited by shared-memory occupancy and measured no faster than the tiled one)
-        const char *e = getenv("MPS_GRAD_SPREAD");
-        if (scatter_supported(gp, TZ) && e && strcmp(e, "scatter") == 0) {
-            using S = ScatterShape<TZ, NR>;
-            if (S::kSmem > 48 * 1024)
-                MPS_CUDA_TRY(cudaFuncSetAttribute(k_spread_grad_scatter<TZ, NR>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::kSmem));
-            k_spread_grad_scatter<TZ, NR><<<(unsigned)tb.ntiles, S::kWarps * 32, S::kSmem, s>>>(
-                m, n, r0, start, w, g, gp, tb.tile_start, tb.entries, tb.ntx, tb.nty, grid);
-        } else {
-            k_spread_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start,
-                                                                             tb.entries, tb.ntx, tb.nty, grid);
-        }
+        k_spread_grad_tiled<TZ, NR><<<(unsigned)tb.ntiles, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start,
+                                                                         tb.entries, tb.ntx, tb.nty, grid);
         MPS_LAUNCH_CHECK();
         return MPS_OK;
     }

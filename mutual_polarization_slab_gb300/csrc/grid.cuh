@@ -15,6 +15,9 @@ struct GridParams {
     double xi;
     double wconst;     // (2 xi^2/pi)^{3/2} / sqrt(prod eta)
     double hprod;      // trapezoid factor of the contraction
+    // optional visiting order of the particles (ids sorted by cell, n entries):
+    // per-particle gather kernels read overlapping stencils from neighbouring warps
+    const int32_t *order = nullptr;
 };
 
 GridParams make_grid_params(const int64_t *Ngrid, const double *box, double xi, const double *eta, int P);

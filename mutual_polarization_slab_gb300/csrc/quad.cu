@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) k_spread_gen(const double *__restrict__ m
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t G = gp.G;
     for (int64_t t = warp; t < n * nrhs; t += nw) {
-        const int64_t a = t % n;
+        const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
         const int r = (int)(t / n);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
         const T *wa = w + a * 3 * P;
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) k_contract_gen(const T *__restrict__ grid
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t G = gp.G;
     for (int64_t t = warp; t < n * nrhs; t += nw) {
-        const int64_t a = t % n;
+        const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
         const int r = (int)(t / n);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
         const T *wa = w + a * 3 * P;

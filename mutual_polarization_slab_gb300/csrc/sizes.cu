@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m,
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t P3 = (int64_t)P * P * P;
     for (int64_t t = warp; t < n * nrhs; t += nw) {
-        const int64_t a = t % n;
+        const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
         const int r = (int)(t / n);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
         const double *ma = m + ((int64_t)r * n + a) * 3;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid,
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t P3 = (int64_t)P * P * P;
     for (int64_t t = warp; t < n * nrhs; t += nw) {
-        const int64_t a = t % n;
+        const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
         const int r = (int)(t / n);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
         const T bx = (T)(base[3 * a] - lo * gp.h[0]), by = (T)(base[3 * a + 1] - lo * gp.h[1]),

@@ -111,6 +111,7 @@ struct mps_system {
     float *cs_h32 = nullptr;
     int32_t *start = nullptr;
     int32_t *order = nullptr;        // particle ids sorted by (cell, id): spatial visiting order
+    dfv *wdf = nullptr;              // double-float copy of w64 (built by the first double-float matvec)
     double *w64 = nullptr;
     float *w32 = nullptr;
     double *h64 = nullptr;       // owned by green (shared, cached per grid)
@@ -129,6 +130,7 @@ struct mps_system {
     size_t fft_work_bytes = 0;
     TileBins tb64, tb32;        // tile binning for the tiled spread/contract (per precision tile depth)
     double *partial64 = nullptr;
+    int tb_use[2] = {-1, -1};         // tuner consumer that built tb64 / tb32
     float *partial32 = nullptr;
     bool tiled = true;
     bool profile = false;
@@ -154,7 +156,7 @@ static void free_system(mps_system *s) {
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
                     s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->g32, s->pdf.A, s->pdf.BA,
-                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order};
+                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order, s->wdf};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -320,34 +322,34 @@ static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStrea
         if (ev) MPS_CUDA_TRY(cudaEventRecord(ev->ev[(k)], st));         \
     } while (0)
 
-// Tile depth per precision: float64 accumulators take twice the registers.
-// Autotuner for the tiled spread/contract: the tile depth (z) is timed on the
-// first system of each (grid, support, precision, batch width) and the fastest
-// is kept for the rest of the process.
+// Autotuner for the tiled kernels: the tile depth (z) is timed on the first
+// system of each (grid, support, consumer, batch width) with the kernels that
+// consumer runs, and the fastest is kept for the rest of the process.  The
+// consumers: the float32 reference operator (tiled spread + contract), the
+// float32 gradient operator (its spread), the float64 operator (spread) and the
+// double-float operator (spread); the float32 ones share tb32, the others tb64.
+enum TileUse { kTileRef32 = 0, kTileGrad32 = 1, kTileF64 = 2, kTileDF = 3 };
 struct TuneKey {
     int N[3];
     int P;
-    int dbl;
+    int use;
     int nrhs;
     bool operator<(const TuneKey &o) const { return memcmp(this, &o, sizeof(TuneKey)) < 0; }
 };
 struct TuneResult {
     int tz;
-    float ms[2];   // timings of depth 4 and 8 (spread + contract), -1 if not run
+    float ms[2];   // timings of depth 4 and 8, -1 if not run
 };
 static std::map<TuneKey, TuneResult> g_tune;
 static std::mutex g_tune_mu;
 static const int kDepths[2] = {4, 8};
 
-template <typename T>
-static int time_tiles(mps_system *s, int tz, int nrhs, const double *m, double *out, T *grid, cudaStream_t st,
+static int time_tiles(mps_system *s, int use, int tz, int nrhs, const double *m, double *out, cudaStream_t st,
                       float *ms) {
     TileBins tb;
     MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
-    T *partial = nullptr;
-    const bool dbl = sizeof(T) == 8;
-    if (!dbl) MPS_TRY(dalloc(&partial, (size_t)tb.nentries * 9 * sizeof(T), st));
-    const T *w = dbl ? (const T *)s->w64 : (const T *)s->w32;
+    float *partial = nullptr;
+    if (use == kTileRef32) MPS_TRY(dalloc(&partial, (size_t)tb.nentries * 9 * sizeof(float), st));
     cudaEvent_t e0, e1;
     MPS_CUDA_TRY(cudaEventCreate(&e0));
     MPS_CUDA_TRY(cudaEventCreate(&e1));
@@ -355,8 +357,22 @@ static int time_tiles(mps_system *s, int tz, int nrhs, const double *m, double *
     int rc = MPS_OK;
     for (int rep = 0; rep < 4 && rc == MPS_OK; ++rep) {
         cudaEventRecord(e0, st);
-        rc = spread_tiled<T>(m, s->n, nrhs, s->start, w, s->gp, tb, grid, st);
-        if (rc == MPS_OK && !dbl) rc = contract_tiled<T>(grid, s->n, nrhs, s->start, w, s->gp, tb, partial, out, st);
+        switch (use) {
+            case kTileRef32:
+                rc = spread_tiled<float>(m, s->n, nrhs, s->start, s->w32, s->gp, tb, s->grid32, st);
+                if (rc == MPS_OK)
+                    rc = contract_tiled<float>(s->grid32, s->n, nrhs, s->start, s->w32, s->gp, tb, partial, out, st);
+                break;
+            case kTileGrad32:
+                rc = spread_grad_tiled(m, s->n, nrhs, s->start, s->w32, s->g32, s->gp, tb, s->grid32, st);
+                break;
+            case kTileF64:
+                rc = spread_tiled<double>(m, s->n, nrhs, s->start, s->w64, s->gp, tb, s->grid64, st);
+                break;
+            default:
+                rc = spread_tiled_df(m, s->n, nrhs, s->start, s->wdf, s->gp, tb, (dfv *)s->grid64, st);
+                break;
+        }
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
         float t = 0.f;
@@ -371,12 +387,12 @@ static int time_tiles(mps_system *s, int tz, int nrhs, const double *m, double *
     return rc;
 }
 
-static int tuned_depth(mps_system *s, bool dbl, cudaStream_t st, int *tz) {
+static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     TuneKey key;
     memset(&key, 0, sizeof(key));
     for (int k = 0; k < 3; ++k) key.N[k] = s->gp.N[k];
     key.P = s->gp.P;
-    key.dbl = dbl ? 1 : 0;
+    key.use = use;
     key.nrhs = s->max_rhs < 3 ? s->max_rhs : 3;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -403,8 +419,7 @@ static int tuned_depth(mps_system *s, bool dbl, cudaStream_t st, int *tz) {
     for (int i = 0; i < 2; ++i) {
         if (!tiles_supported(s->gp, kDepths[i])) continue;
         float ms = 0.f;
-        int rc = dbl ? time_tiles<double>(s, kDepths[i], nrhs, m, out, (double *)s->grid64, st, &ms)
-                     : time_tiles<float>(s, kDepths[i], nrhs, m, out, (float *)s->grid32, st, &ms);
+        int rc = time_tiles(s, use, kDepths[i], nrhs, m, out, st, &ms);
         if (rc != MPS_OK) {
             cudaFreeAsync(m, st);
             cudaFreeAsync(out, st);
@@ -427,24 +442,27 @@ static int tuned_depth(mps_system *s, bool dbl, cudaStream_t st, int *tz) {
 }
 
 // Lazily bins the particles for the tiled kernels of one precision (tile depth
-// from the autotuner).
-static int ensure_tiles(mps_system *s, bool dbl, cudaStream_t st, bool *use) {
-    *use = false;
+// from the autotuner, timed for the consumer that asks first).
+static int ensure_tiles(mps_system *s, int use, cudaStream_t st, bool *used) {
+    *used = false;
     // the tiled kernels use the separable Gaussian weights of the dipole operator
     if (!s->tiled || s->kind != MPS_DIPOLE || !s->w32 || !s->w64) return MPS_OK;
+    const bool dbl = use == kTileF64 || use == kTileDF;
     TileBins &tb = dbl ? s->tb64 : s->tb32;
     if (!tb.mem) {
         MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
         int tz = 0;
-        MPS_TRY(tuned_depth(s, dbl, st, &tz));
+        MPS_TRY(tuned_depth(s, use, st, &tz));
         if (tz == 0 || !tiles_supported(s->gp, tz)) {
             s->tiled = false;
             return MPS_OK;
         }
         MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
-        if (!dbl) MPS_TRY(dalloc(&s->partial32, (size_t)tb.nentries * 9 * sizeof(float), st));
+        s->tb_use[dbl ? 0 : 1] = use;
     }
-    *use = true;
+    if (!dbl && !s->partial32 && use == kTileRef32)
+        MPS_TRY(dalloc(&s->partial32, (size_t)tb.nentries * 9 * sizeof(float), st));
+    *used = true;
     return MPS_OK;
 }
 
@@ -477,7 +495,7 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     const bool dbl = sizeof(T) == 8;
     const bool own_fft = !dbl && own_fft32() && df_usable(s);
     bool use_tiles = false;
-    MPS_TRY(ensure_tiles(s, dbl, st, &use_tiles));
+    MPS_TRY(ensure_tiles(s, dbl ? kTileF64 : kTileRef32, st, &use_tiles));
     const TileBins &tb = dbl ? s->tb64 : s->tb32;
     T *partial = dbl ? (T *)s->partial64 : (T *)s->partial32;
     MPS_TRY(ensure_grids(s, dbl ? MPS_FP64 : MPS_FP32, st));
@@ -532,11 +550,14 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
 // weights and grids), the FFTs and Green's scale are the double-float transforms
 // of dffft.cu; the pair sum is the float64 kernel.
 static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    const int64_t nw = (int64_t)s->n * 3 * s->gp.P;
+    if (!s->wdf) {
+        MPS_TRY(dalloc(&s->wdf, sizeof(dfv) * (size_t)nw, st));
+        MPS_TRY(weights_df(s->w64, nw, s->wdf, st));
+    }
     bool use_tiles = false;
-    MPS_TRY(ensure_tiles(s, true, st, &use_tiles));
+    MPS_TRY(ensure_tiles(s, kTileDF, st, &use_tiles));
     MPS_TRY(ensure_grids(s, MPS_FP64, st));
-    if (use_tiles && !s->partial64)
-        MPS_TRY(dalloc(&s->partial64, (size_t)s->tb64.nentries * 9 * sizeof(double), st));
     {
         std::lock_guard<std::mutex> lk(g_green_mu);
         if (!s->green->tm6) {
@@ -555,7 +576,7 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(1);
     const int64_t gvals = (int64_t)3 * nrhs * s->gp.G;
     if (use_tiles) {
-        MPS_TRY(spread_tiled_df(m, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, grid, st));
+        MPS_TRY(spread_tiled_df(m, s->n, nrhs, s->start, s->wdf, s->gp, s->tb64, grid, st));
     } else {
         MPS_TRY(spread<double>(m, s->n, nrhs, s->start, s->w64, s->gp, s->grid64, st));
         MPS_TRY(f64_to_dfv_inplace(s->grid64, gvals, st));
@@ -567,7 +588,12 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(4);
     MPS_TRY(df_inverse_yx(spec, (float2 *)grid, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(5);
-    if (use_tiles) {
+    const char *ce = getenv("MPS_DF_CONTRACT");   // "tiled": the tiled contraction (A/B timing)
+    const bool tiled_contract = use_tiles && ce && strcmp(ce, "tiled") == 0;
+    if (s->gp.P <= kMaxP && !tiled_contract) {
+        MPS_TRY(contract_df_warp(grid, s->n, nrhs, s->order, s->start, s->wdf, s->gp, out, st));
+    } else if (use_tiles) {
+        if (!s->partial64) MPS_TRY(dalloc(&s->partial64, (size_t)s->tb64.nentries * 9 * sizeof(double), st));
         MPS_TRY(contract_tiled_df(grid, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, s->partial64, out, st));
     } else {
         MPS_TRY(dfv_to_f64_inplace(s->grid64, gvals, st));
@@ -659,14 +685,14 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     // the gradient form exists for the dipole operator only: the others run their own float32 operator
     if (s->kind == MPS_DIPOLE_QUADRUPOLE) return matvec_quad<float>(s, m, out, nrhs, st);
     if (s->kind == MPS_POLYDISPERSE) return matvec_cs<float>(s, m, out, nrhs, st);
-    bool use_tiles = false;
-    MPS_TRY(ensure_tiles(s, false, st, &use_tiles));
-    if (!use_tiles) return matvec_impl<float>(s, m, out, nrhs, st);
-    MPS_TRY(ensure_grids(s, MPS_FP32, st));
-    if (!s->g32) {
+    if (!s->g32 && s->w64) {
         MPS_TRY(dalloc(&s->g32, sizeof(float) * 3 * s->n * s->gp.P, st));
         MPS_TRY(grad_factors(s->x, s->n, s->gp, s->w64, s->g32, st));
     }
+    bool use_tiles = false;
+    MPS_TRY(ensure_tiles(s, kTileGrad32, st, &use_tiles));
+    if (!use_tiles) return matvec_impl<float>(s, m, out, nrhs, st);
+    MPS_TRY(ensure_grids(s, MPS_FP32, st));
     {
         std::lock_guard<std::mutex> lk(g_green_mu);
         if (!s->green->hs32) {
@@ -692,11 +718,14 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     {
         // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing); default: warp gather
         const char *e = getenv("MPS_GRAD_CONTRACT");
-        if (e && strcmp(e, "tiled") == 0)
+        if (e && strcmp(e, "tiled") == 0) {
+            if (!s->partial32)
+                MPS_TRY(dalloc(&s->partial32, (size_t)s->tb32.nentries * 9 * sizeof(float), st));
             MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->partial32,
                                         out, st));
-        else
+        } else {
             MPS_TRY(contract_grad_warp(s->grid32, s->n, nrhs, s->order, s->start, s->w32, s->g32, s->gp, out, st));
+        }
     }
     STAGE_MARK(6);
     MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
@@ -1480,6 +1509,7 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (!rc && n > 0 && cudaMemcpyAsync(s->order, cb.sorted, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st) !=
                             cudaSuccess)
         rc = MPS_CUDA_ERR;
+    if (!rc) s->gp.order = s->order;
     int64_t np = 0;
     if (!rc) rc = positions_f32(s->x, n, xf, maxbits, &maxabs, st);
     if (!rc) rc = csr_pairs_count(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);
@@ -1759,7 +1789,7 @@ extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, flo
         memset(&key, 0, sizeof(key));
         for (int k = 0; k < 3; ++k) key.N[k] = sys->gp.N[k];
         key.P = sys->gp.P;
-        key.dbl = p == 0 ? 1 : 0;
+        key.use = sys->tb_use[p];
         key.nrhs = sys->max_rhs < 3 ? sys->max_rhs : 3;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);

@@ -220,11 +220,11 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
     const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
     const int P = gp.P;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
-    T acc[TZ][C];
+    ProdAcc<T> acc[TZ][C];
 #pragma unroll
     for (int z = 0; z < TZ; ++z)
 #pragma unroll
-        for (int c = 0; c < C; ++c) acc[z][c] = (T)0;
+        for (int c = 0; c < C; ++c) acc[z][c].zero();
     const int64_t e0 = tstart[t], e1 = tstart[t + 1];
     for (int64_t cb = e0; cb < e1; cb += kChunk) {
         const int cnt = (int)min((int64_t)kChunk, e1 - cb);
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
                     if (dz < P) {
                         const T wv = wxy * s_w[pp][2 * kMaxP + dz];
 #pragma unroll
-                        for (int c = 0; c < C; ++c) acc[z][c] += wv * mv[c];
+                        for (int c = 0; c < C; ++c) acc[z][c].add(wv, mv[c]);
                     }
                 }
             }
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
             if (gz < Nz) {
                 const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
 #pragma unroll
-                for (int c = 0; c < C; ++c) grid[(int64_t)(3 * r0 + c) * G + node] = (TG)acc[z][c];
+                for (int c = 0; c < C; ++c) grid[(int64_t)(3 * r0 + c) * G + node] = (TG)acc[z][c].get();
             }
         }
     }
@@ -431,10 +431,10 @@ int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, con
     return MPS_BAD_ARG;
 }
 
-int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
+int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const dfv *w, const GridParams &gp,
                     const TileBins &tb, dfv *grid, cudaStream_t s) {
-    if (tb.tz == 8) return spread_dispatch<dfv, 8, double, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
-    if (tb.tz == 4) return spread_dispatch<dfv, 4, double, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 8) return spread_dispatch<dfv, 8, dfv, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
+    if (tb.tz == 4) return spread_dispatch<dfv, 4, dfv, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
     return MPS_BAD_ARG;
 }
 
@@ -485,6 +485,96 @@ int contract_tiled_df(const dfv *grid, int64_t n, int nrhs, const int32_t *start
     if (tb.tz == 4)
         return contract_dispatch<dfv, 4, dfv, double, double>(grid, n, nrhs, start, w, gp, tb, partial, out, s);
     return MPS_BAD_ARG;
+}
+
+// Contraction of double-float grids, one warp per particle, particles visited in
+// `order` (cell order: the warps of a CTA read overlapping stencils).  Lanes take
+// the stencil's (x, y) columns; each column's z sum over the 3*NR grids runs in
+// a ProdAcc<dfv> (exact leading products, two-sum, unnormalised within the
+// column), then the column sums are weighted by wx*wy in double-float.  Fixed
+// summation order: deterministic.
+template <int NR>
+__global__ void __launch_bounds__(256) k_contract_df_warp(const dfv *__restrict__ grid, int64_t n, int r0,
+                                                          const int32_t *__restrict__ order,
+                                                          const int32_t *__restrict__ start,
+                                                          const dfv *__restrict__ w, GridParams gp,
+                                                          double *__restrict__ out) {
+    constexpr int C = 3 * NR;
+    __shared__ dfv s_w[8][3 * kMaxP];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int P = gp.P;
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int64_t G = gp.G;
+    const int64_t NxNy = (int64_t)Nx * Ny;
+    dfv *wb = s_w[wid];
+    for (int64_t i = warp; i < n; i += nw) {
+        const int64_t a = order ? order[i] : i;
+        const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
+        __syncwarp();
+        for (int k = lane; k < 3 * P; k += 32) wb[k] = w[a * 3 * P + k];
+        __syncwarp();
+        dfv acc[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = dfv(0.f, 0.f);
+        for (int idx = lane; idx < P * P; idx += 32) {
+            const int jx = idx % P, jy = idx / P;
+            int ix = sx + jx;
+            if (ix >= Nx) ix -= Nx;
+            int iy = sy + jy;
+            if (iy >= Ny) iy -= Ny;
+            const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
+            ProdAcc<dfv> col[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) col[c].zero();
+#pragma unroll 2
+            for (int jz = 0; jz < P; ++jz) {
+                int iz = sz + jz;
+                if (iz >= Nz) iz -= Nz;
+                const int64_t node = rowb + NxNy * iz;
+                const dfv wz = wb[2 * P + jz];
+#pragma unroll
+                for (int c = 0; c < C; ++c) col[c].add(wz, grid[(int64_t)(3 * r0 + c) * G + node]);
+            }
+            const dfv wxy = wb[jx] * wb[P + jy];
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[c] += wxy * col[c].get();
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < C; ++c) out[((int64_t)r0 * n + a) * 3 + (c / 3) * n * 3 + c % 3] = (double)acc[c] * gp.hprod;
+    }
+}
+
+int contract_df_warp(const dfv *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start, const dfv *w,
+                     const GridParams &gp, double *out, cudaStream_t s) {
+    if (gp.P > kMaxP) return MPS_BAD_ARG;
+    const unsigned blocks = grid_for(n * 32, 256, 152 * 64);
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        if (nr == 3)
+            k_contract_df_warp<3><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, gp, out);
+        else if (nr == 2)
+            k_contract_df_warp<2><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, gp, out);
+        else
+            k_contract_df_warp<1><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, gp, out);
+        MPS_LAUNCH_CHECK();
+    }
+    return MPS_OK;
+}
+
+__global__ void k_weights_df(const double *__restrict__ w, int64_t total, dfv *__restrict__ wd) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        wd[i] = dfv(w[i]);
+}
+
+int weights_df(const double *w, int64_t total, dfv *wd, cudaStream_t s) {
+    k_weights_df<<<grid_for(total, 256), 256, 0, s>>>(w, total, wd);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
 }
 
 // In-place reinterpretation of a grid between float64 values and (hi, lo) pairs

@@ -39,10 +39,16 @@ int contract_tiled(const T *grid, int64_t n, int nrhs, const int32_t *start, con
                    const TileBins &tb, T *partial, double *out, cudaStream_t s);
 
 // The same kernels with double-float accumulation (float-pair arithmetic) on
-// float64 weights, the grids stored as (hi, lo) float pairs: the float64-accurate
+// double-float weights, the grids stored as (hi, lo) float pairs: the float64-accurate
 // matvec without float64 issue (no conversion to or from float64 between stages).
-int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const double *w, const GridParams &gp,
+int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const dfv *w, const GridParams &gp,
                     const TileBins &tb, dfv *grid, cudaStream_t s);
+// Warp-per-particle contraction of double-float grids (particles in `order`, null =
+// input order); out[r][a][c] = hprod * sum (overwrites).  w: double-float weights.
+int contract_df_warp(const dfv *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start, const dfv *w,
+                     const GridParams &gp, double *out, cudaStream_t s);
+// Double-float copy of float64 weights.
+int weights_df(const double *w, int64_t total, dfv *wd, cudaStream_t s);
 int contract_tiled_df(const dfv *grid, int64_t n, int nrhs, const int32_t *start, const double *w,
                       const GridParams &gp, const TileBins &tb, double *partial, double *out, cudaStream_t s);
 // Grid storage conversions in place (float64 <-> (hi, lo) pairs), for the untiled kernels.

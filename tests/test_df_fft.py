@@ -43,6 +43,14 @@ def test_df_matvec_matches_fp64_and_oracle(config, Ngrid):
     o64 = s.matvec(m, precision="fp64").cpu().numpy()
     odf = s.matvec(m, precision="df").cpu().numpy()
     assert _rel(odf, o64) < 1e-12
+    os.environ["MPS_DF_CONTRACT"] = "tiled"                # tiled double-float contraction (default: warp gather)
+    try:
+        odf_tiled = s.matvec(m, precision="df").cpu().numpy()
+    finally:
+        del os.environ["MPS_DF_CONTRACT"]
+    assert _rel(odf_tiled, o64) < 1e-12
+    for k in (1, 2):                                       # 1 and 2 vectors per launch
+        assert _rel(s.matvec(m[:k], precision="df").cpu().numpy(), o64[:k]) < 1e-12
     o32 = s.matvec(m, precision="fp32").cpu().numpy()     # float32 operator, cuFFT
     assert _rel(o32, o64) < 2e-5
     os.environ["MPS_FFT32"] = "own"                        # float32 operator on the hand-written FFT
