@@ -189,19 +189,22 @@ __device__ __forceinline__ dfv group_xor<dfv>(dfv v, int o, int G) {
 }
 
 // T: pair arithmetic (float, double or double-float dfv); mT: the moments read
-// by the pair loop in type TM (float64 m itself, or its double-float copy).
+// by the pair loop in type TM (float64 m itself, or its float / double-float copy).
+// order: optional row visiting order (null = row index).
 template <typename T, int G, int R, typename TM = double>
 __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, double *__restrict__ out, int64_t n,
                                                 int nrhs, int r0, const int64_t *__restrict__ row_ptr,
                                                 PairData<T> pd, const double *__restrict__ diag,
                                                 const int32_t *__restrict__ diag_of_rhs,
                                                 const double *__restrict__ slab, int accumulate,
-                                                const TM *__restrict__ mT) {
+                                                const TM *__restrict__ mT, const int32_t *__restrict__ order) {
     const int lane = threadIdx.x % G;
     const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
     const int nr = min(R, nrhs - r0);
-    for (int64_t a = grp; a < n; a += ngrp) {
+    for (int64_t i = grp; i < n; i += ngrp) {
+        // rows in `order` (cell order): neighbouring groups read overlapping neighbour moments
+        const int64_t a = order ? (int64_t)order[i] : i;
         T acc[R][3];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r][0] = acc[r][1] = acc[r][2] = (T)0;
@@ -260,13 +263,13 @@ int real_space_csr(const double *m, double *out, int64_t n, int nrhs, const int6
     for (int r0 = 0; r0 < nrhs; r0 += 4) {
         int nr = nrhs - r0;
         if (nr >= 4)
-            k_rs_csr<T, G, 4><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
+            k_rs_csr<T, G, 4><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
         else if (nr == 3)
-            k_rs_csr<T, G, 3><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
+            k_rs_csr<T, G, 3><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
         else if (nr == 2)
-            k_rs_csr<T, G, 2><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
+            k_rs_csr<T, G, 2><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
         else
-            k_rs_csr<T, G, 1><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m);
+            k_rs_csr<T, G, 1><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
         MPS_LAUNCH_CHECK();
     }
     return MPS_OK;
@@ -284,7 +287,7 @@ __global__ void k_to_dfv(const double *__restrict__ m, int64_t total, dfv *__res
 
 int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
                       PairData<dfv> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
-                      bool accumulate, cudaStream_t s) {
+                      bool accumulate, const int32_t *order, cudaStream_t s) {
     k_to_dfv<<<grid_for((int64_t)nrhs * n * 3, 256), 256, 0, s>>>(m, (int64_t)nrhs * n * 3, mdf);
     MPS_LAUNCH_CHECK();
     constexpr int G = 8;
@@ -293,13 +296,56 @@ int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrh
         const int nr = nrhs - r0;
         if (nr >= 3)
             k_rs_csr<dfv, G, 3, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
-                                                          accumulate, mdf);
+                                                          accumulate, mdf, order);
         else if (nr == 2)
             k_rs_csr<dfv, G, 2, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
-                                                          accumulate, mdf);
+                                                          accumulate, mdf, order);
         else
             k_rs_csr<dfv, G, 1, dfv><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
-                                                          accumulate, mdf);
+                                                          accumulate, mdf, order);
+        MPS_LAUNCH_CHECK();
+    }
+    return MPS_OK;
+}
+
+__global__ void k_to_f32(const double *__restrict__ m, int64_t total, float *__restrict__ mf) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        mf[i] = (float)m[i];
+}
+
+// Float32 pair sum on a float copy of the moments (converted once per matvec, not
+// once per pair: float64 -> float32 conversions run on GB300's narrow float64
+// pipe), rows in `order`, up to 8 right-hand sides per pass over the pair data.
+int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
+                       PairData<float> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
+                       bool accumulate, const int32_t *order, cudaStream_t s) {
+    k_to_f32<<<grid_for((int64_t)nrhs * n * 3, 256), 256, 0, s>>>(m, (int64_t)nrhs * n * 3, m32);
+    MPS_LAUNCH_CHECK();
+    constexpr int G = 8;
+    const unsigned grid = grid_for(n * G, 256, 152 * 64);
+    for (int r0 = 0; r0 < nrhs;) {
+        const int nr = nrhs - r0;
+        if (nr >= 8) {
+            k_rs_csr<float, G, 8, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, order);
+            r0 += 8;
+        } else if (nr >= 4) {
+            k_rs_csr<float, G, 4, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, order);
+            r0 += 4;
+        } else if (nr == 3) {
+            k_rs_csr<float, G, 3, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, order);
+            r0 += 3;
+        } else if (nr == 2) {
+            k_rs_csr<float, G, 2, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, order);
+            r0 += 2;
+        } else {
+            k_rs_csr<float, G, 1, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, order);
+            r0 += 1;
+        }
         MPS_LAUNCH_CHECK();
     }
     return MPS_OK;

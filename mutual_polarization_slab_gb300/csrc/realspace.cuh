@@ -12,7 +12,11 @@ int real_space_csr(const double *m, double *out, int64_t n, int nrhs, const int6
 // scratch for the double-float copy of m (nrhs x n x 3).
 int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
                       PairData<dfv> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
-                      bool accumulate, cudaStream_t s);
+                      bool accumulate, const int32_t *order, cudaStream_t s);
+// Float32 pair sum on a float copy m32 (nrhs x n x 3, scratch) of the moments.
+int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
+                       PairData<float> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
+                       bool accumulate, const int32_t *order, cudaStream_t s);
 int build_diag(const double *lam, int64_t total, const double *perp, double *diag, cudaStream_t s);
 int slab_terms(const double *m, int64_t n, int nrhs, double scale, double *slab, cudaStream_t s);
 void table_self_terms(double xi, double *s_pc, double *s_fd);

@@ -112,6 +112,7 @@ struct mps_system {
     int32_t *start = nullptr;
     int32_t *order = nullptr;        // particle ids sorted by (cell, id): spatial visiting order
     dfv *wdf = nullptr;              // double-float copy of w64 (built by the first double-float matvec)
+    float *m32 = nullptr;            // float copy of the moments for the float32 pair sum (scratch)
     double *w64 = nullptr;
     float *w32 = nullptr;
     double *h64 = nullptr;       // owned by green (shared, cached per grid)
@@ -156,7 +157,7 @@ static void free_system(mps_system *s) {
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
                     s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->g32, s->pdf.A, s->pdf.BA,
-                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order, s->wdf};
+                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order, s->wdf, s->m32};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -468,6 +469,13 @@ static int ensure_tiles(mps_system *s, int use, cudaStream_t st, bool *used) {
 
 static bool df_usable(mps_system *s);
 
+// Float32 pair sum (accumulates into out) on the system's float copy of the moments.
+static int real_space_f32(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * 3 * (size_t)s->n * s->max_rhs, st));
+    return real_space_csr_f32(m, s->m32, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true,
+                              s->order, st);
+}
+
 // Float64 pair data of the dipole operator, converted from the double-float list
 // the first time a float64 path needs it.
 static int ensure_p64(mps_system *s, cudaStream_t st) {
@@ -539,7 +547,7 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
         MPS_TRY(ensure_p64(s, st));
         MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
     } else {
-        MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+        MPS_TRY(real_space_f32(s, m, out, nrhs, st));
     }
     STAGE_MARK(7);
     return MPS_OK;
@@ -602,7 +610,7 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(6);
     if (!s->mdf) MPS_TRY(dalloc(&s->mdf, sizeof(dfv) * 3 * (size_t)s->n * s->max_rhs, st));
     MPS_TRY(real_space_csr_df(m, s->mdf, out, s->n, nrhs, s->row_ptr, s->pdf, s->diag, s->diag_idx, s->slab, true,
-                              st));
+                              s->order, st));
     STAGE_MARK(7);
     return MPS_OK;
 }
@@ -675,7 +683,7 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
     if (dbl)
         MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
     else
-        MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+        MPS_TRY(real_space_f32(s, m, out, nrhs, st));
     STAGE_MARK(7);
     return MPS_OK;
 }
@@ -728,7 +736,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
         }
     }
     STAGE_MARK(6);
-    MPS_TRY(real_space_csr<float>(m, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true, st));
+    MPS_TRY(real_space_f32(s, m, out, nrhs, st));
     STAGE_MARK(7);
     return MPS_OK;
 }

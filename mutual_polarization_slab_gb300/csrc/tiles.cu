@@ -14,6 +14,9 @@
 // Both produce the same sums as the reference's per-particle loops
 // (EW/ewald.py:370-467) up to summation order.
 #include "tiles.cuh"
+
+#include <cstdlib>
+#include <cstring>
 #include "dfloat.cuh"
 
 namespace mps {
@@ -553,8 +556,12 @@ int contract_df_warp(const dfv *grid, int64_t n, int nrhs, const int32_t *order,
                      const GridParams &gp, double *out, cudaStream_t s) {
     if (gp.P > kMaxP) return MPS_BAD_ARG;
     const unsigned blocks = grid_for(n * 32, 256, 152 * 64);
-    for (int r0 = 0; r0 < nrhs; r0 += 3) {
-        const int nr = min(3, nrhs - r0);
+    // one vector per launch by default: a third of the registers (102 -> ~50), so three times the warps in flight
+    // to cover the L2 latency of the grid reads; MPS_DF_CONTRACT_NR=3 batches three vectors per launch
+    const char *e = getenv("MPS_DF_CONTRACT_NR");
+    const int per = (e && strcmp(e, "3") == 0) ? 3 : 1;
+    for (int r0 = 0; r0 < nrhs; r0 += per) {
+        const int nr = min(per, nrhs - r0);
         if (nr == 3)
             k_contract_df_warp<3><<<blocks, 256, 0, s>>>(grid, n, r0, order, start, w, gp, out);
         else if (nr == 2)
