@@ -76,6 +76,26 @@ int mps_abi_version(void);
  * each with its r = 0 self value in column 0. */
 int mps_real_space_table(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
 
+/* Replaces Compute_Field/RealSpaceTable.m:1-150 (the tables of the probe-point field map):
+ * as mps_real_space_table, with field_dip_1 and field_dip_2 free of the r < 2
+ * overlap polynomial (Compute_Field/RealSpaceTable.m:80-86, 102-109 comment it out). */
+int mps_real_space_table_probe(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
+
+/* Replaces Compute_Field/FieldMap.m:1-59 with its MagneticField.m:1-74 and
+ * RealSpace.m:1-60 (and the probe/particle neighbour list of NeighborList_Types.m):
+ * the field at n_e probe points x_e (n_e x 3) from n_p dipoles p (n_p x 3) at x_p,
+ * E = -(wave-space part contracted at the probes + real-space part), as FieldMap
+ * returns it.  Ngrid, P, eta[3], rc as the caller derives them (FieldMap.m:24-33);
+ * perp / para / rvals: field_dip_1 / field_dip_2 of mps_real_space_table_probe and
+ * their separations (rvals[0] = 0), n_tab rows.  Real-space pairs with d >= rc or
+ * d = 0 are skipped (RealSpace.m:33).  All pointers are float64 device arrays except
+ * box, Ngrid and eta (host).  MPS_RC_GT_HALF_BOX when rc > L/2 on an axis
+ * (FieldMap.m:36-39); MPS_TABLE_RANGE when a separation is beyond the table. */
+int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, const double *p, int64_t n_p,
+                  const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P, const double *eta,
+                  const double *perp, const double *para, const double *rvals, int64_t n_tab, double *E,
+                  mps_stream_t stream);
+
 /* Replaces the dipole + quadrupole couplings of Capacitance_Quadrupole/RealSpaceTable.m:171-378.
  * r: n separations (no zero).  tables: 7 x (n+1) float64, rows field_quad_1,
  * field_quad_2, field_quad_3, grad_quad_1, grad_quad_2, grad_quad_3, grad_quad_4,

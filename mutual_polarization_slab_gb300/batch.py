@@ -78,7 +78,38 @@ def _eps(beta):
     return (1.0 + 2.0 * beta) / (1.0 - beta)
 
 
-def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None):
+def fft_size(n: int) -> int:
+    """Smallest m >= n whose prime factors are 2, 3 and 5 (radices cuFFT runs
+    fast; few such sizes, so many configurations share their plans)."""
+    m = max(int(n), 1)
+    while True:
+        k = m
+        for p in (2, 3, 5):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m += 1
+
+
+def grid_for(box, xi, tol, fft_friendly=True):
+    """(Ngrid, P) of one configuration: the tolerance rule of CS/ComputeField.m:25-31,
+    each axis rounded up to an FFT-friendly size when ``fft_friendly`` (a finer
+    grid, so at least the rule's accuracy; P follows the finer spacing by the same
+    rule).  Configurations then share a few FFT sizes: each new size costs a cuFFT
+    plan (tens of ms), which dominated a batch of configurations of distinct sizes."""
+    from .sizes import spectral_parameters
+
+    _, ng, _, P, _ = spectral_parameters(box, xi, tol)
+    if not fft_friendly:
+        return ng, P
+    ng = np.array([fft_size(int(v)) for v in ng], dtype=np.int64)
+    hm = float(np.mean(np.asarray(box, dtype=np.float64).reshape(3) / ng))
+    return ng, int(math.ceil(2 / hm - 2 * math.log(tol) / math.pi))
+
+
+def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None,
+                        fft_friendly=True):
     """C (K, 3, 3) (row i = mean dipole for the unit field along i) of one
     configuration for every contrast scaling, all 3K solves in one batch."""
     import torch
@@ -96,7 +127,8 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
         xi = lt / rc
     eps_sets = np.stack([_eps(cfg.beta * sk) for sk in s])           # (K, N)
     n = cfg.n
-    sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, box, xi, tol, max_rhs=3 * K)
+    ng, P = grid_for(box, xi, tol, fft_friendly)
+    sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, box, xi, tol, Ngrid=ng, P=P, max_rhs=3 * K)
     try:
         b = torch.zeros((3 * K, n, 3), dtype=torch.float64, device="cuda")
         x0 = torch.zeros_like(b)

@@ -146,6 +146,74 @@ __device__ __forceinline__ void walk_at(const CellWalk &cw, int j, int &o, int64
     pos = __shfl_sync(0xffffffffu, cw.cstart, lo) + (j - __shfl_sync(0xffffffffu, cw.pre, lo));
 }
 
+// Field at probe points from the dipoles of sources within rc (Compute_Field/RealSpace.m:1-60
+// over the probe/source neighbour list of Compute_Field/FieldMap.m:46-52): one warp per probe walks
+// the sources of the 27 cells around the probe's cell.  Minimum image r - L trunc(2 r / L); pairs
+// with d >= rc or d = 0 are skipped; A, B interpolated between the bracketing table rows (first
+// row with rvals >= d); out[e] = sum A m + (B - A) (m . r^) r^ in a fixed order per probe.
+struct Box3 {
+    double L[3];
+};
+
+__global__ void __launch_bounds__(256) k_probe_real(const double *__restrict__ xe, int64_t ne,
+                                                    const int64_t *__restrict__ cell_e,
+                                                    const double *__restrict__ xp, const double *__restrict__ p,
+                                                    const int32_t *__restrict__ sorted,
+                                                    const int32_t *__restrict__ counts,
+                                                    const int64_t *__restrict__ starts, int64_t ncx, int64_t ncy,
+                                                    int64_t ncz, Box3 box, double rc, const double *__restrict__ perp,
+                                                    const double *__restrict__ para, const double *__restrict__ rv,
+                                                    int64_t ntab, double *__restrict__ out, int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < ne; e += nw) {
+        const int32_t c = (int32_t)(cell_e[3 * e] + ncx * (cell_e[3 * e + 1] + ncy * cell_e[3 * e + 2]));
+        const CellWalk cw = cell_walk(c, lane, counts, starts, ncx, ncy, ncz);
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+            if (j >= cw.total) continue;
+            const int32_t b = sorted[pos];
+            double r[3], d2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double v = xe[3 * e + k] - xp[3 * (int64_t)b + k];
+                v -= box.L[k] * trunc(2.0 * v / box.L[k]);
+                r[k] = v;
+                d2 += v * v;
+            }
+            const double d = sqrt(d2);
+            if (!(d < rc) || !(d > 0.0)) continue;
+            int64_t lo = 1, hi = ntab - 1;   // first row with rv >= d, searched in [1, ntab - 1]
+            if (!(rv[hi] >= d)) {
+                atomicExch(err, 1);
+                continue;
+            }
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (rv[mid] >= d) hi = mid; else lo = mid + 1;
+            }
+            const double rh = rv[lo], rl = rv[lo - 1], span = rh - rl;
+            const double A = perp[lo - 1] * (rh - d) / span + perp[lo] * (d - rl) / span;
+            const double B = para[lo - 1] * (rh - d) / span + para[lo] * (d - rl) / span;
+            const double *m = p + 3 * (int64_t)b;
+            const double mr = (m[0] * r[0] + m[1] * r[1] + m[2] * r[2]) / d;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[k] += A * (m[k] - mr * r[k] / d) + B * mr * r[k] / d;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) out[3 * e + k] = acc[k];
+    }
+}
+
 // Candidate counts in emission-slot order: slot(s,o) = 27*start[c] + o*count[c] + (s - start[c]).
 __global__ void k_candidate_slots(const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
                                   const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
@@ -897,6 +965,52 @@ int pairs_df_to_f64(const PairData<dfv> &pdf, int64_t np, PairData<double> p64, 
     k_pairs_df_to_f64<<<grid_for(np, 256), 256, 0, s>>>(pdf, np, p64);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
+}
+
+
+int probe_real_space(const double *xe, int64_t ne, const double *xp, const double *p, int64_t np, const double *box,
+                     double rc, const double *perp, const double *para, const double *rv, int64_t ntab, double *out,
+                     cudaStream_t s) {
+    if (ne == 0) return MPS_OK;
+    if (ntab < 2) return MPS_BAD_ARG;
+    int64_t ncell[3];
+    compute_ncell(box, rc, ncell);
+    const int64_t ncells = ncell[0] * ncell[1] * ncell[2];
+    int64_t *cell_p = nullptr, *cell_e = nullptr;
+    void *bins = nullptr;
+    int *err = nullptr;
+    auto cleanup = [&]() {
+        if (cell_p) cudaFreeAsync(cell_p, s);
+        if (cell_e) cudaFreeAsync(cell_e, s);
+        if (bins) cudaFreeAsync(bins, s);
+        if (err) cudaFreeAsync(err, s);
+    };
+    if (cudaMallocAsync((void **)&cell_p, sizeof(int64_t) * 3 * (np > 0 ? np : 1), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&cell_e, sizeof(int64_t) * 3 * ne, s) != cudaSuccess ||
+        cudaMallocAsync(&bins, cell_bins_bytes(np, ncells), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&err, sizeof(int), s) != cudaSuccess) {
+        cleanup();
+        return MPS_NO_MEMORY;
+    }
+    int rcode = cudaMemsetAsync(err, 0, sizeof(int), s) == cudaSuccess ? MPS_OK : MPS_CUDA_ERR;
+    CellBins cb;
+    if (!rcode) rcode = cell_assign(xp, np, box, ncell, cell_p, s);
+    if (!rcode) rcode = cell_bins_build(cell_p, np, ncell, bins, cb, s);
+    if (!rcode) rcode = cell_assign(xe, ne, box, ncell, cell_e, s);
+    if (!rcode) {
+        Box3 b3{{box[0], box[1], box[2]}};
+        k_probe_real<<<grid_for(ne * 32, 256, 152 * 64), 256, 0, s>>>(
+            xe, ne, cell_e, xp, p, cb.sorted, cb.counts, cb.starts, ncell[0], ncell[1], ncell[2], b3, rc, perp, para,
+            rv, ntab, out, err);
+        if (cudaGetLastError() != cudaSuccess) rcode = MPS_CUDA_ERR;
+    }
+    int herr = 0;
+    if (!rcode && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                   cudaStreamSynchronize(s) != cudaSuccess))
+        rcode = MPS_CUDA_ERR;
+    cleanup();
+    if (!rcode && herr) rcode = MPS_TABLE_RANGE;
+    return rcode;
 }
 
 }  // namespace mps

@@ -64,4 +64,10 @@ int csr_pairs_fill_df(const double *x, const float *xf, const float2 *xdf, doubl
 // p64 = pdf converted to float64 (the float64 operator's pair data, built on demand).
 int pairs_df_to_f64(const PairData<dfv> &pdf, int64_t np, PairData<double> p64, cudaStream_t s);
 
+// Real-space field at ne probe points from np source dipoles within rc (Compute_Field/RealSpace.m
+// over the probe/source pairs of Compute_Field/FieldMap.m:46-52); out: ne x 3 (overwrites).
+int probe_real_space(const double *xe, int64_t ne, const double *xp, const double *p, int64_t np, const double *box,
+                     double rc, const double *perp, const double *para, const double *rv, int64_t ntab, double *out,
+                     cudaStream_t s);
+
 }  // namespace mps

@@ -110,8 +110,10 @@ __device__ double overlap_poly(int t, double r) {
     }
 }
 
+// overlap: bit t set = row t carries the r < 2 overlap polynomial (all six in the solver's tables;
+// Compute_Field/RealSpaceTable.m drops it from field_dip_1 and field_dip_2).
 __global__ void k_tables(const double *__restrict__ r, int64_t n, double xi, TableSet S, double self_pc,
-                         double self_fd, double *__restrict__ out) {
+                         double self_fd, int overlap, double *__restrict__ out) {
     const int64_t row = n + 1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
         if (i == 0) {
@@ -136,7 +138,7 @@ __global__ void k_tables(const double *__restrict__ r, int64_t n, double xi, Tab
                        (horner(T.E[0], T.nE, rv) * ep + horner(T.E[1], T.nE, rv) * em + horner(T.E[2], T.nE, rv) * e0);
             v += T.cF / pow(rv, (double)T.pF) *
                  (horner(T.F[0], T.nF, rv) * fp + horner(T.F[1], T.nF, rv) * fm + horner(T.F[2], T.nF, rv) * f0);
-            if (rv < 2.0) v += overlap_poly(t, rv);
+            if (rv < 2.0 && ((overlap >> t) & 1)) v += overlap_poly(t, rv);
             out[t * row + i] = v;
         }
     }
@@ -407,7 +409,20 @@ extern "C" int mps_real_space_table(const double *r, int64_t n, double xi, doubl
     double spc, sfd;
     table_self_terms(xi, &spc, &sfd);
     cudaStream_t s = (cudaStream_t)stream;
-    k_tables<<<grid_for(n + 1, 128), 128, 0, s>>>(r, n, xi, S, spc, sfd, tables);
+    k_tables<<<grid_for(n + 1, 128), 128, 0, s>>>(r, n, xi, S, spc, sfd, 0x3f, tables);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+extern "C" int mps_real_space_table_probe(const double *r, int64_t n, double xi, double *tables,
+                                          mps_stream_t stream) {
+    if (n < 0 || !(xi > 0) || !tables || (n > 0 && !r)) return MPS_BAD_ARG;
+    TableSet S;
+    build_specs(xi, S);
+    double spc, sfd;
+    table_self_terms(xi, &spc, &sfd);
+    cudaStream_t s = (cudaStream_t)stream;
+    k_tables<<<grid_for(n + 1, 128), 128, 0, s>>>(r, n, xi, S, spc, sfd, 0x33, tables);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

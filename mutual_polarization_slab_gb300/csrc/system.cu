@@ -1031,6 +1031,8 @@ struct GmresFlags {
     bool final_check = true;   // end with a true residual b - A x (one more matvec)
     bool ls_restart = false;   // restart cycles start from the least-squares residual (Arnoldi relation)
     double *r_out = nullptr;   // optional: final residual vectors (nrhs x n3)
+    bool reorth = true;        // classical Gram-Schmidt twice (false: once; enough for the inner solves of the
+                               // mixed refinement, whose relative targets are 1e-4..0.5 in float64 arithmetic)
 };
 
 static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, double tol, int restart, int maxit,
@@ -1075,6 +1077,9 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     double *u = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * (kMaxCols + 1));
     {
         int e = multidot_init(partial, n3, nrhs, st);
+        if (e == MPS_OK && !fl.reorth &&
+            cudaMemsetAsync(S.h2, 0, sizeof(double) * (size_t)nrhs * kMaxCols, st) != cudaSuccess)
+            e = MPS_CUDA_ERR;
         if (e) {
             cudaFreeAsync(base, st);
             return e;
@@ -1153,13 +1158,15 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         for (int j = 0; j < restart; ++j) {
             GM_TRY(matvec_any(s, V + (int64_t)j * ldv, w, nrhs, precision, st));
             ++*mv_count;
-            // classical Gram-Schmidt, twice
+            // classical Gram-Schmidt, twice (once for the inner solves of the mixed refinement)
             GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h1, kMaxCols, st));
             k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h1, kMaxCols, w, n3, n3);
             GM_LAUNCH();
-            GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h2, kMaxCols, st));
-            k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h2, kMaxCols, w, n3, n3);
-            GM_LAUNCH();
+            if (fl.reorth) {
+                GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h2, kMaxCols, st));
+                k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h2, kMaxCols, w, n3, n3);
+                GM_LAUNCH();
+            }
             GM_TRY(multidot(w, n3, n3, 1, w, n3, n3, nrhs, partial, S.nrm2, 1, st));
             k_arnoldi_givens<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, j, nrhs, frozen);
             GM_LAUNCH();
@@ -1310,6 +1317,7 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         GmresFlags f0;
         f0.final_check = false;
         f0.ls_restart = true;
+        f0.reorth = false;
         int icyc = 0;
         e = gmres_core(s, b, x, nrhs, inner_tol, o->restart, inner_maxit, s->inner_prec, ic.data(), ir.data(), &icyc, mv32,
                        st, f0);
@@ -1368,6 +1376,7 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         fl.zero_guess = true;
         fl.final_check = false;
         fl.ls_restart = true;
+        fl.reorth = false;
         fl.r_out = incremental ? rn : nullptr;
         // the correction only has to take the worst residual below the target:
         // relative tolerance max(inner_tol, 0.3 tol / relres), at most 0.5
@@ -1786,6 +1795,80 @@ extern "C" int mps_system_stage_times(mps_system *sys, double *ms, int64_t *coun
         sys->stage_count[p] = 0;
     }
     return MPS_OK;
+}
+
+__global__ void k_field_combine(const double *__restrict__ wave, const double *__restrict__ real, int64_t total,
+                                double *__restrict__ E) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        E[i] = -(wave[i] + real[i]);
+}
+
+extern "C" int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, const double *p, int64_t n_p,
+                             const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P,
+                             const double *eta, const double *perp, const double *para, const double *rvals,
+                             int64_t n_tab, double *E, mps_stream_t stream) {
+    if (n_e < 0 || n_p < 0 || !box || !Ngrid || !eta || !(xi > 0) || !(rc > 0) || P < 1 || n_tab < 2) return MPS_BAD_ARG;
+    if ((n_e > 0 && (!x_e || !E)) || (n_p > 0 && (!x_p || !p)) || !perp || !para || !rvals) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (Ngrid[d] < P || !(box[d] > 0)) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (rc > 0.5 * box[d]) return MPS_RC_GT_HALF_BOX;
+    if (n_e == 0) return MPS_OK;
+    configure_pool_once();
+    cudaStream_t st = (cudaStream_t)stream;
+    const GridParams gp = make_grid_params(Ngrid, box, xi, eta, P);
+    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
+    int32_t *start_p = nullptr, *start_e = nullptr;
+    double *w_p = nullptr, *w_e = nullptr, *grid = nullptr, *spec = nullptr, *H = nullptr, *wave = nullptr,
+           *real = nullptr;
+    void *work = nullptr;
+    auto cleanup = [&]() {
+        void *ptrs[] = {start_p, start_e, w_p, w_e, grid, spec, H, wave, real, work};
+        for (void *q : ptrs)
+            if (q) cudaFreeAsync(q, st);
+    };
+    int rc_ = MPS_OK;
+    rc_ = dalloc(&start_p, sizeof(int32_t) * 3 * (size_t)(n_p > 0 ? n_p : 1), st);
+    if (!rc_) rc_ = dalloc(&w_p, sizeof(double) * 3 * (size_t)P * (n_p > 0 ? n_p : 1), st);
+    if (!rc_) rc_ = dalloc(&start_e, sizeof(int32_t) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&w_e, sizeof(double) * 3 * (size_t)P * n_e, st);
+    if (!rc_) rc_ = dalloc(&grid, sizeof(double) * 3 * (size_t)gp.G, st);
+    if (!rc_) rc_ = dalloc(&spec, sizeof(double) * 2 * 3 * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&H, sizeof(double) * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&wave, sizeof(double) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&real, sizeof(double) * 3 * (size_t)n_e, st);
+    // wave space: spread the source dipoles, D2Z, H k^k^ scale, Z2D, contract at the probes
+    if (!rc_) rc_ = grid_geometry(x_p, n_p, gp, start_p, w_p, nullptr, st);
+    if (!rc_) rc_ = spread<double>(p, n_p, 1, start_p, w_p, gp, grid, st);
+    if (!rc_) rc_ = green_half(gp, H, nullptr, st);
+    CachedPlan fwd{}, inv{};
+    if (!rc_) rc_ = get_plan(CUFFT_D2Z, gp, 3, &fwd);
+    if (!rc_) rc_ = get_plan(CUFFT_Z2D, gp, 3, &inv);
+    if (!rc_) rc_ = dalloc(&work, std::max(fwd.work, inv.work) + 16, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(fwd.h, work) != CUFFT_SUCCESS || cufftSetStream(fwd.h, st) != CUFFT_SUCCESS ||
+            cufftExecD2Z(fwd.h, (cufftDoubleReal *)grid, (cufftDoubleComplex *)spec) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) rc_ = scale_half<double>(spec, 1, gp, H, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(inv.h, work) != CUFFT_SUCCESS || cufftSetStream(inv.h, st) != CUFFT_SUCCESS ||
+            cufftExecZ2D(inv.h, (cufftDoubleComplex *)spec, (cufftDoubleReal *)grid) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) rc_ = grid_geometry(x_e, n_e, gp, start_e, w_e, nullptr, st);
+    if (!rc_) rc_ = contract<double>(grid, n_e, 1, start_e, w_e, gp, wave, st);
+    // real space: sources within rc of each probe
+    if (!rc_) rc_ = probe_real_space(x_e, n_e, x_p, p, n_p, box, rc, perp, para, rvals, n_tab, real, st);
+    if (!rc_) {
+        k_field_combine<<<grid_for(3 * n_e, 256), 256, 0, st>>>(wave, real, 3 * n_e, E);
+        count_launch();
+        if (cudaGetLastError() != cudaSuccess) rc_ = MPS_CUDA_ERR;
+    }
+    cleanup();
+    return rc_;
 }
 
 extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms) {

@@ -415,9 +415,9 @@ static int spread_launch(const double *m, int64_t n, int r0, const int32_t *star
 
 template <typename T, int TZ, typename TW, typename TG>
 static int spread_dispatch(const double *m, int64_t n, int nrhs, const int32_t *start, const TW *w,
-                           const GridParams &gp, const TileBins &tb, TG *grid, cudaStream_t s) {
-    for (int r0 = 0; r0 < nrhs; r0 += 3) {
-        const int nr = min(3, nrhs - r0);
+                           const GridParams &gp, const TileBins &tb, TG *grid, cudaStream_t s, int per = 3) {
+    for (int r0 = 0; r0 < nrhs; r0 += per) {
+        const int nr = min(per, nrhs - r0);
         int rc = nr == 3 ? spread_launch<T, TZ, 3, TW, TG>(m, n, r0, start, w, gp, tb, grid, s)
                  : nr == 2 ? spread_launch<T, TZ, 2, TW, TG>(m, n, r0, start, w, gp, tb, grid, s)
                            : spread_launch<T, TZ, 1, TW, TG>(m, n, r0, start, w, gp, tb, grid, s);
@@ -436,6 +436,8 @@ int spread_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, con
 
 int spread_tiled_df(const double *m, int64_t n, int nrhs, const int32_t *start, const dfv *w, const GridParams &gp,
                     const TileBins &tb, dfv *grid, cudaStream_t s) {
+    // three vectors per launch: one vector per launch (a third of the registers) measured slower, the
+    // per-particle staging and w products then being repeated for every vector
     if (tb.tz == 8) return spread_dispatch<dfv, 8, dfv, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
     if (tb.tz == 4) return spread_dispatch<dfv, 4, dfv, dfv>(m, n, nrhs, start, w, gp, tb, grid, s);
     return MPS_BAD_ARG;

@@ -31,6 +31,15 @@ def test_partition_is_balanced_and_complete():
         assert all(p == sorted(p) for p in parts)
 
 
+def test_fft_friendly_grid():
+    assert [batch.fft_size(v) for v in (1, 31, 32, 47, 61, 89, 97, 191)] == [1, 32, 32, 48, 64, 90, 100, 192]
+    box = np.array([30.0, 30.0, 30.0])
+    ng0, P0 = batch.grid_for(box, 0.55, 1e-4, fft_friendly=False)
+    ng, P = batch.grid_for(box, 0.55, 1e-4)
+    assert np.all(ng >= ng0) and P >= P0
+    assert all(batch.fft_size(int(v)) == int(v) for v in ng)
+
+
 def test_make_configurations_properties():
     cfgs = batch.make_configurations(count=3, seed=4, n_range=(100, 400))
     assert [c.index for c in cfgs] == [0, 1, 2]
