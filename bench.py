@@ -516,6 +516,59 @@ def run_quadrupole(args):
                                                             / math.pi)]}), flush=True)
 
 
+def run_forces(args):
+    """Config 5: N = 200,000 spheres by RSA at volume fraction 0.35 (seed 5),
+    beta = 0.9, H0 = (0, 0, 1); E = -1/2 m.H0 with adjoint forces dE/dx and
+    dE/dbeta (mixed solve to 1e-8), then overdamped Brownian dynamics steps
+    (dt = 1e-4) re-solving every step from the previous moments.  240^3 grid
+    (h = 0.557, the bench spacing rounded to a cuFFT-friendly size), P = 10,
+    rc = (60 / phi)^(1/3), xi = 4 / rc.  Prints one JSON line."""
+    import torch
+
+    from mutual_polarization_slab_gb300 import forces as gf
+    from mutual_polarization_slab_gb300.workloads import rsa
+
+    torch.cuda.set_device(0)
+    n, phi = 200_000, 0.35
+    t0 = time.perf_counter()
+    x, box, _ = rsa(n, phi, seed=5)
+    t_rsa = time.perf_counter() - t0
+    rc = (60.0 / phi) ** (1.0 / 3.0)
+    xi = 4.0 / rc
+    Ngrid, P = [240, 240, 240], 10
+    H0 = np.array([0.0, 0.0, 1.0])
+    xd = torch.as_tensor(x, device="cuda")
+
+    def energy(guess=None):
+        return gf.polarization_energy(xd, 0.9, box, H0, xi, rc, Ngrid, P, tol=1e-8, precision="mixed", guess=guess)
+
+    energy()                                            # warm-up: plans, tables, tuner
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    r = energy()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_force = e0.elapsed_time(e1)
+    bd = gf.BrownianDynamics(xd, 0.9, box, H0, xi, rc, Ngrid, P, dt=1e-4, pol_every=1, tol=1e-8, seed=5)
+    bd.step()                                           # first step solves from scratch
+    steps = max(3, args.steps)
+    torch.cuda.synchronize()
+    e0.record()
+    bd.run(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_bd = e0.elapsed_time(e1) / steps
+    fmax = float(torch.linalg.vector_norm(r.forces, dim=1).max())
+    print(json.dumps({
+        "workload": f"config 5: N={n} RSA phi={phi} (seed 5, {t_rsa:.0f} s to place, untimed), beta=0.9, "
+                    f"H0=(0,0,1), 240^3, P=10, xi={xi:.4f}, rc={rc:.3f}; mixed solve to 1e-8 + adjoint",
+        "metric": "force evaluations/s", "value": 1e3 / ms_force, "ms_per_force_evaluation": ms_force,
+        "relres": r.relres, "energy": r.energy, "max_force": fmax,
+        "brownian_dynamics": {"ms_per_step": ms_bd, "particle_steps_per_s": n / (ms_bd / 1e3), "steps": steps,
+                              "warm_started": True, "solves": bd.solves}}), flush=True)
+
+
 def run_batch(args):
     """Many configurations (polydisperse radii 0.7-1.3, per-particle beta in
     {0.3, 0.9}, volume fraction 0.1-0.35, N log-uniform 500-20000, seed 4), each
@@ -576,8 +629,9 @@ def main():
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--only-mixed", dest="only_mixed", action="store_true",
                     help="time only the mixed solve (profiling runs); prints a short JSON line")
-    ap.add_argument("--workload", default="tensor", choices=["tensor", "quadrupole", "batch"],
-                    help="tensor: the headline N=1e5 capacitance tensor; quadrupole / batch: other configurations")
+    ap.add_argument("--workload", default="tensor", choices=["tensor", "quadrupole", "batch", "forces"],
+                    help="tensor: the headline N=1e5 capacitance tensor; quadrupole / batch / forces: other "
+                         "configurations")
     ap.add_argument("--configs", type=int, default=16, help="batch workload: number of configurations")
     ap.add_argument("--batch-tol", dest="batch_tol", type=float, default=1e-4)
     args = ap.parse_args()
@@ -586,6 +640,9 @@ def main():
         return
     if args.workload == "batch" and args.impl != "reference":
         run_batch(args)
+        return
+    if args.workload == "forces" and args.impl != "reference":
+        run_forces(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -88,13 +88,14 @@ int mps_real_space_table_probe(const double *r, int64_t n, double xi, double *ta
  * returns it.  Ngrid, P, eta[3], rc as the caller derives them (FieldMap.m:24-33);
  * perp / para / rvals: field_dip_1 / field_dip_2 of mps_real_space_table_probe and
  * their separations (rvals[0] = 0), n_tab rows.  Real-space pairs with d >= rc or
- * d = 0 are skipped (RealSpace.m:33).  All pointers are float64 device arrays except
+ * d = 0 are skipped (RealSpace.m:33).  with_real = 0 leaves the real-space part
+ * out (a caller with its own probe/particle pair list, FieldMap.m:44-45, adds it).  All pointers are float64 device arrays except
  * box, Ngrid and eta (host).  MPS_RC_GT_HALF_BOX when rc > L/2 on an axis
  * (FieldMap.m:36-39); MPS_TABLE_RANGE when a separation is beyond the table. */
 int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, const double *p, int64_t n_p,
                   const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P, const double *eta,
-                  const double *perp, const double *para, const double *rvals, int64_t n_tab, double *E,
-                  mps_stream_t stream);
+                  const double *perp, const double *para, const double *rvals, int64_t n_tab, int32_t with_real,
+                  double *E, mps_stream_t stream);
 
 /* Replaces the dipole + quadrupole couplings of Capacitance_Quadrupole/RealSpaceTable.m:171-378.
  * r: n separations (no zero).  tables: 7 x (n+1) float64, rows field_quad_1,

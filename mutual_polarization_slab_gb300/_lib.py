@@ -93,7 +93,7 @@ _SIGS = {
     "mps_sizes_table": (C.c_int, [p, i64, p, i64, f64, p, p, p]),
     "mps_adjoint_forces": (C.c_int, [p, p, p, p, p, i64, i32, p, p, p]),
     "mps_real_space_table_probe": (C.c_int, [p, i64, f64, p, p]),
-    "mps_field_map": (C.c_int, [p, i64, p, p, i64, PD, f64, f64, P64, i32, PD, p, p, p, i64, p, p]),
+    "mps_field_map": (C.c_int, [p, i64, p, p, i64, PD, f64, f64, P64, i32, PD, p, p, p, i64, i32, p, p]),
 }
 
 _lib = None

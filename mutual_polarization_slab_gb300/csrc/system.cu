@@ -1806,7 +1806,7 @@ __global__ void k_field_combine(const double *__restrict__ wave, const double *_
 extern "C" int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, const double *p, int64_t n_p,
                              const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P,
                              const double *eta, const double *perp, const double *para, const double *rvals,
-                             int64_t n_tab, double *E, mps_stream_t stream) {
+                             int64_t n_tab, int32_t with_real, double *E, mps_stream_t stream) {
     if (n_e < 0 || n_p < 0 || !box || !Ngrid || !eta || !(xi > 0) || !(rc > 0) || P < 1 || n_tab < 2) return MPS_BAD_ARG;
     if ((n_e > 0 && (!x_e || !E)) || (n_p > 0 && (!x_p || !p)) || !perp || !para || !rvals) return MPS_BAD_ARG;
     for (int d = 0; d < 3; ++d)
@@ -1861,7 +1861,10 @@ extern "C" int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, 
     if (!rc_) rc_ = grid_geometry(x_e, n_e, gp, start_e, w_e, nullptr, st);
     if (!rc_) rc_ = contract<double>(grid, n_e, 1, start_e, w_e, gp, wave, st);
     // real space: sources within rc of each probe
-    if (!rc_) rc_ = probe_real_space(x_e, n_e, x_p, p, n_p, box, rc, perp, para, rvals, n_tab, real, st);
+    const bool do_real = with_real && n_p > 0;
+    if (!rc_ && do_real) rc_ = probe_real_space(x_e, n_e, x_p, p, n_p, box, rc, perp, para, rvals, n_tab, real, st);
+    if (!rc_ && !do_real && cudaMemsetAsync(real, 0, sizeof(double) * 3 * (size_t)n_e, st) != cudaSuccess)
+        rc_ = MPS_CUDA_ERR;
     if (!rc_) {
         k_field_combine<<<grid_for(3 * n_e, 256), 256, 0, st>>>(wave, real, 3 * n_e, E);
         count_launch();

@@ -1,0 +1,92 @@
+"""Probe-point field map (Compute_Field/FieldMap.m and its folder).
+
+CPU: the oracle's tables equal the solver's tables for r >= 2 and differ from
+them by exactly the overlap polynomial below 2; the oracle's real part over
+given pairs equals its all-pairs form.  GPU: tables 1e-13; the field at 600
+probes (some on particle centres, some inside spheres) against the oracle's
+float64 field map 1e-10 relative (real part of the reference's complex
+pipeline, as the dipole operator); the caller-given pair list path; the
+rc > L/2 guard."""
+import numpy as np
+import pytest
+
+from oracle import ewald_oracle as ew
+from oracle import fieldmap_oracle as fo
+
+
+def test_probe_tables_drop_only_the_overlap():
+    xi = 0.8
+    r = np.arange(1, 10001, dtype=np.float64) * 1e-3
+    p1, p2 = fo.real_space_table_probe(r, xi)
+    _, _, f1, f2, _, _ = ew.real_space_table(r, xi)
+    far = np.concatenate(([True], r >= 2.0))
+    np.testing.assert_array_equal(p1[far], f1[far])
+    np.testing.assert_array_equal(p2[far], f2[far])
+    near = r < 2.0
+    pi = np.pi
+    reg1 = -1 / (4 * pi * r ** 3) + (1 - 9 * r / 16 + r ** 3 / 32) / (4 * pi)
+    reg2 = 1 / (2 * pi * r ** 3) + (1 - 9 * r / 8 + r ** 3 / 8) / (4 * pi)
+    np.testing.assert_allclose((f1[1:] - p1[1:])[near], reg1[near], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose((f2[1:] - p2[1:])[near], reg2[near], rtol=1e-9, atol=1e-9)
+
+
+def _case(seed=3, n_p=300, n_e=600):
+    rng = np.random.default_rng(seed)
+    box = np.array([12.0, 13.0, 14.0])
+    x_p = rng.uniform(0, 1, (n_p, 3)) * box
+    p = rng.standard_normal((n_p, 3))
+    x_e = rng.uniform(0, 1, (n_e, 3)) * box
+    x_e[:20] = x_p[:20]                                              # on particle centres: d = 0 pairs skipped
+    x_e[20:60] = x_p[20:60] + rng.standard_normal((40, 3)) * 0.3     # inside / near spheres (r < 2)
+    return x_e, x_p, p, box
+
+
+def test_oracle_pairs_form_matches_all_pairs():
+    x_e, x_p, p, box = _case(n_p=60, n_e=80)
+    xi = 0.8
+    rc, *_ = fo.field_parameters(box, xi)
+    r = np.arange(1, 10001, dtype=np.float64) * 1e-3
+    perp, para = fo.real_space_table_probe(r, xi)
+    rv = np.concatenate(([0.0], r))
+    full = fo.real_part_pairs(x_e, x_p, p, box, rc, perp, para, rv)
+    a, b = np.meshgrid(np.arange(80), np.arange(60), indexing="ij")
+    again = fo.real_part_pairs(x_e, x_p, p, box, rc, perp, para, rv, (a.reshape(-1), b.reshape(-1)))
+    np.testing.assert_allclose(again, full, rtol=0, atol=1e-14)
+
+
+@pytest.mark.gpu
+def test_field_map_gpu_vs_oracle():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("CUDA device required")
+    from mutual_polarization_slab_gb300 import fieldmap as fm
+
+    xi = 0.8
+    r = np.arange(1, 10001, dtype=np.float64) * 1e-3
+    g1 = fm.real_space_table_probe(r, xi)
+    o1, o2 = fo.real_space_table_probe(r, xi)
+    np.testing.assert_allclose(g1[2], o1, rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(g1[3], o2, rtol=1e-13, atol=1e-15)
+
+    x_e, x_p, p, box = _case()
+    E = fm.field_map(x_e, x_p, p, box, xi)
+    ref = fo.field_map(x_e, x_p, p, box, xi)
+    assert E.shape == (600, 3)
+    assert np.abs(E - ref.real).max() <= 1e-10 * np.abs(ref.real).max()
+
+    # caller-given probe/particle pairs (1-based, as MATLAB): all pairs within rc
+    rc, *_ = fo.field_parameters(box, xi)
+    d = x_e[:, None, :] - x_p[None, :, :]
+    d -= box * np.trunc(2 * d / box)
+    a, b = np.nonzero(np.sqrt((d ** 2).sum(-1)) < rc)
+    E2 = fm.field_map(x_e, x_p, p, box, xi, a + 1, b + 1)
+    assert np.abs(E2 - ref.real).max() <= 1e-10 * np.abs(ref.real).max()
+
+    # CUDA tensors in -> CUDA tensors out
+    Et = fm.field_map(torch.as_tensor(x_e, device="cuda"), torch.as_tensor(x_p, device="cuda"),
+                      torch.as_tensor(p, device="cuda"), box, xi)
+    # (the source spread accumulates float64 with atomics: equal to rounding, not bitwise)
+    assert Et.is_cuda and np.abs(Et.cpu().numpy() - E).max() <= 1e-13 * np.abs(E).max()
+
+    with pytest.raises(ValueError):
+        fm.field_map(x_e, x_p, p, box, 0.2)      # rc = 13.1 > L/2
