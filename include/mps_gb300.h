@@ -218,6 +218,12 @@ typedef struct mps_system_desc {
     int32_t n_class;          /* distinct radii M                                   */
     const double *sizes_tables; /* device 2 x M(M+1)/2 x n_tab: Ep_perp columns then */
                               /* Ep_para columns on rvals (rvals[0] = 0, self first) */
+    /* Complex permittivities (kind MPS_DIPOLE; the spectra of CH/CapacitanceSpectrum.m:38-59 and
+     * CH/CapacitanceTensorSpectrum.m:38-62 with frequency-dependent eps): device n_diag x n imaginary
+     * parts of eps (lambdap holds the real parts), or NULL.  Then every vector of mps_matvec / mps_gmres
+     * is complex, stored as 6 float64 per particle (Re m_x, Re m_y, Re m_z, Im m_x, Im m_y, Im m_z),
+     * and max_rhs counts complex vectors.  mps_matvec_complex and mps_adjoint_forces are not available. */
+    const double *lambdap_imag;
 } mps_system_desc;
 
 enum mps_operator_kind { MPS_DIPOLE = 0, MPS_DIPOLE_QUADRUPOLE = 1, MPS_POLYDISPERSE = 2 };

@@ -44,7 +44,7 @@ class SystemDesc(C.Structure):
         ("n", i64), ("x", p), ("lambdap", p), ("n_diag", i64), ("box", f64 * 3), ("xi", f64), ("rc", f64),
         ("Ngrid", i64 * 3), ("P", i32), ("eta", f64 * 3), ("perp", p), ("para", p), ("rvals", p),
         ("n_tab", i64), ("slab_factor", f64), ("max_rhs", i32), ("kind", i32), ("quad_tables", p),
-        ("radius", p), ("radius_class", p), ("n_class", i32), ("sizes_tables", p),
+        ("radius", p), ("radius_class", p), ("n_class", i32), ("sizes_tables", p), ("lambdap_imag", p),
     ]
 
 

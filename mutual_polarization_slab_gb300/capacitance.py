@@ -46,7 +46,8 @@ def default_table(xi):
 
 def dilute_guess(eps_p, phi, Hhat):
     """4 pi beta / (1 - beta phi) Hhat, beta = (eps-1)/(eps+2), beta(inf) = 1 (capacitance.py:497-501)."""
-    eps = np.asarray(eps_p, dtype=np.float64).reshape(-1)
+    eps = np.asarray(eps_p)
+    eps = eps.astype(np.complex128 if np.iscomplexobj(eps) else np.float64).reshape(-1)
     with np.errstate(invalid="ignore"):
         beta = (eps - 1.0) / (eps + 2.0)
     beta[np.isinf(eps)] = 1.0
@@ -279,6 +280,7 @@ def capacitance_tensor_spectrum(x, box, eps_p, xi, errortol=1e-3, *, slab_factor
                                 restart=None, maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4):
     """Tensor for every permittivity column of ``eps_p (N, N_k)`` and every frame of
     ``x (N,3[,F])`` (Capacitance_Hetero/CapacitanceTensorSpectrum.m:15-62).
+    ``eps_p`` may be complex (frequency-dependent permittivities); C and p are then complex.
 
     The N_k columns of one frame share one system (the permittivity only enters
     the diagonal), and all 3 N_k systems are solved as one batch.
@@ -286,7 +288,11 @@ def capacitance_tensor_spectrum(x, box, eps_p, xi, errortol=1e-3, *, slab_factor
     xn = x.cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x, dtype=np.float64)
     if xn.ndim == 2:
         xn = xn[:, :, None]
-    eps = np.asarray(eps_p, dtype=np.float64)
+    eps = np.asarray(eps_p.cpu() if isinstance(eps_p, torch.Tensor) else eps_p)
+    # complex permittivities (frequency-dependent eps, which the MATLAB driver allows) give complex C and p
+    cplx = np.iscomplexobj(eps)
+    eps = eps.astype(np.complex128 if cplx else np.float64)
+    tdt = torch.complex128 if cplx else torch.float64
     if eps.ndim == 1:
         eps = eps[:, None]
     N, F = xn.shape[0], xn.shape[2]
@@ -297,17 +303,17 @@ def capacitance_tensor_spectrum(x, box, eps_p, xi, errortol=1e-3, *, slab_factor
     perp, para, rv = default_table(xi)
     restart = min(3 * N, 10) if restart is None else int(restart)
     maxit = min(3 * N, 100) if maxit is None else int(maxit)
-    C = np.zeros((3, 3, F, K))
-    p = np.zeros((N, 3, 3, K, F))
+    C = np.zeros((3, 3, F, K), dtype=eps.dtype)
+    p = np.zeros((N, 3, 3, K, F), dtype=eps.dtype)
     for f in range(F):
         lam = eps.T.copy()                                   # (K, N) permittivity sets
         sysm = SpectralEwaldSystem(xn[:, :, f], lam, box, xi, rc, Ngrid, P, perp, para, rv,
                                    slab_factor=slab_factor, eta=eta, max_rhs=3 * K)
-        b = torch.zeros((3 * K, N, 3), dtype=torch.float64, device="cuda")
+        b = torch.zeros((3 * K, N, 3), dtype=tdt, device="cuda")
         x0 = torch.zeros_like(b)
         diag_index = []
         for k in range(K):
-            amp = torch.as_tensor(dilute_guess(eps[:, k], phi, [1.0, 0.0, 0.0])[:, 0], device="cuda")
+            amp = torch.as_tensor(dilute_guess(eps[:, k], phi, [1.0, 0.0, 0.0])[:, 0], dtype=tdt, device="cuda")
             for i in range(3):
                 b[3 * k + i, :, i] = 1.0
                 x0[3 * k + i, :, i] = amp

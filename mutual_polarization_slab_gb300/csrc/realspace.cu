@@ -368,6 +368,29 @@ int build_diag(const double *lam, int64_t total, const double *perp, double *dia
     return MPS_OK;
 }
 
+// Complex permittivity eps = a + i b: D = -3 / (4 pi (1 - eps)) + self_perp, split
+// into its real and imaginary parts (EW/ewald.py:1058 with complex lambda, as the
+// MATLAB spectrum drivers allow).
+__global__ void k_diag_cplx(const double *__restrict__ lr, const double *__restrict__ li, int64_t total,
+                            double self_perp, double *__restrict__ dr, double *__restrict__ di) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const double u = 1.0 - lr[i], v = -li[i];   // 1 - eps = u + i v
+        const double q = u * u + v * v;
+        dr[i] = -3.0 * u / (4.0 * MPS_PI * q) + self_perp;
+        di[i] = 3.0 * v / (4.0 * MPS_PI * q);
+    }
+}
+
+int build_diag_complex(const double *lr, const double *li, int64_t total, const double *perp, double *dr, double *di,
+                       cudaStream_t s) {
+    double self_perp = 0.0;
+    MPS_CUDA_TRY(cudaMemcpyAsync(&self_perp, perp, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaStreamSynchronize(s));
+    k_diag_cplx<<<grid_for(total, 256), 256, 0, s>>>(lr, li, total, self_perp, dr, di);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
 // Slab term per vector: slab_factor * sum_a m_z(a) / V (deterministic two-stage sum).
 __global__ void k_slab(const double *__restrict__ m, int64_t n, double scale, double *__restrict__ slab) {
     __shared__ double sm[32];

@@ -18,6 +18,9 @@ int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int 
                        PairData<float> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
                        bool accumulate, const int32_t *order, cudaStream_t s);
 int build_diag(const double *lam, int64_t total, const double *perp, double *diag, cudaStream_t s);
+// Real and imaginary parts of the diagonal for complex permittivities (lr + i li).
+int build_diag_complex(const double *lr, const double *li, int64_t total, const double *perp, double *dr, double *di,
+                       cudaStream_t s);
 int slab_terms(const double *m, int64_t n, int nrhs, double scale, double *slab, cudaStream_t s);
 void table_self_terms(double xi, double *s_pc, double *s_fd);
 

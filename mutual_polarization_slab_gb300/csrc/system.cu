@@ -113,6 +113,12 @@ struct mps_system {
     int32_t *order = nullptr;        // particle ids sorted by (cell, id): spatial visiting order
     dfv *wdf = nullptr;              // double-float copy of w64 (built by the first double-float matvec)
     float *m32 = nullptr;            // float copy of the moments for the float32 pair sum (scratch)
+    // complex permittivities: vectors are (Re m, Im m) per particle (ndof 6); the real operator runs on the
+    // 2 nc real vectors [Re m_0..Re m_{nc-1}, Im m_0..Im m_{nc-1}] and the imaginary diagonal couples them
+    bool cplx = false;
+    int max_rhs_c = 0;               // complex vectors per matvec (max_rhs = 2 max_rhs_c real ones)
+    double *diag_im = nullptr;       // n_diag x n imaginary part of the diagonal
+    double *cx_in = nullptr, *cx_out = nullptr;   // 2 max_rhs_c x n x 3 scratch
     double *w64 = nullptr;
     float *w32 = nullptr;
     double *h64 = nullptr;       // owned by green (shared, cached per grid)
@@ -157,7 +163,8 @@ static void free_system(mps_system *s) {
                     s->grid64, s->spec64, s->grid32, s->spec32, s->cgrid, s->rgrid2, s->slab, s->diag_idx,
                     s->fft_work, s->p64.dist, s->qcoef, s->qcoef32, s->diagq, s->qkcoef, s->qkcoef32,
                     s->cs_base, s->cs_g64, s->cs_g32, s->cs_h64, s->cs_h32, s->g32, s->pdf.A, s->pdf.BA,
-                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order, s->wdf, s->m32};
+                    s->pdf.rx, s->pdf.ry, s->pdf.rz, s->pdf.dist, s->mdf, s->order, s->wdf, s->m32, s->diag_im,
+                    s->cx_in, s->cx_out};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
@@ -278,7 +285,8 @@ static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *o
 
 static int ensure_grids(mps_system *s, int precision, cudaStream_t st) {
     // component grids per vector: one scalar grid for the polydisperse operator
-    size_t nr = (size_t)s->max_rhs * (s->kind == MPS_POLYDISPERSE ? 1 : s->ndof);
+    // (complex mode: the real operator runs on max_rhs real 3-vectors)
+    size_t nr = (size_t)s->max_rhs * (s->kind == MPS_POLYDISPERSE ? 1 : (s->cplx ? 3 : s->ndof));
     if (precision == MPS_FP64) {
         if (!s->grid64) MPS_TRY(dalloc(&s->grid64, nr * s->gp.G * sizeof(double), st));
         if (!s->spec64) MPS_TRY(dalloc(&s->spec64, nr * s->Gc * 2 * sizeof(double), st));
@@ -296,8 +304,10 @@ static int upload_diag_idx(mps_system *s, const int32_t *diag_index, int nrhs, c
         int32_t v = diag_index ? diag_index[r] : 0;
         if (v < 0 || v >= s->n_diag) return MPS_BAD_ARG;
         s->diag_idx_host[r] = v;
+        if (s->cplx) s->diag_idx_host[nrhs + r] = v;   // the imaginary halves use the same sets
     }
-    MPS_CUDA_TRY(cudaMemcpyAsync(s->diag_idx, s->diag_idx_host, sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+    const int nup = s->cplx ? 2 * nrhs : nrhs;
+    MPS_CUDA_TRY(cudaMemcpyAsync(s->diag_idx, s->diag_idx_host, sizeof(int32_t) * nup, cudaMemcpyHostToDevice, st));
     return MPS_OK;
 }
 
@@ -741,7 +751,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     return MPS_OK;
 }
 
-static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+static int matvec_real(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
     if (precision == MPS_FP32_GRAD) return matvec_grad(s, m, out, nrhs, st);
     if (precision == MPS_DF) {
         if (df_usable(s)) return matvec_df(s, m, out, nrhs, st);
@@ -753,6 +763,53 @@ static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int
         return precision == MPS_FP64 ? matvec_quad<double>(s, m, out, nrhs, st)
                                      : matvec_quad<float>(s, m, out, nrhs, st);
     return precision == MPS_FP64 ? matvec_impl<double>(s, m, out, nrhs, st) : matvec_impl<float>(s, m, out, nrhs, st);
+}
+
+// (Re m, Im m) per particle -> the 2 nc real vectors, and back with the imaginary
+// diagonal's coupling: out_re = Mu + Re(D) u - Im(D) v, out_im = Mv + Re(D) v + Im(D) u
+// (Mu, Mv from the real operator, which already adds Re(D)).
+__global__ void k_cplx_split(const double *__restrict__ m6, int nc, int64_t n, double *__restrict__ cx) {
+    const int64_t tot = (int64_t)nc * n * 3;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = t / (n * 3), a = (t / 3) % n;
+        const int c = (int)(t % 3);
+        const double *src = m6 + (q * n + a) * 6;
+        cx[t] = src[c];
+        cx[tot + t] = src[3 + c];
+    }
+}
+
+__global__ void k_cplx_join(const double *__restrict__ cx, const double *__restrict__ mx, const double *__restrict__ di,
+                            const int32_t *__restrict__ didx, int nc, int64_t n, double *__restrict__ out6) {
+    const int64_t tot = (int64_t)nc * n * 3;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = t / (n * 3), a = (t / 3) % n;
+        const int c = (int)(t % 3);
+        const double dim = di[(int64_t)didx[q] * n + a];
+        const double u = cx[t], v = cx[tot + t];
+        double *dst = out6 + (q * n + a) * 6;
+        dst[c] = mx[t] - dim * v;
+        dst[3 + c] = mx[tot + t] + dim * u;
+    }
+}
+
+static int matvec_cplx(mps_system *s, const double *m6, double *out6, int nc, int precision, cudaStream_t st) {
+    const size_t bytes = sizeof(double) * 2 * (size_t)s->max_rhs_c * s->n * 3;
+    if (!s->cx_in) MPS_TRY(dalloc(&s->cx_in, bytes, st));
+    if (!s->cx_out) MPS_TRY(dalloc(&s->cx_out, bytes, st));
+    const int64_t tot = (int64_t)nc * s->n * 3;
+    k_cplx_split<<<grid_for(tot, 256), 256, 0, st>>>(m6, nc, s->n, s->cx_in);
+    count_launch();
+    MPS_CUDA_TRY(cudaGetLastError());
+    MPS_TRY(matvec_real(s, s->cx_in, s->cx_out, 2 * nc, precision, st));
+    k_cplx_join<<<grid_for(tot, 256), 256, 0, st>>>(s->cx_in, s->cx_out, s->diag_im, s->diag_idx, nc, s->n, out6);
+    count_launch();
+    MPS_CUDA_TRY(cudaGetLastError());
+    return MPS_OK;
+}
+
+static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
+    return s->cplx ? matvec_cplx(s, m, out, nrhs, precision, st) : matvec_real(s, m, out, nrhs, precision, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1448,6 +1505,8 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     }
     // the quadrupole operator has no slab term (CQ/MatrixVectorMultiply.m)
     if (d->kind == MPS_DIPOLE_QUADRUPOLE && (!d->quad_tables || d->slab_factor != 0.0)) return MPS_BAD_ARG;
+    // complex permittivities: dipole operator only
+    if (d->lambdap_imag && d->kind != MPS_DIPOLE) return MPS_BAD_ARG;
     for (int k = 0; k < 3; ++k) {
         if (!(d->box[k] > 0) || d->Ngrid[k] < 1) return MPS_BAD_ARG;
         if (d->Ngrid[k] < d->P) return MPS_BAD_ARG;  // the stencil wraps at most once
@@ -1458,14 +1517,16 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     mps_system *s = new mps_system();
     s->stream = st;
     s->n = d->n;
-    s->max_rhs = d->max_rhs;
+    s->cplx = d->lambdap_imag != nullptr;
+    s->max_rhs_c = s->cplx ? d->max_rhs : 0;
+    s->max_rhs = s->cplx ? 2 * d->max_rhs : d->max_rhs;   // real vectors per matvec
     s->n_diag = d->n_diag;
     memcpy(s->box, d->box, sizeof(s->box));
     s->xi = d->xi;
     s->rc = d->rc;
     s->slab_factor = d->slab_factor;
     s->kind = d->kind;
-    s->ndof = d->kind == MPS_DIPOLE_QUADRUPOLE ? 8 : 3;
+    s->ndof = d->kind == MPS_DIPOLE_QUADRUPOLE ? 8 : (s->cplx ? 6 : 3);
     s->gp = make_grid_params(d->Ngrid, d->box, d->xi, d->eta, d->P);
     s->Gc = (int64_t)(s->gp.N[0] / 2 + 1) * s->gp.N[1] * s->gp.N[2];
     const int64_t n = d->n;
@@ -1485,13 +1546,17 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (s->kind == MPS_POLYDISPERSE)
         CR_TRY(cs_diag(d->lambdap, n, d->n_diag, d->radius, d->radius_class, d->n_class,
                        d->radius_class ? d->sizes_tables : nullptr, d->n_tab, d->xi, s->diag, st));
-    else
+    else if (s->cplx) {
+        CR_TRY(dalloc(&s->diag_im, sizeof(double) * n * d->n_diag, st));
+        CR_TRY(build_diag_complex(d->lambdap, d->lambdap_imag, n * d->n_diag, d->perp, s->diag, s->diag_im, st));
+    } else {
         CR_TRY(build_diag(d->lambdap, n * d->n_diag, d->perp, s->diag, st));
-    CR_TRY(dalloc(&s->slab, sizeof(double) * d->max_rhs, st));
-    if (cudaMemsetAsync(s->slab, 0, sizeof(double) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
-    CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * d->max_rhs, st));
-    if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * d->max_rhs) != cudaSuccess) CR_TRY(MPS_NO_MEMORY);
-    if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * d->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
+    }
+    CR_TRY(dalloc(&s->slab, sizeof(double) * s->max_rhs, st));
+    if (cudaMemsetAsync(s->slab, 0, sizeof(double) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
+    CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * s->max_rhs, st));
+    if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * s->max_rhs) != cudaSuccess) CR_TRY(MPS_NO_MEMORY);
+    if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     // cell list + pair CSR
     compute_ncell(d->box, d->rc, s->ncell);
     const int64_t ncells = s->ncell[0] * s->ncell[1] * s->ncell[2];
@@ -1694,9 +1759,11 @@ extern "C" int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t 
     return MPS_OK;
 }
 
+static int rhs_limit(const mps_system *s) { return s->cplx ? s->max_rhs_c : s->max_rhs; }
+
 extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t nrhs, const int32_t *diag_index,
                           int32_t precision, mps_stream_t stream) {
-    if (!sys || !m || !out || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
+    if (!sys || !m || !out || nrhs < 1 || nrhs > rhs_limit(sys)) return MPS_BAD_ARG;
     if (precision != MPS_FP64 && precision != MPS_FP32 && precision != MPS_DF && precision != MPS_FP32_GRAD)
         return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
@@ -1706,7 +1773,7 @@ extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t
 
 extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *out_ri, int32_t diag_index,
                                   mps_stream_t stream) {
-    if (!sys || !m_ri || !out_ri || sys->max_rhs < 2 || sys->kind != MPS_DIPOLE) return MPS_BAD_ARG;
+    if (!sys || !m_ri || !out_ri || sys->max_rhs < 2 || sys->kind != MPS_DIPOLE || sys->cplx) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     int32_t di[2] = {diag_index, diag_index};
     MPS_TRY(upload_diag_idx(sys, di, 2, st));
@@ -1730,7 +1797,7 @@ extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *o
 extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
                          const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
                          mps_stream_t stream) {
-    if (!sys || !b || !x || !opts || nrhs < 1 || nrhs > sys->max_rhs) return MPS_BAD_ARG;
+    if (!sys || !b || !x || !opts || nrhs < 1 || nrhs > rhs_limit(sys)) return MPS_BAD_ARG;
     if (opts->restart < 1 || opts->restart >= kMaxCols || opts->maxit < 1 || !(opts->tol > 0)) return MPS_BAD_ARG;
     if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32 && opts->precision != MPS_DF) return MPS_BAD_ARG;
     if (opts->residual_precision != MPS_FP64 && opts->residual_precision != MPS_DF) return MPS_BAD_ARG;
@@ -1897,7 +1964,7 @@ extern "C" int mps_adjoint_forces(mps_system *sys, const double *m, const double
                                   const double *rvals, int64_t n_tab, int32_t diag_index, double *forces,
                                   double *dE_deps, mps_stream_t stream) {
     if (!sys || !m || !perp || !para || !rvals || n_tab < 2 || !forces) return MPS_BAD_ARG;
-    if (sys->kind != MPS_DIPOLE) return MPS_BAD_ARG;
+    if (sys->kind != MPS_DIPOLE || sys->cplx) return MPS_BAD_ARG;
     if (diag_index < 0 || diag_index >= sys->n_diag) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(ensure_p64(sys, st));

@@ -77,9 +77,22 @@ class SpectralEwaldSystem:
         self._lib = lib
         self._h = C.c_void_p(0)
         self.x = as_device(x).reshape(-1, 3)
-        lam = as_device(lambdap)
-        if lam.dim() == 1:
-            lam = lam.reshape(1, -1)
+        # complex permittivities (frequency-dependent eps, as the MATLAB spectrum drivers allow): vectors become
+        # complex; the device stores them as (Re m, Im m) per particle
+        self.cplx = bool(torch.is_complex(lambdap)) if isinstance(lambdap, torch.Tensor) else \
+            bool(np.iscomplexobj(lambdap))
+        if self.cplx:
+            lc = lambdap.to(device="cuda", dtype=torch.complex128) if isinstance(lambdap, torch.Tensor) else \
+                torch.as_tensor(np.asarray(lambdap, dtype=np.complex128), device="cuda")
+            if lc.dim() == 1:
+                lc = lc.reshape(1, -1)
+            lam = lc.real.contiguous()
+            self.lambdap_imag = lc.imag.contiguous()
+        else:
+            lam = as_device(lambdap)
+            if lam.dim() == 1:
+                lam = lam.reshape(1, -1)
+            self.lambdap_imag = None
         self.lambdap = lam.contiguous()
         self.n = int(self.x.shape[0])
         if self.lambdap.shape[1] != self.n:
@@ -145,6 +158,9 @@ class SpectralEwaldSystem:
         d.radius_class = self.radius_class.data_ptr() if self.radius_class is not None else None
         d.n_class = int(n_class)
         d.sizes_tables = self.sizes_tables.data_ptr() if self.sizes_tables is not None else None
+        d.lambdap_imag = self.lambdap_imag.data_ptr() if self.lambdap_imag is not None else None
+        if self.cplx and self.kind != L.MPS_DIPOLE:
+            raise ValueError("complex permittivities are supported for the dipole operator")
         L.check(lib.mps_system_create(C.byref(d), C.byref(self._h), L.stream_handle()), "mps_system_create")
         np_ = C.c_int64(0)
         nc = (C.c_int64 * 3)()
@@ -202,9 +218,30 @@ class SpectralEwaldSystem:
         arr = (C.c_int32 * nrhs)(*[int(v) for v in diag_index])
         return arr
 
+    # complex vectors (complex permittivities) <-> the device's (Re m, Im m) per particle
+    def _pack(self, v):
+        vc = v.to(device="cuda", dtype=torch.complex128) if isinstance(v, torch.Tensor) else \
+            torch.as_tensor(np.asarray(v, dtype=np.complex128), device="cuda")
+        return torch.cat((vc.real, vc.imag), dim=-1).contiguous()
+
+    @staticmethod
+    def _unpack(v6):
+        return torch.complex(v6[..., :3].contiguous(), v6[..., 3:].contiguous())
+
     def matvec(self, m, precision="fp64", diag_index=None, out=None) -> torch.Tensor:
         """Field at the particles from real moments ``m`` of shape (N,ndof) or (R,N,ndof)
-        (ndof = 3, or 8 for the dipole + quadrupole operator)."""
+        (ndof = 3, or 8 for the dipole + quadrupole operator).  With complex
+        permittivities ``m`` and the result are complex (N,3) / (R,N,3)."""
+        if self.cplx:
+            m6 = self._pack(m)
+            single = m6.dim() == 2
+            m6 = m6.reshape(-1, self.n, 6).contiguous()
+            o6 = torch.empty_like(m6)
+            L.check(self._lib.mps_matvec(self._h, L.dptr(m6), L.dptr(o6), m6.shape[0],
+                                         self._diag_arg(m6.shape[0], diag_index), PRECISIONS[precision],
+                                         L.stream_handle()), "mps_matvec")
+            r = self._unpack(o6)
+            return r[0] if single else r
         m = as_device(m)
         single = m.dim() == 2
         m = m.reshape(-1, self.n, self.ndof).contiguous()
@@ -239,13 +276,18 @@ class SpectralEwaldSystem:
         float32 operator (one FFT pair per vector; it differs from the reference
         operator by ~1e-5, which the refinement removes).
 
-        ``b``, ``x0``: (N,ndof) or (R,N,ndof).  Returns (x, [SolveInfo] * R)."""
-        b = as_device(b)
+        ``b``, ``x0``: (N,ndof) or (R,N,ndof); complex (N,3) / (R,N,3) with complex
+        permittivities.  Returns (x, [SolveInfo] * R)."""
+        nd = 6 if self.cplx else self.ndof
+        b = self._pack(b) if self.cplx else as_device(b)
         single = b.dim() == 2
-        b = b.reshape(-1, self.n, self.ndof).contiguous()
+        b = b.reshape(-1, self.n, nd).contiguous()
         nrhs = b.shape[0]
         x = torch.empty_like(b)
-        x0d = None if x0 is None else as_device(x0).reshape(nrhs, self.n, self.ndof).contiguous()
+        if x0 is None:
+            x0d = None
+        else:
+            x0d = (self._pack(x0) if self.cplx else as_device(x0)).reshape(nrhs, self.n, nd).contiguous()
         opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
                            precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit),
                            residual_policy=int(residual_policy), verify=1 if verify else 0,
@@ -258,4 +300,6 @@ class SpectralEwaldSystem:
             L.check(st, "mps_gmres")
         infos = [SolveInfo(bool(i.converged), float(i.relres), int(i.matvecs_fp64), int(i.matvecs_fp32),
                            int(i.cycles)) for i in info]
+        if self.cplx:
+            x = self._unpack(x)
         return (x[0] if single else x), infos
