@@ -97,6 +97,34 @@ int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, const doubl
                   const double *perp, const double *para, const double *rvals, int64_t n_tab, int32_t with_real,
                   double *E, mps_stream_t stream);
 
+/* Replaces Compute_Field_Quadrupole/RealSpaceTable.m (the tables of the quadrupole field map):
+ * as mps_quad_table, without the r < 2 overlap polynomials (that file comments them all out). */
+int mps_quad_table_probe(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream);
+
+/* Replaces Compute_Field_Quadrupole/FieldMap.m:1-58 with its MatrixVectorMultiply.m:1-80 and
+ * RealSpace.m:1-77: field E and field gradient G at n_e probe points x_e from dipoles and
+ * quadrupoles sq (n_p x 8: S x y z, Q xx xy xz yy yz) at x_p.  EG: n_e x 8 (E then G), both with
+ * FieldMap's sign (-(wave + real)).  tab9: 9 x n_tab device tables on rvals in the order
+ * field_dip_1, field_dip_2, field_quad_1..3, grad_quad_1..4 (mps_real_space_table_probe rows 2-3 and
+ * mps_quad_table_probe).  Other arguments and status codes as mps_field_map; a source exactly at a
+ * probe (d = 0, where the reference divides by zero) is skipped. */
+int mps_field_map_quad(const double *x_e, int64_t n_e, const double *x_p, const double *sq, int64_t n_p,
+                       const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P, const double *eta,
+                       const double *tab9, const double *rvals, int64_t n_tab, int32_t with_real, double *EG,
+                       mps_stream_t stream);
+
+/* Replaces Compute_Field_Sizes/FieldMap.m:1-43 with its ComputeField.m:1-40 and RealSpace.m:1-77:
+ * field at n_e probe points from dipoles p of n_p spheres of radii `radius` (classes radius_class
+ * among n_class distinct radii); the probes are spheres of the smallest radius (ComputeField.m:33).
+ * eta: the scalar spectral splitting; perp / para: the M(M+1)/2 table columns (Ep_perp, Ep_para of
+ * mps_sizes_table, n_tab rows each) on rvals (FieldMap.m uses 0.5 .. rc + 0.01; separations below
+ * rvals[0] or above rvals[n_tab-1] return MPS_TABLE_RANGE).  E = -(wave + real), FieldMap's sign. */
+int mps_field_map_sizes(const double *x_e, int64_t n_e, const double *x_p, const double *radius,
+                        const int32_t *radius_class, int32_t n_class, const double *p, int64_t n_p,
+                        const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P, double eta,
+                        const double *perp, const double *para, const double *rvals, int64_t n_tab,
+                        int32_t with_real, double *E, mps_stream_t stream);
+
 /* Replaces the dipole + quadrupole couplings of Capacitance_Quadrupole/RealSpaceTable.m:171-378.
  * r: n separations (no zero).  tables: 7 x (n+1) float64, rows field_quad_1,
  * field_quad_2, field_quad_3, grad_quad_1, grad_quad_2, grad_quad_3, grad_quad_4,

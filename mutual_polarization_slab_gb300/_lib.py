@@ -27,7 +27,8 @@ EXPORTS = (
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
     "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
     "mps_dipole_forces", "mps_quad_table", "mps_sizes_table", "mps_adjoint_forces",
-    "mps_real_space_table_probe", "mps_field_map",
+    "mps_real_space_table_probe", "mps_field_map", "mps_quad_table_probe", "mps_field_map_quad",
+    "mps_field_map_sizes",
 )
 
 p = C.c_void_p
@@ -94,6 +95,10 @@ _SIGS = {
     "mps_adjoint_forces": (C.c_int, [p, p, p, p, p, i64, i32, p, p, p]),
     "mps_real_space_table_probe": (C.c_int, [p, i64, f64, p, p]),
     "mps_field_map": (C.c_int, [p, i64, p, p, i64, PD, f64, f64, P64, i32, PD, p, p, p, i64, i32, p, p]),
+    "mps_quad_table_probe": (C.c_int, [p, i64, f64, p, p]),
+    "mps_field_map_quad": (C.c_int, [p, i64, p, p, i64, PD, f64, f64, P64, i32, PD, p, p, i64, i32, p, p]),
+    "mps_field_map_sizes": (C.c_int, [p, i64, p, p, p, i32, p, i64, PD, f64, f64, P64, i32, f64, p, p, p, i64, i32,
+                                      p, p]),
 }
 
 _lib = None

@@ -214,6 +214,166 @@ __global__ void __launch_bounds__(256) k_probe_real(const double *__restrict__ x
     }
 }
 
+// Field and field gradient at probe points from the dipoles and quadrupoles of sources within rc
+// (Compute_Field_Quadrupole/RealSpace.m:1-77 over the probe/particle pairs of FieldMap.m:44-48):
+// the couplings A..I of each pair interpolated from the 9 tables (field_dip_1/2, field_quad_1..3,
+// grad_quad_1..4; first row with rvals >= d), out[e] = (E (3), G (5)).  A source at the probe
+// itself (d = 0) is skipped (the reference divides by d there).
+__global__ void __launch_bounds__(256) k_probe_real_quad(const double *__restrict__ xe, int64_t ne,
+                                                         const int64_t *__restrict__ cell_e,
+                                                         const double *__restrict__ xp,
+                                                         const double *__restrict__ sq,
+                                                         const int32_t *__restrict__ sorted,
+                                                         const int32_t *__restrict__ counts,
+                                                         const int64_t *__restrict__ starts, int64_t ncx,
+                                                         int64_t ncy, int64_t ncz, Box3 box, double rc,
+                                                         const double *__restrict__ tab, const double *__restrict__ rv,
+                                                         int64_t ntab, double *__restrict__ out, int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < ne; e += nw) {
+        const int32_t c = (int32_t)(cell_e[3 * e] + ncx * (cell_e[3 * e + 1] + ncy * cell_e[3 * e + 2]));
+        const CellWalk cw = cell_walk(c, lane, counts, starts, ncx, ncy, ncz);
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+            if (j >= cw.total) continue;
+            const int32_t b = sorted[pos];
+            double r[3], d2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double v = xe[3 * e + k] - xp[3 * (int64_t)b + k];
+                v -= box.L[k] * trunc(2.0 * v / box.L[k]);
+                r[k] = v;
+                d2 += v * v;
+            }
+            const double d = sqrt(d2);
+            if (!(d < rc) || !(d > 0.0)) continue;
+            int64_t lo = 1, hi = ntab - 1;
+            if (!(rv[hi] >= d)) {
+                atomicExch(err, 1);
+                continue;
+            }
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (rv[mid] >= d) hi = mid; else lo = mid + 1;
+            }
+            const double rh = rv[lo], rl = rv[lo - 1], span = rh - rl;
+            double cf[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q)
+                cf[q] = tab[q * ntab + lo - 1] * (rh - d) / span + tab[q * ntab + lo] * (d - rl) / span;
+            const double A = cf[0], B = cf[1], Cc = cf[2], D = cf[3], E = cf[4], F = cf[5], Gg = cf[6], H = cf[7],
+                         I = cf[8];
+            const double rx = r[0] / d, ry = r[1] / d, rz = r[2] / d;
+            const double *m = sq + 8 * (int64_t)b;
+            const double Sx = m[0], Sy = m[1], Sz = m[2], Q0 = m[3], Q1 = m[4], Q2 = m[5], Q3 = m[6], Q4 = m[7];
+            const double sr = Sx * rx + Sy * ry + Sz * rz;
+            const double Qr0 = Q0 * rx + Q1 * ry + Q2 * rz;
+            const double Qr1 = Q1 * rx + Q3 * ry + Q4 * rz;
+            const double Qr2 = Q2 * rx + Q4 * ry - (Q0 + Q3) * rz;
+            const double rQr = Q0 * (rx * rx - rz * rz) + 2 * Q1 * rx * ry + 2 * Q2 * rx * rz +
+                               Q3 * (ry * ry - rz * rz) + 2 * Q4 * ry * rz;
+            const double sE = (B - A) * sr - 0.5 * Cc * rQr;
+            acc[0] += A * Sx + sE * rx - D * Qr0;
+            acc[1] += A * Sy + sE * ry - D * Qr1;
+            acc[2] += A * Sz + sE * rz - D * Qr2;
+            const double q5[5] = {rx * rx, rx * ry, rx * rz, ry * ry, ry * rz};
+            const double srs[5] = {2 * Sx * rx, Sx * ry + rx * Sy, Sx * rz + rx * Sz, 2 * Sy * ry, Sy * rz + ry * Sz};
+            const double qq[5] = {4 * Qr0 * rx, 2 * (Qr0 * ry + rx * Qr1), 2 * (Qr0 * rz + rx * Qr2), 4 * Qr1 * ry,
+                                  2 * (Qr1 * rz + ry * Qr2)};
+            const double Qv[5] = {Q0, Q1, Q2, Q3, Q4};
+            const double cq = Cc * sr + 0.5 * I * rQr;
+            const double di = (D + E) * sr + 0.5 * (F + H) * rQr;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                double v = cq * q5[k] + D * srs[k] + 0.5 * (Gg * Qv[k] + H * qq[k]);
+                if (k == 0 || k == 3) v += di;
+                acc[3 + k] += v;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) out[8 * e + k] = acc[k];
+    }
+}
+
+// Polydisperse field map, real space (Compute_Field_Sizes/RealSpace.m:1-77): probes are spheres of the
+// smallest radius (class cmin), so the couplings of a probe/source pair come from the table column
+// of the classes (cmin, cls[b]) (column order of CS/RealSpaceTable.m: i <= j, row-major over i);
+// rvals need not start at 0: a separation below rvals[0] or above rvals[ntab-1] is out of the table.
+__global__ void __launch_bounds__(256) k_probe_real_cs(const double *__restrict__ xe, int64_t ne,
+                                                       const int64_t *__restrict__ cell_e,
+                                                       const double *__restrict__ xp, const double *__restrict__ p,
+                                                       const int32_t *__restrict__ cls, int32_t cmin, int32_t M,
+                                                       const int32_t *__restrict__ sorted,
+                                                       const int32_t *__restrict__ counts,
+                                                       const int64_t *__restrict__ starts, int64_t ncx, int64_t ncy,
+                                                       int64_t ncz, Box3 box, double rc,
+                                                       const double *__restrict__ perp,
+                                                       const double *__restrict__ para,
+                                                       const double *__restrict__ rv, int64_t ntab,
+                                                       double *__restrict__ out, int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < ne; e += nw) {
+        const int32_t c = (int32_t)(cell_e[3 * e] + ncx * (cell_e[3 * e + 1] + ncy * cell_e[3 * e + 2]));
+        const CellWalk cw = cell_walk(c, lane, counts, starts, ncx, ncy, ncz);
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int j0 = 0; j0 < cw.total; j0 += 32) {
+            const int j = j0 + lane;
+            int o;
+            int64_t pos;
+            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+            if (j >= cw.total) continue;
+            const int32_t b = sorted[pos];
+            double r[3], d2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double v = xe[3 * e + k] - xp[3 * (int64_t)b + k];
+                v -= box.L[k] * trunc(2.0 * v / box.L[k]);
+                r[k] = v;
+                d2 += v * v;
+            }
+            const double d = sqrt(d2);
+            if (!(d < rc)) continue;
+            if (!(d > rv[0]) || !(rv[ntab - 1] >= d)) {
+                atomicExch(err, 1);
+                continue;
+            }
+            int64_t lo = 1, hi = ntab - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (rv[mid] >= d) hi = mid; else lo = mid + 1;
+            }
+            const int32_t ci = cmin < cls[b] ? cmin : cls[b], cj = cmin < cls[b] ? cls[b] : cmin;
+            const int64_t col = (int64_t)ci * M - (int64_t)ci * (ci - 1) / 2 + (cj - ci);
+            const double *tp = perp + col * ntab, *ta = para + col * ntab;
+            const double rh = rv[lo], rl = rv[lo - 1], span = rh - rl;
+            const double A = tp[lo - 1] * (rh - d) / span + tp[lo] * (d - rl) / span;
+            const double B = ta[lo - 1] * (rh - d) / span + ta[lo] * (d - rl) / span;
+            const double *m = p + 3 * (int64_t)b;
+            const double mr = (m[0] * r[0] + m[1] * r[1] + m[2] * r[2]) / d;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[k] += A * (m[k] - mr * r[k] / d) + B * mr * r[k] / d;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) out[3 * e + k] = acc[k];
+    }
+}
+
 // Candidate counts in emission-slot order: slot(s,o) = 27*start[c] + o*count[c] + (s - start[c]).
 __global__ void k_candidate_slots(const int32_t *__restrict__ sorted, const int32_t *__restrict__ lin,
                                   const int32_t *__restrict__ counts, const int64_t *__restrict__ starts, int64_t n,
@@ -1002,6 +1162,98 @@ int probe_real_space(const double *xe, int64_t ne, const double *xp, const doubl
         k_probe_real<<<grid_for(ne * 32, 256, 152 * 64), 256, 0, s>>>(
             xe, ne, cell_e, xp, p, cb.sorted, cb.counts, cb.starts, ncell[0], ncell[1], ncell[2], b3, rc, perp, para,
             rv, ntab, out, err);
+        if (cudaGetLastError() != cudaSuccess) rcode = MPS_CUDA_ERR;
+    }
+    int herr = 0;
+    if (!rcode && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                   cudaStreamSynchronize(s) != cudaSuccess))
+        rcode = MPS_CUDA_ERR;
+    cleanup();
+    if (!rcode && herr) rcode = MPS_TABLE_RANGE;
+    return rcode;
+}
+
+
+int probe_real_space_quad(const double *xe, int64_t ne, const double *xp, const double *sq, int64_t np,
+                          const double *box, double rc, const double *tab9, const double *rv, int64_t ntab,
+                          double *out, cudaStream_t s) {
+    if (ne == 0) return MPS_OK;
+    if (ntab < 2) return MPS_BAD_ARG;
+    int64_t ncell[3];
+    compute_ncell(box, rc, ncell);
+    const int64_t ncells = ncell[0] * ncell[1] * ncell[2];
+    int64_t *cell_p = nullptr, *cell_e = nullptr;
+    void *bins = nullptr;
+    int *err = nullptr;
+    auto cleanup = [&]() {
+        if (cell_p) cudaFreeAsync(cell_p, s);
+        if (cell_e) cudaFreeAsync(cell_e, s);
+        if (bins) cudaFreeAsync(bins, s);
+        if (err) cudaFreeAsync(err, s);
+    };
+    if (cudaMallocAsync((void **)&cell_p, sizeof(int64_t) * 3 * (np > 0 ? np : 1), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&cell_e, sizeof(int64_t) * 3 * ne, s) != cudaSuccess ||
+        cudaMallocAsync(&bins, cell_bins_bytes(np, ncells), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&err, sizeof(int), s) != cudaSuccess) {
+        cleanup();
+        return MPS_NO_MEMORY;
+    }
+    int rcode = cudaMemsetAsync(err, 0, sizeof(int), s) == cudaSuccess ? MPS_OK : MPS_CUDA_ERR;
+    CellBins cb;
+    if (!rcode) rcode = cell_assign(xp, np, box, ncell, cell_p, s);
+    if (!rcode) rcode = cell_bins_build(cell_p, np, ncell, bins, cb, s);
+    if (!rcode) rcode = cell_assign(xe, ne, box, ncell, cell_e, s);
+    if (!rcode) {
+        Box3 b3{{box[0], box[1], box[2]}};
+        k_probe_real_quad<<<grid_for(ne * 32, 256, 152 * 64), 256, 0, s>>>(
+            xe, ne, cell_e, xp, sq, cb.sorted, cb.counts, cb.starts, ncell[0], ncell[1], ncell[2], b3, rc, tab9, rv,
+            ntab, out, err);
+        if (cudaGetLastError() != cudaSuccess) rcode = MPS_CUDA_ERR;
+    }
+    int herr = 0;
+    if (!rcode && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                   cudaStreamSynchronize(s) != cudaSuccess))
+        rcode = MPS_CUDA_ERR;
+    cleanup();
+    if (!rcode && herr) rcode = MPS_TABLE_RANGE;
+    return rcode;
+}
+
+
+int probe_real_space_cs(const double *xe, int64_t ne, const double *xp, const double *p, const int32_t *cls,
+                        int32_t cmin, int32_t M, int64_t np, const double *box, double rc, const double *perp,
+                        const double *para, const double *rv, int64_t ntab, double *out, cudaStream_t s) {
+    if (ne == 0) return MPS_OK;
+    if (ntab < 2 || M < 1 || cmin < 0 || cmin >= M) return MPS_BAD_ARG;
+    int64_t ncell[3];
+    compute_ncell(box, rc, ncell);
+    const int64_t ncells = ncell[0] * ncell[1] * ncell[2];
+    int64_t *cell_p = nullptr, *cell_e = nullptr;
+    void *bins = nullptr;
+    int *err = nullptr;
+    auto cleanup = [&]() {
+        if (cell_p) cudaFreeAsync(cell_p, s);
+        if (cell_e) cudaFreeAsync(cell_e, s);
+        if (bins) cudaFreeAsync(bins, s);
+        if (err) cudaFreeAsync(err, s);
+    };
+    if (cudaMallocAsync((void **)&cell_p, sizeof(int64_t) * 3 * (np > 0 ? np : 1), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&cell_e, sizeof(int64_t) * 3 * ne, s) != cudaSuccess ||
+        cudaMallocAsync(&bins, cell_bins_bytes(np, ncells), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&err, sizeof(int), s) != cudaSuccess) {
+        cleanup();
+        return MPS_NO_MEMORY;
+    }
+    int rcode = cudaMemsetAsync(err, 0, sizeof(int), s) == cudaSuccess ? MPS_OK : MPS_CUDA_ERR;
+    CellBins cb;
+    if (!rcode) rcode = cell_assign(xp, np, box, ncell, cell_p, s);
+    if (!rcode) rcode = cell_bins_build(cell_p, np, ncell, bins, cb, s);
+    if (!rcode) rcode = cell_assign(xe, ne, box, ncell, cell_e, s);
+    if (!rcode) {
+        Box3 b3{{box[0], box[1], box[2]}};
+        k_probe_real_cs<<<grid_for(ne * 32, 256, 152 * 64), 256, 0, s>>>(
+            xe, ne, cell_e, xp, p, cls, cmin, M, cb.sorted, cb.counts, cb.starts, ncell[0], ncell[1], ncell[2], b3,
+            rc, perp, para, rv, ntab, out, err);
         if (cudaGetLastError() != cudaSuccess) rcode = MPS_CUDA_ERR;
     }
     int herr = 0;

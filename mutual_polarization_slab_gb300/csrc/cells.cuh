@@ -70,4 +70,16 @@ int probe_real_space(const double *xe, int64_t ne, const double *xp, const doubl
                      double rc, const double *perp, const double *para, const double *rv, int64_t ntab, double *out,
                      cudaStream_t s);
 
+// Field and gradient (ne x 8: E then G xx xy xz yy yz) at probes from source dipoles + quadrupoles
+// sq (np x 8) within rc; tab9: the 9 coupling tables (9 x ntab) on rv (Compute_Field_Quadrupole/RealSpace.m).
+int probe_real_space_quad(const double *xe, int64_t ne, const double *xp, const double *sq, int64_t np,
+                          const double *box, double rc, const double *tab9, const double *rv, int64_t ntab,
+                          double *out, cudaStream_t s);
+
+// Real-space field (ne x 3) at probes of radius class cmin from source dipoles p (np x 3) of classes cls
+// within rc; perp/para: M(M+1)/2 columns of ntab rows on rv (Compute_Field_Sizes/RealSpace.m).
+int probe_real_space_cs(const double *xe, int64_t ne, const double *xp, const double *p, const int32_t *cls,
+                        int32_t cmin, int32_t M, int64_t np, const double *box, double rc, const double *perp,
+                        const double *para, const double *rv, int64_t ntab, double *out, cudaStream_t s);
+
 }  // namespace mps

@@ -200,8 +200,9 @@ __device__ double quad_overlap(int t, double r) {
     }
 }
 
+// overlap = 0: no r < 2 overlap polynomial (Compute_Field_Quadrupole/RealSpaceTable.m comments them all out).
 __global__ void k_quad_tables(const double *__restrict__ r, int64_t n, double xi, QSet S, double self_gq2,
-                              double *__restrict__ out) {
+                              int overlap, double *__restrict__ out) {
     const int64_t row = n + 1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
         if (i == 0) {
@@ -222,7 +223,7 @@ __global__ void k_quad_tables(const double *__restrict__ r, int64_t n, double xi
                         qhorner(T.E[2], T.nE, rv) * e0);
             v += T.cF / pow(rv, (double)T.pF) *
                  (qhorner(T.F[0], T.nF, rv) * fp + qhorner(T.F[1], T.nF, rv) * fm + qhorner(T.F[2], T.nF, rv) * f0);
-            if (rv < 2.0) v += quad_overlap(t, rv);
+            if (rv < 2.0 && overlap) v += quad_overlap(t, rv);
             out[t * row + i] = v;
         }
     }
@@ -246,7 +247,17 @@ extern "C" int mps_quad_table(const double *r, int64_t n, double xi, double *tab
     QSet S;
     build_quad_specs(xi, S);
     cudaStream_t s = (cudaStream_t)stream;
-    k_quad_tables<<<grid_for(n + 1, 256), 256, 0, s>>>(r, n, xi, S, quad_self_value(xi), tables);
+    k_quad_tables<<<grid_for(n + 1, 256), 256, 0, s>>>(r, n, xi, S, quad_self_value(xi), 1, tables);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+extern "C" int mps_quad_table_probe(const double *r, int64_t n, double xi, double *tables, mps_stream_t stream) {
+    if (n < 0 || !tables || (n > 0 && !r) || !(xi > 0)) return MPS_BAD_ARG;
+    QSet S;
+    build_quad_specs(xi, S);
+    cudaStream_t s = (cudaStream_t)stream;
+    k_quad_tables<<<grid_for(n + 1, 256), 256, 0, s>>>(r, n, xi, S, quad_self_value(xi), 0, tables);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

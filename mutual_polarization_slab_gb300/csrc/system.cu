@@ -1941,6 +1941,180 @@ extern "C" int mps_field_map(const double *x_e, int64_t n_e, const double *x_p, 
     return rc_;
 }
 
+extern "C" int mps_field_map_quad(const double *x_e, int64_t n_e, const double *x_p, const double *sq, int64_t n_p,
+                                  const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P,
+                                  const double *eta, const double *tab9, const double *rvals, int64_t n_tab,
+                                  int32_t with_real, double *EG, mps_stream_t stream) {
+    if (n_e < 0 || n_p < 0 || !box || !Ngrid || !eta || !(xi > 0) || !(rc > 0) || P < 1 || n_tab < 2) return MPS_BAD_ARG;
+    if ((n_e > 0 && (!x_e || !EG)) || (n_p > 0 && (!x_p || !sq)) || !tab9 || !rvals) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (Ngrid[d] < P || !(box[d] > 0)) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (rc > 0.5 * box[d]) return MPS_RC_GT_HALF_BOX;
+    if (n_e == 0) return MPS_OK;
+    configure_pool_once();
+    cudaStream_t st = (cudaStream_t)stream;
+    const GridParams gp = make_grid_params(Ngrid, box, xi, eta, P);
+    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
+    int32_t *start_p = nullptr, *start_e = nullptr;
+    double *w_p = nullptr, *w_e = nullptr, *grid = nullptr, *spec = nullptr, *kc = nullptr, *wave = nullptr,
+           *real = nullptr;
+    void *work = nullptr;
+    auto cleanup = [&]() {
+        void *ptrs[] = {start_p, start_e, w_p, w_e, grid, spec, kc, wave, real, work};
+        for (void *q : ptrs)
+            if (q) cudaFreeAsync(q, st);
+    };
+    int rc_ = dalloc(&start_p, sizeof(int32_t) * 3 * (size_t)(n_p > 0 ? n_p : 1), st);
+    if (!rc_) rc_ = dalloc(&w_p, sizeof(double) * 3 * (size_t)P * (n_p > 0 ? n_p : 1), st);
+    if (!rc_) rc_ = dalloc(&start_e, sizeof(int32_t) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&w_e, sizeof(double) * 3 * (size_t)P * n_e, st);
+    if (!rc_) rc_ = dalloc(&grid, sizeof(double) * 8 * (size_t)gp.G, st);
+    if (!rc_) rc_ = dalloc(&spec, sizeof(double) * 2 * 8 * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&kc, sizeof(double) * 4 * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&wave, sizeof(double) * 8 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&real, sizeof(double) * 8 * (size_t)n_e, st);
+    // wave space: the 8 source grids, D2Z, the dipole/quadrupole scale, Z2D, contract at the probes
+    if (!rc_) rc_ = grid_geometry(x_p, n_p, gp, start_p, w_p, nullptr, st);
+    if (!rc_ && n_p > 0) rc_ = spread_gen<double>(sq, n_p, 1, 8, start_p, w_p, gp, grid, st);
+    if (!rc_ && n_p == 0 && cudaMemsetAsync(grid, 0, sizeof(double) * 8 * (size_t)gp.G, st) != cudaSuccess)
+        rc_ = MPS_CUDA_ERR;
+    if (!rc_) rc_ = quad_kcoef(gp, kc, nullptr, st);
+    CachedPlan fwd{}, inv{};
+    if (!rc_) rc_ = get_plan(CUFFT_D2Z, gp, 8, &fwd);
+    if (!rc_) rc_ = get_plan(CUFFT_Z2D, gp, 8, &inv);
+    if (!rc_) rc_ = dalloc(&work, std::max(fwd.work, inv.work) + 16, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(fwd.h, work) != CUFFT_SUCCESS || cufftSetStream(fwd.h, st) != CUFFT_SUCCESS ||
+            cufftExecD2Z(fwd.h, (cufftDoubleReal *)grid, (cufftDoubleComplex *)spec) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) rc_ = scale_quad<double>(spec, 1, gp, kc, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(inv.h, work) != CUFFT_SUCCESS || cufftSetStream(inv.h, st) != CUFFT_SUCCESS ||
+            cufftExecZ2D(inv.h, (cufftDoubleComplex *)spec, (cufftDoubleReal *)grid) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) rc_ = grid_geometry(x_e, n_e, gp, start_e, w_e, nullptr, st);
+    if (!rc_) rc_ = contract_gen<double>(grid, n_e, 1, 8, start_e, w_e, gp, wave, st);
+    const bool do_real = with_real && n_p > 0;
+    if (!rc_ && do_real)
+        rc_ = probe_real_space_quad(x_e, n_e, x_p, sq, n_p, box, rc, tab9, rvals, n_tab, real, st);
+    if (!rc_ && !do_real && cudaMemsetAsync(real, 0, sizeof(double) * 8 * (size_t)n_e, st) != cudaSuccess)
+        rc_ = MPS_CUDA_ERR;
+    if (!rc_) {
+        k_field_combine<<<grid_for(8 * n_e, 256), 256, 0, st>>>(wave, real, 8 * n_e, EG);
+        count_launch();
+        if (cudaGetLastError() != cudaSuccess) rc_ = MPS_CUDA_ERR;
+    }
+    cleanup();
+    return rc_;
+}
+
+__global__ void k_fill_value(double *__restrict__ a, int64_t n, double v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+extern "C" int mps_field_map_sizes(const double *x_e, int64_t n_e, const double *x_p, const double *radius,
+                                   const int32_t *radius_class, int32_t n_class, const double *p, int64_t n_p,
+                                   const double *box, double xi, double rc, const int64_t *Ngrid, int32_t P,
+                                   double eta, const double *perp, const double *para, const double *rvals,
+                                   int64_t n_tab, int32_t with_real, double *E, mps_stream_t stream) {
+    if (n_e < 0 || n_p < 1 || !box || !Ngrid || !(xi > 0) || !(rc > 0) || P < 1 || !(eta > 0) || n_tab < 2 ||
+        n_class < 1)
+        return MPS_BAD_ARG;
+    if ((n_e > 0 && (!x_e || !E)) || !x_p || !p || !radius || !radius_class || !perp || !para || !rvals)
+        return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (Ngrid[d] < P || !(box[d] > 0)) return MPS_BAD_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (rc > 0.5 * box[d]) return MPS_RC_GT_HALF_BOX;
+    if (n_e == 0) return MPS_OK;
+    configure_pool_once();
+    cudaStream_t st = (cudaStream_t)stream;
+    const double eta3[3] = {eta, eta, eta};
+    const GridParams gp = make_grid_params(Ngrid, box, xi, eta3, P);
+    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
+    const int64_t P3 = (int64_t)P * P * P;
+    // probes are spheres of the smallest radius (Compute_Field_Sizes/ComputeField.m:33, RealSpace.m:7-8):
+    // the class and radius of the particle with the smallest radius (first one on ties, as min does)
+    std::vector<double> hr(n_p);
+    std::vector<int32_t> hc(n_p);
+    MPS_CUDA_TRY(cudaMemcpyAsync(hr.data(), radius, sizeof(double) * n_p, cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaMemcpyAsync(hc.data(), radius_class, sizeof(int32_t) * n_p, cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    int64_t imin = 0;
+    for (int64_t i = 1; i < n_p; ++i)
+        if (hr[i] < hr[imin]) imin = i;
+    const double a_min = hr[imin];
+    const int32_t cmin = hc[imin];
+    if (cmin < 0 || cmin >= n_class) return MPS_BAD_ARG;
+    int32_t *start_p = nullptr, *start_e = nullptr;
+    double *base_p = nullptr, *base_e = nullptr, *g_p = nullptr, *g_e = nullptr, *rad_e = nullptr, *grid = nullptr,
+           *spec = nullptr, *hcoef = nullptr, *wave = nullptr, *real = nullptr;
+    void *work = nullptr;
+    auto cleanup = [&]() {
+        void *ptrs[] = {start_p, start_e, base_p, base_e, g_p, g_e, rad_e, grid, spec, hcoef, wave, real, work};
+        for (void *q : ptrs)
+            if (q) cudaFreeAsync(q, st);
+    };
+    int rc_ = dalloc(&start_p, sizeof(int32_t) * 3 * (size_t)n_p, st);
+    if (!rc_) rc_ = dalloc(&base_p, sizeof(double) * 3 * (size_t)n_p, st);
+    if (!rc_) rc_ = dalloc(&g_p, sizeof(double) * (size_t)(n_p * P3), st);
+    if (!rc_) rc_ = dalloc(&start_e, sizeof(int32_t) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&base_e, sizeof(double) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&g_e, sizeof(double) * (size_t)(n_e * P3), st);
+    if (!rc_) rc_ = dalloc(&rad_e, sizeof(double) * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&grid, sizeof(double) * (size_t)gp.G, st);
+    if (!rc_) rc_ = dalloc(&spec, sizeof(double) * 2 * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&hcoef, sizeof(double) * (size_t)Gc, st);
+    if (!rc_) rc_ = dalloc(&wave, sizeof(double) * 3 * (size_t)n_e, st);
+    if (!rc_) rc_ = dalloc(&real, sizeof(double) * 3 * (size_t)n_e, st);
+    // wave space: scalar grid of the sources, D2Z, exp(-(1-eta) q^2/4 xi^2)/q^2, Z2D, contract at the probes
+    if (!rc_) rc_ = cs_geometry(x_p, n_p, gp, radius, xi, eta, start_p, base_p, g_p, nullptr, st);
+    if (!rc_) rc_ = spread_cs<double>(p, n_p, 1, start_p, base_p, g_p, gp, grid, st);
+    if (!rc_) rc_ = cs_green(gp, eta, xi, hcoef, nullptr, st);
+    CachedPlan fwd{}, inv{};
+    if (!rc_) rc_ = get_plan(CUFFT_D2Z, gp, 1, &fwd);
+    if (!rc_) rc_ = get_plan(CUFFT_Z2D, gp, 1, &inv);
+    if (!rc_) rc_ = dalloc(&work, std::max(fwd.work, inv.work) + 16, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(fwd.h, work) != CUFFT_SUCCESS || cufftSetStream(fwd.h, st) != CUFFT_SUCCESS ||
+            cufftExecD2Z(fwd.h, (cufftDoubleReal *)grid, (cufftDoubleComplex *)spec) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) rc_ = scale_cs<double>(spec, 1, gp, hcoef, st);
+    if (!rc_) {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (cufftSetWorkArea(inv.h, work) != CUFFT_SUCCESS || cufftSetStream(inv.h, st) != CUFFT_SUCCESS ||
+            cufftExecZ2D(inv.h, (cufftDoubleComplex *)spec, (cufftDoubleReal *)grid) != CUFFT_SUCCESS)
+            rc_ = MPS_CUFFT_ERR;
+    }
+    if (!rc_) {
+        k_fill_value<<<grid_for(n_e, 256), 256, 0, st>>>(rad_e, n_e, a_min);
+        count_launch();
+        if (cudaGetLastError() != cudaSuccess) rc_ = MPS_CUDA_ERR;
+    }
+    if (!rc_) rc_ = cs_geometry(x_e, n_e, gp, rad_e, xi, eta, start_e, base_e, g_e, nullptr, st);
+    if (!rc_) rc_ = contract_cs<double>(grid, n_e, 1, start_e, base_e, g_e, gp, wave, st);
+    if (!rc_ && with_real)
+        rc_ = probe_real_space_cs(x_e, n_e, x_p, p, radius_class, cmin, n_class, n_p, box, rc, perp, para, rvals,
+                                  n_tab, real, st);
+    if (!rc_ && !with_real && cudaMemsetAsync(real, 0, sizeof(double) * 3 * (size_t)n_e, st) != cudaSuccess)
+        rc_ = MPS_CUDA_ERR;
+    if (!rc_) {
+        k_field_combine<<<grid_for(3 * n_e, 256), 256, 0, st>>>(wave, real, 3 * n_e, E);
+        count_launch();
+        if (cudaGetLastError() != cudaSuccess) rc_ = MPS_CUDA_ERR;
+    }
+    cleanup();
+    return rc_;
+}
+
 extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms) {
     if (!sys || !tile_depth || !ms) return MPS_BAD_ARG;
     tile_depth[0] = sys->tb64.tz;

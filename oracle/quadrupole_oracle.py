@@ -282,9 +282,16 @@ def real_space_quad(x, S, Q, lam, box, pairs, rc, tables, rvals):
     d = np.sqrt(np.sum(r * r, axis=1))
     keep = d < rc
     p1, p2, r, d = p1[keep], p2[keep], r[keep], d[keep]
-    r = r / d[:, None]
+    dE, dG = quad_pair_terms(r / d[:, None], d, S[p2], Q[p2], tables, rvals)
+    np.add.at(E, p1, dE)
+    np.add.at(G, p1, dG)
+    return E, G
+
+
+def quad_pair_terms(r, d, Sj, Qj, tables, rvals):
+    """Field and gradient contributions of sources (Sj, Qj) at unit vectors r (target minus
+    source) and separations d (CQ/RealSpace.m:56-99, Compute_Field_Quadrupole/RealSpace.m:53-73)."""
     A, B, C, D, Ec, F, Gc, H, I = _lerp_all(tables, rvals, d)
-    Sj, Qj = S[p2], Q[p2]
     rx, ry, rz = r[:, 0], r[:, 1], r[:, 2]
     sr = np.sum(Sj * r, axis=1)
     q5 = np.stack((rx * rx, rx * ry, rx * rz, ry * ry, ry * rz), axis=1)   # rr in 5-component form
@@ -304,9 +311,7 @@ def real_space_quad(x, S, Q, lam, box, pairs, rc, tables, rvals):
     dG = (C * sr)[:, None] * q5 + D[:, None] * (Sr + rS) + ((D + Ec) * sr)[:, None] * i5 \
         + 0.5 * (F[:, None] * IrrQ + Gc[:, None] * Qj + H[:, None] * (IrrQ + 2 * Qrr + 2 * rrQ)
                  + (I * rQr)[:, None] * q5)
-    np.add.at(E, p1, dE)
-    np.add.at(G, p1, dG)
-    return E, G
+    return dE, dG
 
 
 class QuadGeometry:

@@ -90,3 +90,65 @@ def test_field_map_gpu_vs_oracle():
 
     with pytest.raises(ValueError):
         fm.field_map(x_e, x_p, p, box, 0.2)      # rc = 13.1 > L/2
+
+
+@pytest.mark.gpu
+def test_field_map_quadrupole_gpu_vs_oracle():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("CUDA device required")
+    from mutual_polarization_slab_gb300 import fieldmap as fm
+
+    xi = 0.8
+    r = np.arange(1, 100001, dtype=np.float64) * 1e-4
+    t9 = fm.quad_tables_probe(r, xi).cpu().numpy()
+    ot = fo.quad_tables_probe(r, xi)
+    from oracle import quadrupole_oracle as qo
+    # without the overlap polynomials the tables are differences of terms growing like r^-5 at small r:
+    # below r ~ 0.1 both sides are rounding noise of those terms (also in the reference), so the
+    # comparison covers r >= 0.1 and the probes keep 0.2 from every centre
+    far = np.concatenate(([True], r >= 0.1))
+    for i, name in enumerate(qo.TABLE_ORDER):
+        np.testing.assert_allclose(t9[i][far], ot[name][far], rtol=1e-9, atol=1e-12 * np.abs(ot[name][far]).max())
+
+    x_e, x_p, p, box = _case(n_p=200, n_e=300)
+    d = x_e[:, None, :] - x_p[None, :, :]
+    d -= box * np.trunc(2 * d / box)
+    x_e = x_e[np.sqrt((d ** 2).sum(-1)).min(1) > 0.2]
+    Q = np.random.default_rng(4).standard_normal((200, 5))
+    E, G = fm.field_map_quadrupole(x_e, x_p, p, Q, box, xi, return_gradient=True)
+    oE, oG = fo.field_map_quadrupole(x_e, x_p, p, Q, box, xi)
+    assert np.abs(E - oE.real).max() <= 1e-10 * np.abs(oE.real).max()
+    assert np.abs(G - oG.real).max() <= 1e-10 * np.abs(oG.real).max()
+    assert np.array_equal(fm.field_map_quadrupole(x_e, x_p, p, Q, box, xi), E) or \
+        np.abs(fm.field_map_quadrupole(x_e, x_p, p, Q, box, xi) - E).max() <= 1e-13 * np.abs(E).max()
+
+
+@pytest.mark.gpu
+def test_field_map_sizes_gpu_vs_oracle():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("CUDA device required")
+    from mutual_polarization_slab_gb300 import fieldmap as fm
+
+    rng = np.random.default_rng(6)
+    box = np.array([12.0, 13.0, 14.0])
+    n_p, n_e = 150, 250
+    x_p = rng.uniform(0, 1, (n_p, 3)) * box
+    a = rng.choice([0.7, 1.0, 1.3], n_p)
+    p = rng.standard_normal((n_p, 3))
+    # probes at least 0.5 from every sphere centre (the reference's table starts at 0.5)
+    x_e = []
+    while len(x_e) < n_e:
+        c = rng.uniform(0, 1, 3) * box
+        d = c - x_p
+        d -= box * np.trunc(2 * d / box)
+        if np.sqrt((d ** 2).sum(1)).min() > 0.55:
+            x_e.append(c)
+    x_e = np.array(x_e)
+    xi = 0.8
+    E = fm.field_map_sizes(x_e, x_p, a, p, box, xi)
+    ref = fo.field_map_sizes(x_e, x_p, a, p, box, xi)
+    assert np.abs(E - ref).max() <= 1e-10 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        fm.field_map_sizes(x_p[:3] + 0.1, x_p, a, p, box, xi)     # probe 0.17 from a centre: outside the table
