@@ -113,6 +113,10 @@ struct mps_system {
     int32_t *order = nullptr;        // particle ids sorted by (cell, id): spatial visiting order
     dfv *wdf = nullptr;              // double-float copy of w64 (built by the first double-float matvec)
     float *m32 = nullptr;            // float copy of the moments for the float32 pair sum (scratch)
+    // side stream: the float32 pair sum runs beside the spread / FFT / contraction of the same matvec
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    double *rs_buf = nullptr;        // max_rhs x n x 3: the pair-sum part of a float32 matvec
     // complex permittivities: vectors are (Re m, Im m) per particle (ndof 6); the real operator runs on the
     // 2 nc real vectors [Re m_0..Re m_{nc-1}, Im m_0..Im m_{nc-1}] and the imaginary diagonal couples them
     bool cplx = false;
@@ -154,6 +158,8 @@ struct mps_system {
 
 static void free_system(mps_system *s) {
     if (!s) return;
+    // a matvec that failed between fork and join may leave pair-sum work on the side stream
+    if (s->side) cudaStreamSynchronize(s->side);
     for (auto &e : s->pending)
         for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
     for (auto &e : s->spare)
@@ -168,6 +174,10 @@ static void free_system(mps_system *s) {
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
+    if (s->rs_buf) cudaFreeAsync(s->rs_buf, s->stream);
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     tile_bins_free(s->tb64, s->stream);
     tile_bins_free(s->tb32, s->stream);
     if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
@@ -699,6 +709,8 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
 }
 
 // Gradient form of the float32 operator (gradop.cu): one scalar grid per vector.
+__global__ void k_axpy1(const double *__restrict__ x, double *__restrict__ y, int64_t total);
+
 static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     // the gradient form exists for the dipole operator only: the others run their own float32 operator
     if (s->kind == MPS_DIPOLE_QUADRUPOLE) return matvec_quad<float>(s, m, out, nrhs, st);
@@ -723,7 +735,28 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
+    // the pair sum is independent of the wave-space stages: unless the stages are being timed, it runs on
+    // the side stream into rs_buf and is added after the contraction (MPS_PAIR_STREAM=same keeps it on the
+    // matvec's stream after the contraction, for A/B timing)
+    const char *ps = getenv("MPS_PAIR_STREAM");
+    const bool beside = ev == nullptr && !(ps && strcmp(ps, "same") == 0);
+    if (beside) {
+        if (!s->side) {
+            MPS_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+            MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+            MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+        }
+        if (!s->rs_buf) MPS_TRY(dalloc(&s->rs_buf, sizeof(double) * 3 * (size_t)s->n * s->max_rhs, st));
+        if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * 3 * (size_t)s->n * s->max_rhs, st));
+    }
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    if (beside) {
+        MPS_CUDA_TRY(cudaEventRecord(s->ev_fork, st));
+        MPS_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+        MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx,
+                                   s->slab, false, s->order, s->side));
+        MPS_CUDA_TRY(cudaEventRecord(s->ev_join, s->side));
+    }
     STAGE_MARK(1);
     MPS_TRY(spread_grad_tiled(m, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->grid32, st));
     STAGE_MARK(2);
@@ -746,7 +779,15 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
         }
     }
     STAGE_MARK(6);
-    MPS_TRY(real_space_f32(s, m, out, nrhs, st));
+    if (beside) {
+        MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
+        const int64_t tot = (int64_t)nrhs * s->n * 3;
+        k_axpy1<<<grid_for(tot, 256), 256, 0, st>>>(s->rs_buf, out, tot);
+        count_launch();
+        MPS_CUDA_TRY(cudaGetLastError());
+    } else {
+        MPS_TRY(real_space_f32(s, m, out, nrhs, st));
+    }
     STAGE_MARK(7);
     return MPS_OK;
 }
