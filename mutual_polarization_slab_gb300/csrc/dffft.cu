@@ -44,12 +44,18 @@ __device__ __forceinline__ dfr fts(float a, float b) {
     const float s = __fadd_rn(a, b);
     return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
+// Sums and products inside a butterfly leave their result unnormalised: (s, e)
+// with s the rounded leading sum (product) and e its exact rounding error plus
+// the companion terms, |e| a few ulp of s.  The two-sum and the FMA residual are
+// exact for any leading parts, so an unnormalised operand costs at most a couple
+// of bits of the ~2^-48 accuracy; values are normalised once when a stage stores
+// them (st4, re_s, nim_s), not after every operation.
 __device__ __forceinline__ dfr dadd(dfr a, dfr b) {
     const float s = __fadd_rn(a.hi, b.hi);
     const float bb = __fsub_rn(s, a.hi);
     float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
     e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-    return fts(s, e);
+    return {s, e};
 }
 __device__ __forceinline__ dfr dneg(dfr a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ dfr dsub(dfr a, dfr b) { return dadd(a, dneg(b)); }
@@ -58,8 +64,9 @@ __device__ __forceinline__ dfr dmul(dfr a, dfr b) {
     float e = __fmaf_rn(a.hi, b.hi, -p);
     e = __fmaf_rn(a.hi, b.lo, e);
     e = __fmaf_rn(a.lo, b.hi, e);
-    return fts(p, e);
+    return {p, e};
 }
+__device__ __forceinline__ dfr dnorm(dfr a) { return fts(a.hi, a.lo); }
 __device__ __forceinline__ dfr dhalf(dfr a) { return {__fmul_rn(a.hi, 0.5f), __fmul_rn(a.lo, 0.5f)}; }
 __device__ __forceinline__ dfr dfrom(double v) {
     const float h = __double2float_rn(v);
@@ -78,7 +85,10 @@ __device__ __forceinline__ dfc mul_i(dfc a) { return {dneg(a.im), a.re}; }
 __device__ __forceinline__ dfc mul_mi(dfc a) { return {a.im, dneg(a.re)}; }
 __device__ __forceinline__ dfc cconj(dfc a) { return {a.re, dneg(a.im)}; }
 __device__ __forceinline__ dfc ld4(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
-__device__ __forceinline__ float4 st4(dfc a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
+__device__ __forceinline__ float4 st4(dfc a) {
+    const dfr r = dnorm(a.re), i = dnorm(a.im);
+    return make_float4(r.hi, r.lo, i.hi, i.lo);
+}
 __device__ __forceinline__ dfc czero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
 
 // Arithmetic policies: the storage type S of a complex value in memory and its
@@ -101,8 +111,14 @@ struct ArithDF {
     __device__ static __forceinline__ V make(double re, double im) { return {dfrom(re), dfrom(im)}; }
     // grids stored as (hi, lo) pairs
     __device__ static __forceinline__ V make(float2 re, float2 im) { return {{re.x, re.y}, {im.x, im.y}}; }
-    __device__ static __forceinline__ float2 re_s(V a) { return make_float2(a.re.hi, a.re.lo); }
-    __device__ static __forceinline__ float2 nim_s(V a) { return make_float2(-a.im.hi, -a.im.lo); }
+    __device__ static __forceinline__ float2 re_s(V a) {
+        const dfr r = dnorm(a.re);
+        return make_float2(r.hi, r.lo);
+    }
+    __device__ static __forceinline__ float2 nim_s(V a) {
+        const dfr r = dnorm(a.im);
+        return make_float2(-r.hi, -r.lo);
+    }
     __device__ static __forceinline__ double re(V a) { return dto(a.re); }
     __device__ static __forceinline__ double im(V a) { return dto(a.im); }
     __device__ static __forceinline__ V zero_im(V a) { return {a.re, {0.f, 0.f}}; }

@@ -312,7 +312,13 @@ __global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__re
         float acc[3 * NR];
 #pragma unroll
         for (int c = 0; c < 3 * NR; ++c) acc[c] = 0.f;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int base = 0; base < P * P; base += 32) {
+            // a full pass gives each lane one (x, y) row of the stencil; the last, partial pass splits the z run
+            // of each remaining row over lpp lanes (lane sub takes z = sub, sub + lpp, ...) so no lane idles
+            const int rem = P * P - base;
+            const int lpp = rem >= 32 ? 1 : 32 / rem;
+            const int idx = base + lane / lpp, sub = lane - (lane / lpp) * lpp;
+            if (idx >= P * P) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__re
             for (int r = 0; r < NR; ++r) s0[r] = s1[r] = 0.f;
             // unrolled so that 5 x NR loads are in flight per lane
 #pragma unroll 5
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const int64_t node = rowb + (int64_t)Nx * Ny * iz;

@@ -523,7 +523,13 @@ __global__ void __launch_bounds__(256) k_contract_df_warp(const dfv *__restrict_
         dfv acc[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) acc[c] = dfv(0.f, 0.f);
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int base = 0; base < P * P; base += 32) {
+            // one (x, y) stencil row per lane; the last, partial pass splits the z run of each remaining row
+            // over lpp lanes (z = sub, sub + lpp, ...)
+            const int rem = P * P - base;
+            const int lpp = rem >= 32 ? 1 : 32 / rem;
+            const int idx = base + lane / lpp, sub = lane - (lane / lpp) * lpp;
+            if (idx >= P * P) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(256) k_contract_df_warp(const dfv *__restrict_
 #pragma unroll
             for (int c = 0; c < C; ++c) col[c].zero();
 #pragma unroll 2
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const int64_t node = rowb + NxNy * iz;
