@@ -112,7 +112,9 @@ __global__ void __launch_bounds__(256) k_wave_force(const double *__restrict__ p
         }
         const double mx = m[3 * a], my = m[3 * a + 1], mz = m[3 * a + 2];
         double gx = 0.0, gy = 0.0, gz = 0.0;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(256) k_wave_force(const double *__restrict__ p
             const double ry = base[1] + (double)(jy - lo) * gp.h[1];
             const double wxy = wa[jx] * wa[P + jy];
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const double rz = base[2] + (double)(jz - lo) * gp.h[2];

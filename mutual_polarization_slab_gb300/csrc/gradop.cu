@@ -312,13 +312,9 @@ __global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__re
         float acc[3 * NR];
 #pragma unroll
         for (int c = 0; c < 3 * NR; ++c) acc[c] = 0.f;
-        for (int base = 0; base < P * P; base += 32) {
-            // a full pass gives each lane one (x, y) row of the stencil; the last, partial pass splits the z run
-            // of each remaining row over lpp lanes (lane sub takes z = sub, sub + lpp, ...) so no lane idles
-            const int rem = P * P - base;
-            const int lpp = rem >= 32 ? 1 : 32 / rem;
-            const int idx = base + lane / lpp, sub = lane - (lane / lpp) * lpp;
-            if (idx >= P * P) continue;
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;

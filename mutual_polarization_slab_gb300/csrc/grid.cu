@@ -62,7 +62,9 @@ __global__ void __launch_bounds__(256) k_spread(const double *__restrict__ m, in
             const double *ma = m + ((int64_t)r * n + a) * 3;
             const T m0 = (T)ma[0], m1 = (T)ma[1], m2 = (T)ma[2];
             T *g0 = grid + (int64_t)(3 * r) * G;
-            for (int idx = lane; idx < P * P; idx += 32) {
+            for (int row0 = 0; row0 < P * P; row0 += 32) {
+                int idx, sub, lpp;
+                if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
                 const int jx = idx % P, jy = idx / P;
                 int ix = sx + jx;
                 if (ix >= Nx) ix -= Nx;
@@ -70,7 +72,7 @@ __global__ void __launch_bounds__(256) k_spread(const double *__restrict__ m, in
                 if (iy >= Ny) iy -= Ny;
                 const T wxy = wa[jx] * wa[P + jy];
                 const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-                for (int jz = 0; jz < P; ++jz) {
+                for (int jz = sub; jz < P; jz += lpp) {
                     int iz = sz + jz;
                     if (iz >= Nz) iz -= Nz;
                     const T wv = wxy * wa[2 * P + jz];
@@ -101,7 +103,9 @@ __global__ void __launch_bounds__(256) k_contract(const T *__restrict__ grid, in
         for (int r = 0; r < nrhs; ++r) {
             const T *g0 = grid + (int64_t)(3 * r) * G;
             T a0 = 0, a1 = 0, a2 = 0;
-            for (int idx = lane; idx < P * P; idx += 32) {
+            for (int row0 = 0; row0 < P * P; row0 += 32) {
+                int idx, sub, lpp;
+                if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
                 const int jx = idx % P, jy = idx / P;
                 int ix = sx + jx;
                 if (ix >= Nx) ix -= Nx;
@@ -109,7 +113,7 @@ __global__ void __launch_bounds__(256) k_contract(const T *__restrict__ grid, in
                 if (iy >= Ny) iy -= Ny;
                 const T wxy = wa[jx] * wa[P + jy];
                 const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-                for (int jz = 0; jz < P; ++jz) {
+                for (int jz = sub; jz < P; jz += lpp) {
                     int iz = sz + jz;
                     if (iz >= Nz) iz -= Nz;
                     const T wv = wxy * wa[2 * P + jz];

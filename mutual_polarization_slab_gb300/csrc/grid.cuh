@@ -20,6 +20,21 @@ struct GridParams {
     const int32_t *order = nullptr;
 };
 
+// The P x P (x, y) rows of a particle's stencil, handed to the lanes of a warp
+// 32 at a time.  In a full pass lane l takes row row0 + l and its whole z run; in
+// the last, partial pass the z run of each of the rem remaining rows is split over
+// lpp = 32 / rem lanes (lane sub of a row takes z = sub, sub + lpp, ...), so no
+// lane idles.  Returns false for a lane left without a row.
+__device__ __forceinline__ bool stencil_row(int row0, int P, int lane, int *idx, int *sub, int *lpp) {
+    const int rem = P * P - row0;
+    const int l = rem >= 32 ? 1 : 32 / rem;
+    const int q = lane / l;
+    *idx = row0 + q;
+    *sub = lane - q * l;
+    *lpp = l;
+    return row0 + q < P * P;
+}
+
 GridParams make_grid_params(const int64_t *Ngrid, const double *box, double xi, const double *eta, int P);
 int grid_geometry(const double *x, int64_t n, const GridParams &gp, int32_t *start, double *w64, float *w32,
                   cudaStream_t s);

@@ -40,7 +40,9 @@ __global__ void __launch_bounds__(256) k_spread_gen(const double *__restrict__ m
 #pragma unroll
         for (int c = 0; c < 8; ++c) mv[c] = c < ncomp ? (T)m[((int64_t)r * n + a) * ncomp + c] : (T)0;
         T *g0 = grid + (int64_t)r * ncomp * G;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -48,7 +50,7 @@ __global__ void __launch_bounds__(256) k_spread_gen(const double *__restrict__ m
             if (iy >= Ny) iy -= Ny;
             const T wxy = wa[jx] * wa[P + jy];
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const T wv = wxy * wa[2 * P + jz];
@@ -80,7 +82,9 @@ __global__ void __launch_bounds__(256) k_contract_gen(const T *__restrict__ grid
         T acc[8];
 #pragma unroll
         for (int c = 0; c < 8; ++c) acc[c] = (T)0;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -88,7 +92,7 @@ __global__ void __launch_bounds__(256) k_contract_gen(const T *__restrict__ grid
             if (iy >= Ny) iy -= Ny;
             const T wxy = wa[jx] * wa[P + jy];
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const T wv = wxy * wa[2 * P + jz];

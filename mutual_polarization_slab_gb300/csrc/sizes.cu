@@ -291,7 +291,9 @@ __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m,
         const T hx = (T)gp.h[0], hy = (T)gp.h[1], hz = (T)gp.h[2];
         const T *ga = g + a * P3;
         T *gr = grid + (int64_t)r * gp.G;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m,
             const T rx = bx + (T)jx * hx, ry = by + (T)jy * hy;
             const T pxy = rx * px + ry * py;
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const T rz = bz + (T)jz * hz;
@@ -343,7 +345,9 @@ __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid,
         const T *ga = g + a * P3;
         const T *gr = grid + (int64_t)r * gp.G;
         T ax = 0, ay = 0, az = 0;
-        for (int idx = lane; idx < P * P; idx += 32) {
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid,
             const T rx = bx + (T)jx * hx, ry = by + (T)jy * hy;
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
             T sxy = 0, szz = 0;
-            for (int jz = 0; jz < P; ++jz) {
+            for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const T v = ga[jx + P * (jy + P * jz)] * gr[rowb + (int64_t)Nx * Ny * iz];

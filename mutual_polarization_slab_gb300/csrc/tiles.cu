@@ -523,13 +523,9 @@ __global__ void __launch_bounds__(256) k_contract_df_warp(const dfv *__restrict_
         dfv acc[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) acc[c] = dfv(0.f, 0.f);
-        for (int base = 0; base < P * P; base += 32) {
-            // one (x, y) stencil row per lane; the last, partial pass splits the z run of each remaining row
-            // over lpp lanes (z = sub, sub + lpp, ...)
-            const int rem = P * P - base;
-            const int lpp = rem >= 32 ? 1 : 32 / rem;
-            const int idx = base + lane / lpp, sub = lane - (lane / lpp) * lpp;
-            if (idx >= P * P) continue;
+        for (int row0 = 0; row0 < P * P; row0 += 32) {
+            int idx, sub, lpp;
+            if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
             const int jx = idx % P, jy = idx / P;
             int ix = sx + jx;
             if (ix >= Nx) ix -= Nx;
