@@ -69,7 +69,8 @@ __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, f
 // w and dw/dr at every tile column, row and plane, zero where the stencil does
 // not reach -- plus a mask of the tile rows they cover, so a warp (two rows)
 // skips a particle with one uniform test and otherwise runs a branch-free
-// update: value(x,y,z) = (mx gx wy + my wx gy) wz + mz wx wy gz.
+// update: value(x,y,z) = (mx gx wy + my wx gy) wz + mz wx wy gz, over the groups
+// of 4 tile planes the particle reaches (a plane mask staged with the factors).
 constexpr int kGChunk = 32;
 
 template <int TZ, int NR>
@@ -84,6 +85,7 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     __shared__ float2 s_f[kGChunk][kPos];        // (w, dw/dr) at tile columns, rows, planes
     __shared__ __align__(16) float s_m[kGChunk][kMS];
     __shared__ unsigned s_rows[kGChunk];
+    __shared__ unsigned s_planes[kGChunk];
     const int64_t t = blockIdx.x;
     const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
     const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     const int64_t e0 = tstart[t], e1 = tstart[t + 1];
     for (int64_t cb = e0; cb < e1; cb += kGChunk) {
         const int cnt = (int)min((int64_t)kGChunk, e1 - cb);
-        if (threadIdx.x < kGChunk) s_rows[threadIdx.x] = 0u;
+        if (threadIdx.x < kGChunk) s_rows[threadIdx.x] = s_planes[threadIdx.x] = 0u;
         if (threadIdx.x < cnt) {
             const int32_t a = entries[cb + threadIdx.x];
 #pragma unroll
@@ -125,6 +127,7 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
                 const int64_t o = (int64_t)a * 3 * P + d * P + j;
                 f = make_float2(w[o], g[o]);
                 if (d == 1) atomicOr(&s_rows[pp], 1u << tpos);
+                if (d == 2) atomicOr(&s_planes[pp], 1u << tpos);
             }
             s_f[pp][k] = f;
         }
@@ -139,11 +142,17 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
                 cA[r] = s_m[pp][3 * r] * gxwy + s_m[pp][3 * r + 1] * wxgy;
                 cB[r] = s_m[pp][3 * r + 2] * wxwy;
             }
+            // planes in groups of 4; a group the particle does not reach is skipped (uniform over the CTA)
+            const unsigned planes = s_planes[pp];
 #pragma unroll
-            for (int z = 0; z < TZ; ++z) {
-                const float2 fz = s_f[pp][kTileX + kTileY + z];
+            for (int z0 = 0; z0 < TZ; z0 += 4) {
+                if (TZ > 4 && ((planes >> z0) & 0xFu) == 0u) continue;
 #pragma unroll
-                for (int r = 0; r < NR; ++r) acc[z][r] += cA[r] * fz.x + cB[r] * fz.y;
+                for (int z = z0; z < z0 + 4 && z < TZ; ++z) {
+                    const float2 fz = s_f[pp][kTileX + kTileY + z];
+#pragma unroll
+                    for (int r = 0; r < NR; ++r) acc[z][r] += cA[r] * fz.x + cB[r] * fz.y;
+                }
             }
         }
         __syncthreads();
@@ -324,8 +333,8 @@ __global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__re
             float s0[NR], s1[NR];
 #pragma unroll
             for (int r = 0; r < NR; ++r) s0[r] = s1[r] = 0.f;
-            // unrolled so that 5 x NR loads are in flight per lane
-#pragma unroll 5
+            // unrolled over the whole z run of P = 10 (10 x NR loads in flight per lane; 5 and 2 measured slower)
+#pragma unroll 10
             for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
