@@ -51,7 +51,8 @@ def config_dict(w, extra=None):
                      f"{int(w['Ngrid'][0])}^3 grid, P={w['P']}, xi={w['xi']:.4f}, rc={w['rc']:.4f}, "
                      f"fully periodic; geometry setup + solve per step",
          "n_particles": int(w["n"]), "n_rhs": 3, "grid": int(w["Ngrid"][0]), "P": int(w["P"]),
-         "l2": "per-step grids (9 x 192^3 fp32 = 255 MB) exceed the 129 MB L2; L2 also flushed between steps"}
+         "l2": "per-step working set (9 x 192^3 double-float residual grids = 510 MB, 3 x 192^3 fp32 grids, "
+               "pair lists) exceeds the 129 MB L2; L2 also flushed (256 MB write) between steps"}
     if extra:
         d.update(extra)
     return d
