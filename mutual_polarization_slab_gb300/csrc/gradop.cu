@@ -67,8 +67,10 @@ __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, f
 // tile's particle list (fixed order: deterministic, no atomics).  Particles are
 // staged in chunks with their per-axis factors already aligned to the tile --
 // w and dw/dr at every tile column, row and plane, zero where the stencil does
-// not reach -- plus a mask of the tile rows they cover, so a warp (two rows)
-// skips a particle with one uniform test and otherwise runs a branch-free
+// not reach -- plus masks of the tile columns, rows and planes they cover, so a
+// warp (an 8 x 4 patch of the tile's columns: the particle's 10-wide stencil
+// often misses one half of the tile in x, which a warp of two full 16-wide rows
+// could not skip) skips a particle with one uniform test and otherwise runs a branch-free
 // update: value(x,y,z) = (mx gx wy + my wx gy) wz + mz wx wy gz, over the groups
 // of 4 tile planes the particle reaches (a plane mask staged with the factors).
 constexpr int kGChunk = 32;
@@ -85,11 +87,15 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     __shared__ float2 s_f[kGChunk][kPos];        // (w, dw/dr) at tile columns, rows, planes
     __shared__ __align__(16) float s_m[kGChunk][kMS];
     __shared__ unsigned s_rows[kGChunk];
+    __shared__ unsigned s_cols[kGChunk];
     __shared__ unsigned s_planes[kGChunk];
     const int64_t t = blockIdx.x;
     const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
     const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
-    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4, wid = threadIdx.x >> 5;
+    // warp wid owns the 8 x 4 patch (columns 8 (wid & 1) .. +8, rows 4 (wid >> 1) .. +4) of the 16 x 16 tile
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int px = wid & 1, py = wid >> 1;
+    const int tx = 8 * px + (lane & 7), ty = 4 * py + (lane >> 3);
     const int P = gp.P;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     float acc[TZ][NR];
@@ -100,7 +106,7 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
     const int64_t e0 = tstart[t], e1 = tstart[t + 1];
     for (int64_t cb = e0; cb < e1; cb += kGChunk) {
         const int cnt = (int)min((int64_t)kGChunk, e1 - cb);
-        if (threadIdx.x < kGChunk) s_rows[threadIdx.x] = s_planes[threadIdx.x] = 0u;
+        if (threadIdx.x < kGChunk) s_rows[threadIdx.x] = s_cols[threadIdx.x] = s_planes[threadIdx.x] = 0u;
         if (threadIdx.x < cnt) {
             const int32_t a = entries[cb + threadIdx.x];
 #pragma unroll
@@ -126,14 +132,14 @@ __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restr
             if (node < Nd && j < P) {
                 const int64_t o = (int64_t)a * 3 * P + d * P + j;
                 f = make_float2(w[o], g[o]);
-                if (d == 1) atomicOr(&s_rows[pp], 1u << tpos);
-                if (d == 2) atomicOr(&s_planes[pp], 1u << tpos);
+                atomicOr(d == 0 ? &s_cols[pp] : (d == 1 ? &s_rows[pp] : &s_planes[pp]), 1u << tpos);
             }
             s_f[pp][k] = f;
         }
         __syncthreads();
         for (int pp = 0; pp < cnt; ++pp) {
-            if (((s_rows[pp] >> (2 * wid)) & 3u) == 0u) continue;   // neither row of this warp is covered
+            // the particle misses this warp's patch: none of its 4 rows or none of its 8 columns is covered
+            if (((s_rows[pp] >> (4 * py)) & 0xFu) == 0u || ((s_cols[pp] >> (8 * px)) & 0xFFu) == 0u) continue;
             const float2 fx = s_f[pp][tx], fy = s_f[pp][kTileX + ty];
             const float gxwy = fx.y * fy.x, wxgy = fx.x * fy.y, wxwy = fx.x * fy.x;
             float cA[NR], cB[NR];

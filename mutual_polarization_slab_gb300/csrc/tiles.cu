@@ -220,7 +220,11 @@ __global__ void __launch_bounds__(256) k_spread_tiled(const double *__restrict__
     const int64_t t = blockIdx.x;
     const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((int64_t)ntx * nty));
     const int X0 = bx * kTileX, Y0 = by * kTileY, Z0 = bz * TZ;
-    const int tx = threadIdx.x & (kTileX - 1), ty = threadIdx.x >> 4;
+    // warp w owns the 8 x 4 patch (columns 8 (w & 1) .. +8, rows 4 (w >> 1) .. +4) of the 16 x 16 tile: a particle
+    // whose stencil misses the patch costs the warp one uniform branch (with two full 16-wide rows per warp, every
+    // warp whose rows the particle reaches would run it, however few of the columns it covers)
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tx = 8 * (wid & 1) + (lane & 7), ty = 4 * (wid >> 1) + (lane >> 3);
     const int P = gp.P;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     ProdAcc<T> acc[TZ][C];
