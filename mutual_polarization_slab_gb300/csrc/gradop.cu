@@ -73,7 +73,9 @@ __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, f
 // could not skip) skips a particle with one uniform test and otherwise runs a branch-free
 // update: value(x,y,z) = (mx gx wy + my wx gy) wz + mz wx wy gz, over the groups
 // of 4 tile planes the particle reaches (a plane mask staged with the factors).
-constexpr int kGChunk = 32;
+// particles staged per barrier interval: 96 measured 0.300 ms per launch at the bench workload against 0.323
+// for 32 (fewer barriers, and the warps' uneven shares of a chunk even out), 0.306 for 64 and 0.301 for 128
+constexpr int kGChunk = 96;
 
 template <int TZ, int NR>
 __global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
