@@ -136,7 +136,11 @@ struct mps_system {
     double *rgrid2 = nullptr;   // 2 x 3 x G
     double *slab = nullptr;     // max_rhs
     int32_t *diag_idx = nullptr;  // max_rhs (device)
-    int32_t *diag_idx_host = nullptr;  // pinned mirror
+    int32_t *diag_idx_host = nullptr;  // pinned mirror (start of the pinned block below)
+    // pinned host scratch of the solvers, in the same block: the frozen flags (max_rhs) and the convergence
+    // scalars read back every GMRES step (6 max_rhs doubles); pinned so the reads are plain DMA
+    int32_t *host_frozen = nullptr;
+    double *host_scr = nullptr;
     void *fft_work = nullptr;
     size_t fft_work_bytes = 0;
     TileBins tb64, tb32;        // tile binning for the tiled spread/contract (per precision tile depth)
@@ -1184,8 +1188,9 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         }
     }
 
-    std::vector<double> hres(nrhs);
-    std::vector<int32_t> hfrozen(nrhs, 0);
+    double *hres = s->host_scr;         // pinned (nrhs)
+    int32_t *hfrozen = s->host_frozen;  // pinned (nrhs)
+    for (int r = 0; r < nrhs; ++r) hfrozen[r] = 0;
     int rc = MPS_OK;
     const dim3 vgrid(grid_for(n3, 256, 152 * 8), nrhs);
     int cyc = 0;
@@ -1237,7 +1242,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         GM_TRY(multidot(V, ldv, n3, 1, V, n3, n3, nrhs, partial, S.nrm2, 1, st));
         k_cycle_start<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs);
         GM_LAUNCH();
-        GM_CUDA(cudaMemcpyAsync(hres.data(), S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        GM_CUDA(cudaMemcpyAsync(hres, S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
         GM_CUDA(cudaStreamSynchronize(st));
         bool all = true;
         for (int r = 0; r < nrhs; ++r) {
@@ -1250,7 +1255,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             at_start_exit = true;
             break;
         }
-        GM_CUDA(cudaMemcpyAsync(frozen, hfrozen.data(), sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+        GM_CUDA(cudaMemcpyAsync(frozen, hfrozen, sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
         k_scale_vec<<<vgrid, 256, 0, st>>>(V, n3, V, n3, S.beta, 1, n3);
         GM_LAUNCH();
         for (int j = 0; j < restart; ++j) {
@@ -1270,7 +1275,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             GM_LAUNCH();
             k_scale_vec<<<vgrid, 256, 0, st>>>(w, n3, V + (int64_t)(j + 1) * ldv, n3, S.nrm2, 1, n3);
             GM_LAUNCH();
-            GM_CUDA(cudaMemcpyAsync(hres.data(), S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+            GM_CUDA(cudaMemcpyAsync(hres, S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
             GM_CUDA(cudaStreamSynchronize(st));
             bool done = true, changed = false;
             for (int r = 0; r < nrhs; ++r) {
@@ -1282,7 +1287,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             }
             if (done) break;
             if (changed)
-                GM_CUDA(cudaMemcpyAsync(frozen, hfrozen.data(), sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
+                GM_CUDA(cudaMemcpyAsync(frozen, hfrozen, sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
         }
         k_backsolve<<<(nrhs + 31) / 32, 32, 0, st>>>(S, restart, nrhs);
         GM_LAUNCH();
@@ -1329,9 +1334,9 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     GM_LAUNCH();
     GM_TRY(multidot(w, n3, n3, 1, w, n3, n3, nrhs, partial, S.nrm2, 1, st));
     {
-        std::vector<double> nr(nrhs), nb(nrhs);
-        GM_CUDA(cudaMemcpyAsync(nr.data(), S.nrm2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
-        GM_CUDA(cudaMemcpyAsync(nb.data(), S.bnorm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        double *nr = s->host_scr + nrhs, *nb = s->host_scr + 2 * nrhs;
+        GM_CUDA(cudaMemcpyAsync(nr, S.nrm2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        GM_CUDA(cudaMemcpyAsync(nb, S.bnorm, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
         GM_CUDA(cudaStreamSynchronize(st));
         for (int r = 0; r < nrhs; ++r) {
             relres_out[r] = nb[r] > 0 ? sqrt(nr[r]) / nb[r] : 0.0;
@@ -1356,8 +1361,8 @@ static int true_residual(mps_system *s, const double *b, const double *x, double
     MPS_LAUNCH_CHECK();
     MPS_TRY(multidot(r, n3, n3, 1, r, n3, n3, nrhs, partial, nrm, 1, st));
     MPS_TRY(multidot(b, n3, n3, 1, b, n3, n3, nrhs, partial, nrm + nrhs, 1, st));
-    std::vector<double> hn(2 * nrhs);
-    MPS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
+    double *hn = s->host_scr + 3 * nrhs;   // pinned (2 nrhs)
+    MPS_CUDA_TRY(cudaMemcpyAsync(hn, nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
     MPS_CUDA_TRY(cudaStreamSynchronize(st));
     for (int q = 0; q < nrhs; ++q) relres[q] = hn[nrhs + q] > 0 ? sqrt(hn[q]) / sqrt(hn[nrhs + q]) : 0.0;
     return MPS_OK;
@@ -1365,11 +1370,10 @@ static int true_residual(mps_system *s, const double *b, const double *x, double
 
 // Norms ||r_q|| / ||b_q|| for every system (host result).
 static int rel_norms(const double *r, const double *b, int64_t n3, int nrhs, double *partial, double *nrm,
-                     std::vector<double> &rel, cudaStream_t st) {
+                     std::vector<double> &rel, double *hn, cudaStream_t st) {
     MPS_TRY(multidot(r, n3, n3, 1, r, n3, n3, nrhs, partial, nrm, 1, st));
     MPS_TRY(multidot(b, n3, n3, 1, b, n3, n3, nrhs, partial, nrm + nrhs, 1, st));
-    std::vector<double> hn(2 * nrhs);
-    MPS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaMemcpyAsync(hn, nrm, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, st));
     MPS_CUDA_TRY(cudaStreamSynchronize(st));
     for (int q = 0; q < nrhs; ++q) rel[q] = hn[nrhs + q] > 0 ? sqrt(hn[q]) / sqrt(hn[nrhs + q]) : 0.0;
     return MPS_OK;
@@ -1502,7 +1506,7 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
                 e = MPS_CUDA_ERR;
                 break;
             }
-            e = rel_norms(r, b, n3, nrhs, partial, nrm, rel, st);
+            e = rel_norms(r, b, n3, nrhs, partial, nrm, rel, s->host_scr + 3 * nrhs, st);
             estimated = true;
         } else {
             e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
@@ -1596,7 +1600,14 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CR_TRY(dalloc(&s->slab, sizeof(double) * s->max_rhs, st));
     if (cudaMemsetAsync(s->slab, 0, sizeof(double) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * s->max_rhs, st));
-    if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * s->max_rhs) != cudaSuccess) CR_TRY(MPS_NO_MEMORY);
+    {
+        const size_t ints = ((size_t)2 * s->max_rhs + 1) & ~(size_t)1;   // even: the doubles stay 8-byte aligned
+        if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * ints + sizeof(double) * 6 * s->max_rhs) !=
+            cudaSuccess)
+            CR_TRY(MPS_NO_MEMORY);
+        s->host_frozen = s->diag_idx_host + s->max_rhs;
+        s->host_scr = reinterpret_cast<double *>(s->diag_idx_host + ints);
+    }
     if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     // cell list + pair CSR
     compute_ncell(d->box, d->rc, s->ncell);
