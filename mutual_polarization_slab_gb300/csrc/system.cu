@@ -116,6 +116,7 @@ struct mps_system {
     // side stream: the float32 pair sum runs beside the spread / FFT / contraction of the same matvec
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_res = nullptr;    // GMRES: residual estimates read back (a matvec may be queued behind it)
     double *rs_buf = nullptr;        // max_rhs x n x 3: the pair-sum part of a float32 matvec
     // complex permittivities: vectors are (Re m, Im m) per particle (ndof 6); the real operator runs on the
     // 2 nc real vectors [Re m_0..Re m_{nc-1}, Im m_0..Im m_{nc-1}] and the imaginary diagonal couples them
@@ -182,6 +183,7 @@ static void free_system(mps_system *s) {
     if (s->side) cudaStreamDestroy(s->side);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->ev_res) cudaEventDestroy(s->ev_res);
     tile_bins_free(s->tb64, s->stream);
     tile_bins_free(s->tb32, s->stream);
     if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
@@ -1258,9 +1260,28 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         GM_CUDA(cudaMemcpyAsync(frozen, hfrozen, sizeof(int32_t) * nrhs, cudaMemcpyHostToDevice, st));
         k_scale_vec<<<vgrid, 256, 0, st>>>(V, n3, V, n3, S.beta, 1, n3);
         GM_LAUNCH();
+        // With a float32 operator (a matvec of about a millisecond), step j + 1's matvec is queued before the
+        // host waits for step j's residual estimates whenever their trend says step j cannot finish every
+        // system: the estimate after step j, extrapolated from the last two, is above 2 tol for some active
+        // system.  The wait then overlaps that matvec instead of leaving the GPU idle; a wrong guess costs one
+        // discarded matvec (w is rewritten before it is read again).
+        const bool may_speculate = precision == MPS_FP32 || precision == MPS_FP32_GRAD;
+        std::vector<double> hlast(hres, hres + nrhs), hprev(nrhs, -1.0);
+        auto likely_continues = [&]() {
+            for (int r = 0; r < nrhs; ++r) {
+                if (hfrozen[r]) continue;
+                const double ratio = hprev[r] > 0.0 ? std::min(1.0, hlast[r] / hprev[r]) : 0.5;
+                if (hlast[r] * ratio > 2.0 * tol) return true;
+            }
+            return false;
+        };
+        bool queued = false;   // step j's matvec already queued into w
         for (int j = 0; j < restart; ++j) {
-            GM_TRY(matvec_any(s, V + (int64_t)j * ldv, w, nrhs, precision, st));
-            ++*mv_count;
+            if (!queued) {
+                GM_TRY(matvec_any(s, V + (int64_t)j * ldv, w, nrhs, precision, st));
+                ++*mv_count;
+            }
+            queued = false;
             // classical Gram-Schmidt, twice (once for the inner solves of the mixed refinement)
             GM_TRY(multidot(V, ldv, n3, j + 1, w, n3, n3, nrhs, partial, S.h1, kMaxCols, st));
             k_sub_basis<<<vgrid, 256, 0, st>>>(V, ldv, n3, j + 1, S.h1, kMaxCols, w, n3, n3);
@@ -1276,7 +1297,20 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             k_scale_vec<<<vgrid, 256, 0, st>>>(w, n3, V + (int64_t)(j + 1) * ldv, n3, S.nrm2, 1, n3);
             GM_LAUNCH();
             GM_CUDA(cudaMemcpyAsync(hres, S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
-            GM_CUDA(cudaStreamSynchronize(st));
+            if (may_speculate && j + 1 < restart && likely_continues()) {
+                if (!s->ev_res) GM_CUDA(cudaEventCreateWithFlags(&s->ev_res, cudaEventDisableTiming));
+                GM_CUDA(cudaEventRecord(s->ev_res, st));
+                GM_TRY(matvec_any(s, V + (int64_t)(j + 1) * ldv, w, nrhs, precision, st));
+                ++*mv_count;
+                queued = true;
+                GM_CUDA(cudaEventSynchronize(s->ev_res));
+            } else {
+                GM_CUDA(cudaStreamSynchronize(st));
+            }
+            for (int r = 0; r < nrhs; ++r) {
+                hprev[r] = hlast[r];
+                hlast[r] = hres[r];
+            }
             bool done = true, changed = false;
             for (int r = 0; r < nrhs; ++r) {
                 if (!hfrozen[r] && hres[r] <= tol) {
