@@ -310,8 +310,10 @@ __global__ void k_contract_grad_gather(const float *__restrict__ partial, int64_
 // columns of the stencil, each runs its z column; fixed summation order.  Warps
 // visit particles in `order` (spatially sorted: the warps of one CTA read
 // overlapping stencils, so much of it comes from L1); null = input order.
+// 3 blocks per SM (79 registers for 3 vectors, no spills): 0.283 ms per launch at the bench workload against 0.293
+// with the 64-register cap of 4 blocks (which spills) and 0.338 with 2 blocks
 template <int NR>
-__global__ void __launch_bounds__(256, 4) k_contract_grad_warp(const float *__restrict__ grid, int64_t n, int r0,
+__global__ void __launch_bounds__(256, 3) k_contract_grad_warp(const float *__restrict__ grid, int64_t n, int r0,
                                                             const int32_t *__restrict__ order,
                                                             const int32_t *__restrict__ start,
                                                             const float *__restrict__ w, const float *__restrict__ g,
