@@ -130,17 +130,16 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
     ng, P = grid_for(box, xi, tol, fft_friendly)
     sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, box, xi, tol, Ngrid=ng, P=P, max_rhs=3 * K)
     try:
-        b = torch.zeros((3 * K, n, 3), dtype=torch.float64, device="cuda")
-        x0 = torch.zeros_like(b)
+        # right-hand side 3k + i: unit field along i with contrast scaling k; guess 4 pi a^3 beta / (1 - beta phi)
+        # along the field (CS/CapacitanceTensorSpectrum.m:45-48), built in a few tensor operations (one
+        # assignment per right-hand side costs more host time than a small configuration's solve)
         phi_v = 4 * math.pi * float(np.sum(cfg.radii ** 3)) / (3 * float(np.prod(box)))
-        diag_index = []
-        for k in range(K):
-            beta = cfg.beta * s[k]
-            amp = torch.as_tensor(4 * math.pi * cfg.radii ** 3 * beta / (1 - beta * phi_v), device="cuda")
-            for i in range(3):
-                b[3 * k + i, :, i] = 1.0
-                x0[3 * k + i, :, i] = amp
-                diag_index.append(k)
+        beta = s[:, None] * np.asarray(cfg.beta, dtype=np.float64)[None, :]                  # (K, N)
+        amp = torch.as_tensor(4 * math.pi * cfg.radii[None, :] ** 3 * beta / (1 - beta * phi_v), device="cuda")
+        eye = torch.eye(3, dtype=torch.float64, device="cuda")
+        b = eye[None, :, None, :].expand(K, 3, n, 3).reshape(3 * K, n, 3).contiguous()
+        x0 = (amp[:, None, :, None] * eye[None, :, None, :]).reshape(3 * K, n, 3).contiguous()
+        diag_index = [k for k in range(K) for _ in range(3)]
         sol, info = sysm.solve(b, x0, tol=tol, restart=min(3 * n, 30), maxit=100 if precision != "mixed" else 8,
                                precision=precision, diag_index=diag_index)
         C = sol.reshape(K, 3, n, 3).mean(dim=2).cpu().numpy()

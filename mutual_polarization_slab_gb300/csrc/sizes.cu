@@ -17,6 +17,8 @@
 // base offset.
 #include <math.h>
 
+#include <cstdlib>
+
 #include "sizes.cuh"
 
 namespace mps {
@@ -268,8 +270,11 @@ __global__ void k_cs_green(GridParams gp, double eta, double xi, double *__restr
     }
 }
 
-// Spread: a warp per (particle, vector); lanes walk the (x, y) footprint.
-template <typename T>
+// Spread: a warp per (particle, block of RB vectors); lanes walk the (x, y)
+// footprint.  The particle's node weights K(d)/d (P^3 per particle) are read once
+// per block of vectors instead of once per vector: with a spectrum batch (3 fields x
+// K contrasts) they were the dominant read.
+template <typename T, int RB>
 __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m, int64_t n, int nrhs,
                                                    const int32_t *__restrict__ start, const double *__restrict__ base,
                                                    const T *__restrict__ g, GridParams gp, T *__restrict__ grid) {
@@ -280,17 +285,25 @@ __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m,
     const int lo = (P - 1) / 2;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t P3 = (int64_t)P * P * P;
-    for (int64_t t = warp; t < n * nrhs; t += nw) {
+    const int nblk = (nrhs + RB - 1) / RB;
+    for (int64_t t = warp; t < n * nblk; t += nw) {
         const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
-        const int r = (int)(t / n);
+        const int r0 = (int)(t / n) * RB;
+        const int cnt = min(RB, nrhs - r0);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
-        const double *ma = m + ((int64_t)r * n + a) * 3;
-        const T px = (T)ma[0], py = (T)ma[1], pz = (T)ma[2];
+        T px[RB], py[RB], pz[RB];
+#pragma unroll
+        for (int q = 0; q < RB; ++q) {
+            const double *ma = m + ((int64_t)(r0 + (q < cnt ? q : 0)) * n + a) * 3;
+            px[q] = (T)ma[0];
+            py[q] = (T)ma[1];
+            pz[q] = (T)ma[2];
+        }
         const T bx = (T)(base[3 * a] - lo * gp.h[0]), by = (T)(base[3 * a + 1] - lo * gp.h[1]),
                 bz = (T)(base[3 * a + 2] - lo * gp.h[2]);
         const T hx = (T)gp.h[0], hy = (T)gp.h[1], hz = (T)gp.h[2];
         const T *ga = g + a * P3;
-        T *gr = grid + (int64_t)r * gp.G;
+        T *gr = grid + (int64_t)r0 * gp.G;
         for (int row0 = 0; row0 < P * P; row0 += 32) {
             int idx, sub, lpp;
             if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
@@ -300,14 +313,19 @@ __global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m,
             int iy = sy + jy;
             if (iy >= Ny) iy -= Ny;
             const T rx = bx + (T)jx * hx, ry = by + (T)jy * hy;
-            const T pxy = rx * px + ry * py;
+            T pxy[RB];
+#pragma unroll
+            for (int q = 0; q < RB; ++q) pxy[q] = rx * px[q] + ry * py[q];
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
             for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
                 const T rz = bz + (T)jz * hz;
-                const T v = ga[jx + P * (jy + P * jz)] * (pxy + rz * pz);
-                atomicAdd(gr + rowb + (int64_t)Nx * Ny * iz, v);
+                const T wv = ga[jx + P * (jy + P * jz)];
+                T *node = gr + rowb + (int64_t)Nx * Ny * iz;
+#pragma unroll
+                for (int q = 0; q < RB; ++q)
+                    if (q < cnt) atomicAdd(node + (int64_t)q * gp.G, wv * (pxy[q] + rz * pz[q]));
             }
         }
     }
@@ -323,7 +341,9 @@ __global__ void k_scale_cs(T *__restrict__ spec, int nrhs, int64_t Gc, const T *
 }
 
 // Contract: out = prod(h) sum_nodes K(d)/d (node - x) E~(node)  (overwrites).
-template <typename T>
+// A warp per (particle, block of RB vectors): the node weights are read once per
+// block; each vector's sums run in the same order as with one vector per warp.
+template <typename T, int RB>
 __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid, int64_t n, int nrhs,
                                                      const int32_t *__restrict__ start,
                                                      const double *__restrict__ base, const T *__restrict__ g,
@@ -335,16 +355,20 @@ __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid,
     const int lo = (P - 1) / 2;
     const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
     const int64_t P3 = (int64_t)P * P * P;
-    for (int64_t t = warp; t < n * nrhs; t += nw) {
+    const int nblk = (nrhs + RB - 1) / RB;
+    for (int64_t t = warp; t < n * nblk; t += nw) {
         const int64_t a = gp.order ? (int64_t)gp.order[t % n] : t % n;
-        const int r = (int)(t / n);
+        const int r0 = (int)(t / n) * RB;
+        const int cnt = min(RB, nrhs - r0);
         const int sx = start[3 * a], sy = start[3 * a + 1], sz = start[3 * a + 2];
         const T bx = (T)(base[3 * a] - lo * gp.h[0]), by = (T)(base[3 * a + 1] - lo * gp.h[1]),
                 bz = (T)(base[3 * a + 2] - lo * gp.h[2]);
         const T hx = (T)gp.h[0], hy = (T)gp.h[1], hz = (T)gp.h[2];
         const T *ga = g + a * P3;
-        const T *gr = grid + (int64_t)r * gp.G;
-        T ax = 0, ay = 0, az = 0;
+        const T *gr = grid + (int64_t)r0 * gp.G;
+        T ax[RB], ay[RB], az[RB];
+#pragma unroll
+        for (int q = 0; q < RB; ++q) ax[q] = ay[q] = az[q] = 0;
         for (int row0 = 0; row0 < P * P; row0 += 32) {
             int idx, sub, lpp;
             if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
@@ -355,26 +379,40 @@ __global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid,
             if (iy >= Ny) iy -= Ny;
             const T rx = bx + (T)jx * hx, ry = by + (T)jy * hy;
             const int64_t rowb = (int64_t)ix + (int64_t)Nx * iy;
-            T sxy = 0, szz = 0;
+            T sxy[RB], szz[RB];
+#pragma unroll
+            for (int q = 0; q < RB; ++q) sxy[q] = szz[q] = 0;
             for (int jz = sub; jz < P; jz += lpp) {
                 int iz = sz + jz;
                 if (iz >= Nz) iz -= Nz;
-                const T v = ga[jx + P * (jy + P * jz)] * gr[rowb + (int64_t)Nx * Ny * iz];
-                sxy += v;
-                szz += v * (bz + (T)jz * hz);
+                const T wv = ga[jx + P * (jy + P * jz)];
+                const T rz = bz + (T)jz * hz;
+                const T *node = gr + rowb + (int64_t)Nx * Ny * iz;
+#pragma unroll
+                for (int q = 0; q < RB; ++q) {
+                    if (q < cnt) {
+                        const T v = wv * node[(int64_t)q * gp.G];
+                        sxy[q] += v;
+                        szz[q] += v * rz;
+                    }
+                }
             }
-            ax += rx * sxy;
-            ay += ry * sxy;
-            az += szz;
+#pragma unroll
+            for (int q = 0; q < RB; ++q) {
+                ax[q] += rx * sxy[q];
+                ay[q] += ry * sxy[q];
+                az[q] += szz[q];
+            }
         }
-        ax = warp_sum(ax);
-        ay = warp_sum(ay);
-        az = warp_sum(az);
-        if (lane == 0) {
-            double *o = out + ((int64_t)r * n + a) * 3;
-            o[0] = (double)ax * gp.hprod;
-            o[1] = (double)ay * gp.hprod;
-            o[2] = (double)az * gp.hprod;
+#pragma unroll
+        for (int q = 0; q < RB; ++q) {
+            const T sxq = warp_sum(ax[q]), syq = warp_sum(ay[q]), szq = warp_sum(az[q]);
+            if (lane == 0 && q < cnt) {
+                double *o = out + ((int64_t)(r0 + q) * n + a) * 3;
+                o[0] = (double)sxq * gp.hprod;
+                o[1] = (double)syq * gp.hprod;
+                o[2] = (double)szq * gp.hprod;
+            }
         }
     }
 }
@@ -418,7 +456,9 @@ int spread_cs(const double *m, int64_t n, int nrhs, const int32_t *start, const 
               const GridParams &gp, T *grid, cudaStream_t s) {
     MPS_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(T) * (size_t)nrhs * gp.G, s));
     if (n == 0) return MPS_OK;
-    k_spread_cs<T><<<grid_for(n * nrhs * 32, 256, 152 * 64), 256, 0, s>>>(m, n, nrhs, start, base, g, gp, grid);
+    // 8 vectors per warp pass (the node weights read once per 8 vectors); 4 and 16 measured slower
+    const int64_t items = n * ((nrhs + 7) / 8);
+    k_spread_cs<T, 8><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(m, n, nrhs, start, base, g, gp, grid);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
@@ -435,7 +475,10 @@ template <typename T>
 int contract_cs(const T *grid, int64_t n, int nrhs, const int32_t *start, const double *base, const T *g,
                 const GridParams &gp, double *out, cudaStream_t s) {
     if (n == 0) return MPS_OK;
-    k_contract_cs<T><<<grid_for(n * nrhs * 32, 256, 152 * 64), 256, 0, s>>>(grid, n, nrhs, start, base, g, gp, out);
+    // 4 vectors per warp pass (5 x 4 accumulators per lane): 99 ms against 104 for 8 over the 16-configuration
+    // batch's float32 matvecs; 16 spills
+    const int64_t items = n * ((nrhs + 3) / 4);
+    k_contract_cs<T, 4><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(grid, n, nrhs, start, base, g, gp, out);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
