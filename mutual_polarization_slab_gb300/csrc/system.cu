@@ -682,6 +682,46 @@ static int matvec_quad(mps_system *s, const double *m, double *out, int nrhs, cu
     return MPS_OK;
 }
 
+// The float32 pair sum is independent of the wave-space stages of the same
+// matvec: pair_sum_fork runs it on the system's side stream into rs_buf (from
+// the point the moments are ready on st), pair_sum_join makes st wait for it and
+// adds it into out after the contraction.  MPS_PAIR_STREAM=same keeps it on st
+// after the contraction (A/B timing); so do profiled matvecs (their stage times
+// are taken on st).
+__global__ void k_axpy1(const double *__restrict__ x, double *__restrict__ y, int64_t total);
+
+static bool pair_sum_beside(const StageEvents *ev) {
+    const char *ps = getenv("MPS_PAIR_STREAM");
+    return ev == nullptr && !(ps && strcmp(ps, "same") == 0);
+}
+
+static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t st) {
+    if (!s->side) {
+        MPS_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+        MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    }
+    // the real operator's vectors: 3 components per particle (complex systems run it on 2 nc real vectors)
+    const size_t vals = (size_t)3 * s->n * s->max_rhs;
+    if (!s->rs_buf) MPS_TRY(dalloc(&s->rs_buf, sizeof(double) * vals, st));
+    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * vals, st));
+    MPS_CUDA_TRY(cudaEventRecord(s->ev_fork, st));
+    MPS_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab,
+                               false, s->order, s->side));
+    MPS_CUDA_TRY(cudaEventRecord(s->ev_join, s->side));
+    return MPS_OK;
+}
+
+static int pair_sum_join(mps_system *s, double *out, int nrhs, cudaStream_t st) {
+    MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
+    const int64_t tot = (int64_t)nrhs * s->n * 3;
+    k_axpy1<<<grid_for(tot, 256), 256, 0, st>>>(s->rs_buf, out, tot);
+    count_launch();
+    MPS_CUDA_TRY(cudaGetLastError());
+    return MPS_OK;
+}
+
 // Polydisperse operator (CS/ComputeField.m:23-57): scalar spread of the dipoles
 // as charges, one FFT pair per vector, vector contraction, real space with the
 // per-pair couplings of the two radii.
@@ -695,6 +735,8 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
     const T *hc = dbl ? (const T *)s->cs_h64 : (const T *)s->cs_h32;
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
+    const bool beside = !dbl && pair_sum_beside(ev);
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
     STAGE_MARK(1);
     MPS_TRY(spread_cs<T>(m, s->n, nrhs, s->start, s->cs_base, g, s->gp, grid, st));
     STAGE_MARK(2);
@@ -708,6 +750,8 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(6);
     if (dbl)
         MPS_TRY(real_space_csr<double>(m, out, s->n, nrhs, s->row_ptr, s->p64, s->diag, s->diag_idx, s->slab, true, st));
+    else if (beside)
+        MPS_TRY(pair_sum_join(s, out, nrhs, st));
     else
         MPS_TRY(real_space_f32(s, m, out, nrhs, st));
     STAGE_MARK(7);
@@ -715,7 +759,6 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
 }
 
 // Gradient form of the float32 operator (gradop.cu): one scalar grid per vector.
-__global__ void k_axpy1(const double *__restrict__ x, double *__restrict__ y, int64_t total);
 
 static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     // the gradient form exists for the dipole operator only: the others run their own float32 operator
@@ -741,28 +784,10 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
-    // the pair sum is independent of the wave-space stages: unless the stages are being timed, it runs on
-    // the side stream into rs_buf and is added after the contraction (MPS_PAIR_STREAM=same keeps it on the
-    // matvec's stream after the contraction, for A/B timing)
-    const char *ps = getenv("MPS_PAIR_STREAM");
-    const bool beside = ev == nullptr && !(ps && strcmp(ps, "same") == 0);
-    if (beside) {
-        if (!s->side) {
-            MPS_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
-            MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
-            MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
-        }
-        if (!s->rs_buf) MPS_TRY(dalloc(&s->rs_buf, sizeof(double) * 3 * (size_t)s->n * s->max_rhs, st));
-        if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * 3 * (size_t)s->n * s->max_rhs, st));
-    }
+    // the pair sum runs beside the wave-space stages (pair_sum_fork / pair_sum_join)
+    const bool beside = pair_sum_beside(ev);
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
-    if (beside) {
-        MPS_CUDA_TRY(cudaEventRecord(s->ev_fork, st));
-        MPS_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
-        MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx,
-                                   s->slab, false, s->order, s->side));
-        MPS_CUDA_TRY(cudaEventRecord(s->ev_join, s->side));
-    }
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
     STAGE_MARK(1);
     MPS_TRY(spread_grad_tiled(m, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->grid32, st));
     STAGE_MARK(2);
@@ -785,15 +810,10 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
         }
     }
     STAGE_MARK(6);
-    if (beside) {
-        MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
-        const int64_t tot = (int64_t)nrhs * s->n * 3;
-        k_axpy1<<<grid_for(tot, 256), 256, 0, st>>>(s->rs_buf, out, tot);
-        count_launch();
-        MPS_CUDA_TRY(cudaGetLastError());
-    } else {
+    if (beside)
+        MPS_TRY(pair_sum_join(s, out, nrhs, st));
+    else
         MPS_TRY(real_space_f32(s, m, out, nrhs, st));
-    }
     STAGE_MARK(7);
     return MPS_OK;
 }
