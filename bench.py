@@ -597,7 +597,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     plan_s = time.perf_counter() - tw
     t0 = time.perf_counter()
-    res = batch.solve_configurations(cfgs, scal, tol=args.batch_tol, precision="mixed")
+    res = batch.solve_configurations(cfgs, scal, tol=args.batch_tol, precision="mixed", workers=args.batch_workers)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     units = sum(c.n for c in cfgs) * 3 * len(scal)
@@ -605,7 +605,7 @@ def run_batch(args):
         "workload": f"{len(cfgs)} polydisperse configurations (N {min(c.n for c in cfgs)}..{max(c.n for c in cfgs)}, "
                     f"sum {sum(c.n for c in cfgs)}), 3 fields x 16 contrast scalings each, tol {args.batch_tol}",
         "metric": "particle-solves/s", "value": units / dt, "seconds": dt,
-        "converged": sum(1 for v in res.values() if v[1]), "configs": len(cfgs),
+        "converged": sum(1 for v in res.values() if v[1]), "configs": len(cfgs), "workers": args.batch_workers,
         "distinct_grids": len(seen), "plan_warmup_seconds_untimed": plan_s}), flush=True)
 
 
@@ -635,6 +635,8 @@ def main():
                          "configurations")
     ap.add_argument("--configs", type=int, default=16, help="batch workload: number of configurations")
     ap.add_argument("--batch-tol", dest="batch_tol", type=float, default=1e-4)
+    ap.add_argument("--batch-workers", dest="batch_workers", type=int, default=4,
+                    help="batch workload: configurations solved at a time (host threads, one CUDA stream each)")
     args = ap.parse_args()
     if args.workload == "quadrupole" and args.impl != "reference":
         run_quadrupole(args)

@@ -149,17 +149,65 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
     return C, conv
 
 
+def _solve_concurrently(todo: List[Configuration], solve: Callable, workers: int) -> dict:
+    """Solve ``todo`` with ``workers`` host threads, each on its own CUDA stream,
+    taking the largest remaining configuration first.  A solve runs in the C
+    library with the GIL released, so one thread's host round trips (GMRES
+    convergence checks, result read-back) overlap the others' GPU work."""
+    import threading
+
+    import torch
+
+    dev = torch.cuda.current_device()
+    queue = sorted(todo, key=lambda c: c.n)          # pop() takes the largest
+    lock = threading.Lock()
+    results: dict = {}
+    errors: List[BaseException] = []
+
+    def work():
+        try:
+            torch.cuda.set_device(dev)
+            stream = torch.cuda.Stream()
+            with torch.cuda.stream(stream):
+                while True:
+                    with lock:
+                        if not queue or errors:
+                            break
+                        cfg = queue.pop()
+                    out = solve(cfg)
+                    with lock:
+                        results[cfg.index] = out
+            stream.synchronize()
+        except BaseException as exc:   # re-raised in the caller
+            with lock:
+                errors.append(exc)
+
+    threads = [threading.Thread(target=work) for _ in range(min(workers, len(todo)))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    return results
+
+
 def solve_configurations(configs: Sequence[Configuration], scalings, tol=1e-4, precision="mixed",
-                         solver: Optional[Callable] = None, gather=True):
+                         solver: Optional[Callable] = None, gather=True, workers=1):
     """Solve this rank's share of ``configs``; returns {index: (C, converged)} for
-    all configurations when gathered, else for this rank's share."""
+    all configurations when gathered, else for this rank's share.  ``workers`` > 1
+    solves that many configurations at a time on one GPU (one host thread and CUDA
+    stream each)."""
     import torch.distributed as dist
 
     world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
     rank = dist.get_rank() if world > 1 else 0
     parts = partition([c.n for c in configs], world)
     solve = solver or (lambda cfg: solve_configuration(cfg, scalings, tol=tol, precision=precision))
-    mine = {configs[i].index: solve(configs[i]) for i in parts[rank]}
+    if workers > 1 and len(parts[rank]) > 1:
+        mine = _solve_concurrently([configs[i] for i in parts[rank]], solve, workers)
+    else:
+        mine = {configs[i].index: solve(configs[i]) for i in parts[rank]}
     if world == 1 or not gather:
         return mine
     everything: List[Optional[dict]] = [None] * world

@@ -9,16 +9,22 @@
 // explicitly rounded operations (no FMA contraction) so they match numpy's.
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "cells.cuh"
 
 namespace mps {
 
 __constant__ int c_off27[27][3];
 
-static bool g_off_ready = false;
+static std::atomic<bool> g_off_ready{false};
+static std::mutex g_off_mu;
 
 static int ensure_offsets() {
-    if (g_off_ready) return MPS_OK;
+    if (g_off_ready.load(std::memory_order_acquire)) return MPS_OK;
+    std::lock_guard<std::mutex> lk(g_off_mu);   // systems may be built from several host threads
+    if (g_off_ready.load(std::memory_order_relaxed)) return MPS_OK;
     int h[27][3];
     int k = 0;
     for (int a = -1; a <= 1; ++a)
@@ -30,7 +36,7 @@ static int ensure_offsets() {
                 ++k;
             }
     MPS_CUDA_TRY(cudaMemcpyToSymbol(c_off27, h, sizeof(h)));
-    g_off_ready = true;
+    g_off_ready.store(true, std::memory_order_release);
     return MPS_OK;
 }
 

@@ -610,12 +610,12 @@ int df_plan(const GridParams &gp, DfPlan3 *out) {
 }
 
 static int max_smem_optin() {
-    static int v = -1;
-    if (v < 0) {
-        int dev = 0;
+    static const int v = [] {   // thread-safe one-time initialisation
+        int dev = 0, r = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) v = 48 * 1024;
-    }
+        if (cudaDeviceGetAttribute(&r, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) r = 48 * 1024;
+        return r;
+    }();
     return v;
 }
 

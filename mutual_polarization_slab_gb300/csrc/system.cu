@@ -195,9 +195,11 @@ static void free_system(mps_system *s) {
 // with its release threshold raised, so building a system for the next
 // configuration reuses the previous one's memory instead of mapping new pages.
 static void configure_pool_once() {
+    static std::mutex mu;
     static int done_dev = -1;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lk(mu);
     if (done_dev == dev) return;
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {

@@ -15,6 +15,7 @@
 // (EW/ewald.py:370-467) up to summation order.
 #include "tiles.cuh"
 
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include "dfloat.cuh"
@@ -454,11 +455,11 @@ static int contract_launch(const TG *grid, int64_t n, int r0, const int32_t *sta
                            const GridParams &gp, const TileBins &tb, TP *partial, double *out, cudaStream_t s) {
     constexpr int C = 3 * NR;
     const size_t smem = sizeof(T) * ((size_t)C * TZ * kTileY * kRowPad + 8 * 3 * kMaxP);
-    static bool attr_set = false;  // one attribute call per instantiation
-    if (!attr_set) {
+    static std::atomic<bool> attr_set{false};  // one attribute call per instantiation (a repeat is harmless)
+    if (!attr_set.load(std::memory_order_acquire)) {
         MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_tiled<T, TZ, NR, TG, TP, TW>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
+        attr_set.store(true, std::memory_order_release);
     }
     k_contract_tiled<T, TZ, NR, TG, TP, TW><<<(unsigned)tb.ntiles, 256, smem, s>>>(
         grid, r0, start, w, gp, tb.tile_start, tb.entries, tb.ntx, tb.nty, partial);
