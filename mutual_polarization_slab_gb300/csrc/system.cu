@@ -117,6 +117,8 @@ struct mps_system {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_res = nullptr;    // GMRES: residual estimates read back (a matvec may be queued behind it)
+    cudaEvent_t ev_diag = nullptr;   // the last upload of the permittivity-set indices
+    int diag_up_n = 0;               // entries of diag_idx that match diag_idx_host (0: none uploaded yet)
     double *rs_buf = nullptr;        // max_rhs x n x 3: the pair-sum part of a float32 matvec
     // complex permittivities: vectors are (Re m, Im m) per particle (ndof 6); the real operator runs on the
     // 2 nc real vectors [Re m_0..Re m_{nc-1}, Im m_0..Im m_{nc-1}] and the imaginary diagonal couples them
@@ -178,12 +180,14 @@ static void free_system(mps_system *s) {
                     s->cx_in, s->cx_out};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
+    if (s->ev_diag) cudaEventSynchronize(s->ev_diag);   // the last index upload reads the pinned block
     if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
     if (s->rs_buf) cudaFreeAsync(s->rs_buf, s->stream);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->ev_res) cudaEventDestroy(s->ev_res);
+    if (s->ev_diag) cudaEventDestroy(s->ev_diag);
     tile_bins_free(s->tb64, s->stream);
     tile_bins_free(s->tb32, s->stream);
     if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
@@ -316,16 +320,28 @@ static int ensure_grids(mps_system *s, int precision, cudaStream_t st) {
 }
 
 static int upload_diag_idx(mps_system *s, const int32_t *diag_index, int nrhs, cudaStream_t st) {
-    // stage through pinned memory so the async copy does not read caller memory late
-    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    const int nup = s->cplx ? 2 * nrhs : nrhs;
+    std::vector<int32_t> want(nup);
     for (int r = 0; r < nrhs; ++r) {
         int32_t v = diag_index ? diag_index[r] : 0;
         if (v < 0 || v >= s->n_diag) return MPS_BAD_ARG;
-        s->diag_idx_host[r] = v;
-        if (s->cplx) s->diag_idx_host[nrhs + r] = v;   // the imaginary halves use the same sets
+        want[r] = v;
+        if (s->cplx) want[nrhs + r] = v;   // the imaginary halves use the same sets
     }
-    const int nup = s->cplx ? 2 * nrhs : nrhs;
+    // unchanged since the last upload (the usual case for repeated matvecs): no copy and no host wait, only
+    // stream order behind the copy that put them there
+    if (s->diag_up_n == nup && std::equal(want.begin(), want.end(), s->diag_idx_host)) {
+        if (s->ev_diag) MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_diag, 0));
+        return MPS_OK;
+    }
+    // stage through pinned memory so the async copy does not read caller memory late; the previous copy must
+    // have finished reading the staging buffer before it is overwritten
+    if (!s->ev_diag) MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_diag, cudaEventDisableTiming));
+    else MPS_CUDA_TRY(cudaEventSynchronize(s->ev_diag));
+    std::copy(want.begin(), want.end(), s->diag_idx_host);
     MPS_CUDA_TRY(cudaMemcpyAsync(s->diag_idx, s->diag_idx_host, sizeof(int32_t) * nup, cudaMemcpyHostToDevice, st));
+    MPS_CUDA_TRY(cudaEventRecord(s->ev_diag, st));
+    s->diag_up_n = nup;
     return MPS_OK;
 }
 
