@@ -21,6 +21,8 @@ from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
+from .system import fft_size  # noqa: F401  (part of this module's interface)
+
 __all__ = ["Configuration", "make_configurations", "partition", "solve_configuration", "solve_configurations"]
 
 
@@ -78,18 +80,6 @@ def _eps(beta):
     return (1.0 + 2.0 * beta) / (1.0 - beta)
 
 
-def fft_size(n: int) -> int:
-    """Smallest m >= n whose prime factors are 2, 3 and 5 (radices cuFFT runs
-    fast; few such sizes, so many configurations share their plans)."""
-    m = max(int(n), 1)
-    while True:
-        k = m
-        for p in (2, 3, 5):
-            while k % p == 0:
-                k //= p
-        if k == 1:
-            return m
-        m += 1
 
 
 def grid_for(box, xi, tol, fft_friendly=True):

@@ -30,7 +30,7 @@ import torch
 
 from . import _lib as L
 from . import ewald
-from .system import SpectralEwaldSystem, as_device, spectral_parameters
+from .system import SpectralEwaldSystem, as_device, fft_size, spectral_parameters
 
 __all__ = ["TABLE_ORDER", "real_space_table", "default_table", "QuadrupoleSystem", "matrix_vector_multiply",
            "matrix_vector_multiply_flat", "matrix_vector_solve", "capacitance_tensor",
@@ -67,9 +67,13 @@ def default_table(xi, rmin=0.001, dr=0.001, rmax=10.0):
     return _TABLE_CACHE[key]
 
 
-def _params(box, xi, errortol, rc, Ngrid, P):
+def _params(box, xi, errortol, rc, Ngrid, P, fft_friendly=False):
     rc0, Ng0, _, P0, _ = spectral_parameters(box, xi, errortol)
     rc = rc0 if rc is None else float(rc)
+    if Ngrid is None and fft_friendly:
+        # each axis of the rule's grid rounded up to a 5-smooth size: a finer grid (at least the rule's accuracy;
+        # the support P of the rule does not depend on the spacing) that cuFFT transforms without prime factors
+        Ngrid = np.array([fft_size(int(v)) for v in Ng0], dtype=np.int64)
     Ngrid = Ng0 if Ngrid is None else np.asarray(Ngrid, dtype=np.int64).reshape(3)
     P = P0 if P is None else int(P)
     box = np.asarray(box, dtype=np.float64).reshape(3)
@@ -85,14 +89,15 @@ class QuadrupoleSystem(SpectralEwaldSystem):
 
     ``tables``/``r_vals`` default to ``default_table(xi)``; ``errortol`` fixes
     rc, grid and support as ``CQ/CapacitanceTensor.m:30-36`` (each may be
-    overridden).  ``lambda_p`` may hold several permittivity sets (K, N)."""
+    overridden; ``fft_friendly=True`` rounds each axis of that grid up to a
+    5-smooth size).  ``lambda_p`` may hold several permittivity sets (K, N)."""
 
     def __init__(self, x, lambda_p, box, xi, errortol, tables=None, r_vals=None, *, rc=None, Ngrid=None, P=None,
-                 max_rhs=3):
+                 max_rhs=3, fft_friendly=False):
         if tables is None:
             tables, r_vals = default_table(xi)
         tables = as_device(tables).reshape(9, -1)
-        rc, Ngrid, P, eta = _params(box, xi, errortol, rc, Ngrid, P)
+        rc, Ngrid, P, eta = _params(box, xi, errortol, rc, Ngrid, P, fft_friendly)
         super().__init__(x, lambda_p, box, xi, rc, Ngrid, P, tables[0], tables[1], r_vals, slab_factor=0.0,
                          eta=eta, max_rhs=max_rhs, quad_tables=tables[2:])
         self.errortol = float(errortol)

@@ -49,6 +49,20 @@ def spectral_parameters(box, xi, errortol):
     return rc, Ngrid, h, P, eta
 
 
+def fft_size(n: int) -> int:
+    """Smallest m >= n whose prime factors are 2, 3 and 5 (radices cuFFT runs
+    fast; few such sizes, so many configurations share their plans)."""
+    m = max(int(n), 1)
+    while True:
+        k = m
+        for p in (2, 3, 5):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m += 1
+
+
 class SpectralEwaldSystem:
     """Precomputed geometry of one configuration and its batched operator.
 

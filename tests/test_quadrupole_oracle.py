@@ -142,3 +142,22 @@ def test_tensor_solve_converges():
     # column i is the mean dipole for the field along i
     np.testing.assert_allclose(C[:, 1], S[:, :, 1].mean(axis=0))
     assert np.all(np.diag(C) > 0)
+
+
+def test_fft_friendly_grid_rule():
+    """``fft_friendly`` rounds each axis of the tolerance rule's grid up to a
+    5-smooth size and keeps the rule's cutoff and support (host logic only)."""
+    torch = pytest.importorskip("torch")  # noqa: F841  (the package imports torch)
+    from mutual_polarization_slab_gb300 import quadrupole as gq
+    from mutual_polarization_slab_gb300.system import fft_size, spectral_parameters
+
+    box = np.array([69.2820323, 69.2820323, 74.0])
+    xi, tol = 0.6506, 1e-4
+    rc0, ng0, _, P0, _ = spectral_parameters(box, xi, tol)
+    rc, ng, P, eta = gq._params(box, xi, tol, None, None, None, fft_friendly=True)
+    assert list(ng0) == [89, 89, 95] and list(ng) == [90, 90, 96]
+    assert rc == rc0 and P == P0
+    assert all(fft_size(int(v)) == int(v) for v in ng)
+    np.testing.assert_allclose(eta, P * (box / ng * xi) ** 2 / np.pi)
+    rc, ng_rule, _, _ = gq._params(box, xi, tol, None, None, None)
+    assert list(ng_rule) == [89, 89, 95]
