@@ -601,7 +601,11 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
 // tiled spread and contraction accumulate in double-float arithmetic (float64
 // weights and grids), the FFTs and Green's scale are the double-float transforms
 // of dffft.cu; the pair sum is the float64 kernel.
-static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+// Wave-space field grids of nrhs moment vectors with the float64-accurate operator: double-float spread,
+// FFTs and dipole scale; the 3 nrhs component grids are left in s->grid64 as (hi, lo) float pairs.  Stage
+// marks 2..5 of the calling matvec (ev may be null).
+static int df_field_grids(mps_system *s, const double *m, int nrhs, StageEvents *ev, cudaStream_t st,
+                          bool *use_tiles_out) {
     const int64_t nw = (int64_t)s->n * 3 * s->gp.P;
     if (!s->wdf) {
         MPS_TRY(dalloc(&s->wdf, sizeof(dfv) * (size_t)nw, st));
@@ -621,11 +625,6 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     }
     dfv *grid = (dfv *)s->grid64;           // (hi, lo) float pairs: the size of a double
     float4 *spec = (float4 *)s->spec64;     // float4 per complex value: the size of a double2
-    const double vol = s->box[0] * s->box[1] * s->box[2];
-    StageEvents *ev = nullptr;
-    MPS_TRY(stage_begin(s, MPS_DF, &ev, st));
-    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
-    STAGE_MARK(1);
     const int64_t gvals = (int64_t)3 * nrhs * s->gp.G;
     if (use_tiles) {
         MPS_TRY(spread_tiled_df(m, s->n, nrhs, s->start, s->wdf, s->gp, s->tb64, grid, st));
@@ -640,6 +639,20 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     STAGE_MARK(4);
     MPS_TRY(df_inverse_yx(spec, (float2 *)grid, 3 * nrhs, s->gp, s->dfp, st));
     STAGE_MARK(5);
+    *use_tiles_out = use_tiles;
+    return MPS_OK;
+}
+
+static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    const double vol = s->box[0] * s->box[1] * s->box[2];
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, MPS_DF, &ev, st));
+    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    STAGE_MARK(1);
+    bool use_tiles = false;
+    MPS_TRY(df_field_grids(s, m, nrhs, ev, st, &use_tiles));
+    dfv *grid = (dfv *)s->grid64;
+    const int64_t gvals = (int64_t)3 * nrhs * s->gp.G;
     const char *ce = getenv("MPS_DF_CONTRACT");   // "tiled": the tiled contraction (A/B timing)
     const bool tiled_contract = use_tiles && ce && strcmp(ce, "tiled") == 0;
     if (s->gp.P <= kMaxP && !tiled_contract) {
@@ -2272,12 +2285,20 @@ extern "C" int mps_adjoint_forces(mps_system *sys, const double *m, const double
     int rc = MPS_OK;
     if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) rc = MPS_CUDA_ERR;
     if (!rc) rc = rs_force(m, n, sys->row_ptr, sys->p64, perp, para, rvals, n_tab, forces, err, st);
-    // wave space: phi = IFFT(scale(FFT(spread(m)))) in float64, then the weight-gradient contraction
-    if (!rc) rc = ensure_grids(sys, MPS_FP64, st);
-    if (!rc) rc = spread<double>(m, n, 1, sys->start, sys->w64, sys->gp, sys->grid64, st);
-    if (!rc) rc = exec_plan(sys, CUFFT_D2Z, 3, sys->grid64, sys->spec64, 0, st);
-    if (!rc) rc = scale_half<double>(sys->spec64, 1, sys->gp, sys->h64, st);
-    if (!rc) rc = exec_plan(sys, CUFFT_Z2D, 3, sys->spec64, sys->grid64, 0, st);
+    // wave space: phi = IFFT(scale(FFT(spread(m)))), float64-accurate, then the weight-gradient contraction.
+    // Grids the double-float FFTs support take the double-float pipeline (float64 issue is slow on GB300) and
+    // convert phi to float64 in place; the others use the float64 spread and cuFFT.
+    if (!rc && df_usable(sys)) {
+        bool tiles_used = false;
+        rc = df_field_grids(sys, m, 1, nullptr, st, &tiles_used);
+        if (!rc) rc = dfv_to_f64_inplace(sys->grid64, 3 * sys->gp.G, st);
+    } else if (!rc) {
+        rc = ensure_grids(sys, MPS_FP64, st);
+        if (!rc) rc = spread<double>(m, n, 1, sys->start, sys->w64, sys->gp, sys->grid64, st);
+        if (!rc) rc = exec_plan(sys, CUFFT_D2Z, 3, sys->grid64, sys->spec64, 0, st);
+        if (!rc) rc = scale_half<double>(sys->spec64, 1, sys->gp, sys->h64, st);
+        if (!rc) rc = exec_plan(sys, CUFFT_Z2D, 3, sys->spec64, sys->grid64, 0, st);
+    }
     if (!rc) rc = wave_force(sys->grid64, sys->x, m, n, sys->start, sys->w64, sys->gp, forces, st);
     if (!rc && dE_deps) {
         double self = 0.0;
