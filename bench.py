@@ -36,14 +36,18 @@ METRIC = "particle-solves/s at N=1e5 (3-direction capacitance tensor, rel. momen
 UNIT = "particle-solves/s"
 
 
+def workload_params(n=100_000, phi=0.3, beta=0.9, grid=192, P=10):
+    """The workload's parameters without its positions (rc from about 60 neighbours, xi = 4 / rc)."""
+    rc = (60.0 / phi) ** (1.0 / 3.0)
+    return dict(rc=rc, xi=4.0 / rc, Ngrid=np.array([grid, grid, grid]), P=P, n=n, phi=phi, beta=beta)
+
+
 def workload(n=100_000, phi=0.3, seed=2, beta=0.9, grid=192, P=10):
     from mutual_polarization_slab_gb300.workloads import rsa
     x, box, _ = rsa(n, phi, seed=seed)
-    rc = (60.0 / phi) ** (1.0 / 3.0)
-    xi = 4.0 / rc
-    eps = np.full(n, (1.0 + 2.0 * beta) / (1.0 - beta))
-    Ng = np.array([grid, grid, grid])
-    return dict(x=x, box=box, eps=eps, rc=rc, xi=xi, Ngrid=Ng, P=P, n=n, phi=phi, beta=beta)
+    w = workload_params(n=n, phi=phi, beta=beta, grid=grid, P=P)
+    w.update(x=x, box=box, eps=np.full(n, (1.0 + 2.0 * beta) / (1.0 - beta)))
+    return w
 
 
 def config_dict(w, extra=None):
@@ -425,7 +429,7 @@ def run_reference(args):
     nproc = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(nproc))
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(nproc))
-    w = workload(n=args.cpu_n, grid=2)
+    w = workload_params(n=args.n, grid=args.grid)   # the GPU arm's workload; each step times a bounded sample of it
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_sample(n=args.cpu_n)
     vals, dts = [], []
