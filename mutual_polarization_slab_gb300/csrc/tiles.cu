@@ -504,9 +504,11 @@ int contract_tiled_df(const dfv *grid, int64_t n, int nrhs, const int32_t *start
 // the stencil's (x, y) columns; each column's z sum over the 3*NR grids runs in
 // a ProdAcc<dfv> (exact leading products, two-sum, unnormalised within the
 // column), then the column sums are weighted by wx*wy in double-float.  Fixed
-// summation order: deterministic.
+// summation order: deterministic.  Bounds of 3 blocks per SM let ptxas keep more
+// loads in flight (72 registers for one vector; 1.19 ms per residual matvec at the
+// bench workload against 1.30 ms with 56 registers under the default heuristic).
 template <int NR>
-__global__ void __launch_bounds__(256) k_contract_df_warp(const dfv *__restrict__ grid, int64_t n, int r0,
+__global__ void __launch_bounds__(256, 3) k_contract_df_warp(const dfv *__restrict__ grid, int64_t n, int r0,
                                                           const int32_t *__restrict__ order,
                                                           const int32_t *__restrict__ start,
                                                           const dfv *__restrict__ w, GridParams gp,
