@@ -274,8 +274,8 @@ __global__ void k_cs_green(GridParams gp, double eta, double xi, double *__restr
 // footprint.  The particle's node weights K(d)/d (P^3 per particle) are read once
 // per block of vectors instead of once per vector: with a spectrum batch (3 fields x
 // K contrasts) they were the dominant read.
-template <typename T, int RB>
-__global__ void __launch_bounds__(256) k_spread_cs(const double *__restrict__ m, int64_t n, int nrhs,
+template <typename T, int RB, int MB = 1>
+__global__ void __launch_bounds__(256, MB) k_spread_cs(const double *__restrict__ m, int64_t n, int nrhs,
                                                    const int32_t *__restrict__ start, const double *__restrict__ base,
                                                    const T *__restrict__ g, GridParams gp, T *__restrict__ grid) {
     const int lane = threadIdx.x & 31;
@@ -343,8 +343,8 @@ __global__ void k_scale_cs(T *__restrict__ spec, int nrhs, int64_t Gc, const T *
 // Contract: out = prod(h) sum_nodes K(d)/d (node - x) E~(node)  (overwrites).
 // A warp per (particle, block of RB vectors): the node weights are read once per
 // block; each vector's sums run in the same order as with one vector per warp.
-template <typename T, int RB>
-__global__ void __launch_bounds__(256) k_contract_cs(const T *__restrict__ grid, int64_t n, int nrhs,
+template <typename T, int RB, int MB = 1>
+__global__ void __launch_bounds__(256, MB) k_contract_cs(const T *__restrict__ grid, int64_t n, int nrhs,
                                                      const int32_t *__restrict__ start,
                                                      const double *__restrict__ base, const T *__restrict__ g,
                                                      GridParams gp, double *__restrict__ out) {
@@ -458,7 +458,10 @@ int spread_cs(const double *m, int64_t n, int nrhs, const int32_t *start, const 
     if (n == 0) return MPS_OK;
     // 8 vectors per warp pass (the node weights read once per 8 vectors); 4 and 16 measured slower
     const int64_t items = n * ((nrhs + 7) / 8);
-    k_spread_cs<T, 8><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(m, n, nrhs, start, base, g, gp, grid);
+    // float: bounds of 4 blocks per SM (72.8 ms over the 16-configuration batch's float32 matvecs against 75.8
+    // unbounded); double: unbounded (a 64-register cap spills it)
+    constexpr int MB = sizeof(T) == 4 ? 4 : 1;
+    k_spread_cs<T, 8, MB><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(m, n, nrhs, start, base, g, gp, grid);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
@@ -478,7 +481,9 @@ int contract_cs(const T *grid, int64_t n, int nrhs, const int32_t *start, const 
     // 4 vectors per warp pass (5 x 4 accumulators per lane): 99 ms against 104 for 8 over the 16-configuration
     // batch's float32 matvecs; 16 spills
     const int64_t items = n * ((nrhs + 3) / 4);
-    k_contract_cs<T, 4><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(grid, n, nrhs, start, base, g, gp, out);
+    // float: bounds of 3 blocks per SM (76 registers: 83 ms over the batch's float32 matvecs against 99 at 64)
+    constexpr int MB = sizeof(T) == 4 ? 3 : 1;
+    k_contract_cs<T, 4, MB><<<grid_for(items * 32, 256, 152 * 64), 256, 0, s>>>(grid, n, nrhs, start, base, g, gp, out);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
