@@ -77,8 +77,10 @@ __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, f
 // for 32 (fewer barriers, and the warps' uneven shares of a chunk even out), 0.306 for 64 and 0.301 for 128
 constexpr int kGChunk = 96;
 
+// Bounds of 5 blocks per SM (48 registers, 36.5 KB of shared memory each): 0.293 ms per launch at the bench
+// workload against 0.299 at 4 blocks (64 registers), 0.300 at 6 (spills) and 0.342 unbounded.
 template <int TZ, int NR>
-__global__ void __launch_bounds__(256) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
+__global__ void __launch_bounds__(256, 5) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
                                                            const int32_t *__restrict__ start,
                                                            const float *__restrict__ w, const float *__restrict__ g,
                                                            GridParams gp, const int64_t *__restrict__ tstart,
