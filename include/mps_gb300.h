@@ -362,10 +362,14 @@ int mps_dipole_forces(const double *pos, const double *dip, int64_t n, const dou
  * receives the pair count.  Returns MPS_SCRATCH_LIMIT, before touching the GPU,
  * when mps_neighbor_list_workspace(n, ncell) exceeds the scratch (roughly
  * n > 32,000 particles), and MPS_SCRATCH_LIMIT with *n_pairs set when the pairs
- * do not fit in max_pairs.  The first call on a device looks up that device's
- * scratch address; make it before any stream capture.  All calls share the one
- * array: calls whose GPU work overlaps race, so serialise them.  Synchronises
- * the stream (the pair count is data dependent). */
+ * do not fit in max_pairs, and MPS_BAD_ARG, also before touching the GPU, when
+ * a cell count is below 1 or the cell counts' product overflows.  The first call
+ * on a device looks up that device's scratch address; make it before any stream
+ * capture.  The call waits for the pair count (data dependent), then queues the
+ * fill on `stream` and returns: p1/p2 are ready only in the order of `stream`,
+ * and the scratch stays in use until that fill has run.  All calls share the one
+ * array: calls whose GPU work overlaps (other streams, other host threads) race,
+ * so serialise them. */
 int mps_neighbor_list_noalloc(const int64_t *cell, int64_t n, const int64_t *ncell, int64_t *p1, int64_t *p2,
                               int64_t max_pairs, int64_t *n_pairs, mps_stream_t stream);
 
@@ -386,6 +390,13 @@ int mps_system_profile(mps_system *sys, int32_t enable);
  * stages 0..6] in milliseconds, count[3] = matvecs recorded per precision.
  * Resets the accumulators. */
 int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count);
+
+/* Drops the process's cache of Green's coefficients and scale tensors (keyed by
+ * device, grid, box, xi and eta; shared by systems built on the same grid), so
+ * the next system built recomputes its k-space data, as the reference does on
+ * every capacitance() call (EW/capacitance.py:385).  Systems that hold
+ * coefficients keep them until destroyed.  Host only; no GPU work. */
+int mps_kspace_cache_clear(void);
 
 /* Tile depth the autotuner chose for the tiled kernels: tile_depth[0] for the
  * float64-width tiles (float64 or double-float spread, whichever ran first),

@@ -9,36 +9,9 @@
 // explicitly rounded operations (no FMA contraction) so they match numpy's.
 #include <string.h>
 
-#include <atomic>
-#include <mutex>
-
 #include "cells.cuh"
 
 namespace mps {
-
-__constant__ int c_off27[27][3];
-
-static std::atomic<bool> g_off_ready{false};
-static std::mutex g_off_mu;
-
-static int ensure_offsets() {
-    if (g_off_ready.load(std::memory_order_acquire)) return MPS_OK;
-    std::lock_guard<std::mutex> lk(g_off_mu);   // systems may be built from several host threads
-    if (g_off_ready.load(std::memory_order_relaxed)) return MPS_OK;
-    int h[27][3];
-    int k = 0;
-    for (int a = -1; a <= 1; ++a)
-        for (int b = -1; b <= 1; ++b)
-            for (int c = -1; c <= 1; ++c) {
-                h[k][0] = a;
-                h[k][1] = b;
-                h[k][2] = c;
-                ++k;
-            }
-    MPS_CUDA_TRY(cudaMemcpyToSymbol(c_off27, h, sizeof(h)));
-    g_off_ready.store(true, std::memory_order_release);
-    return MPS_OK;
-}
 
 // ---------------------------------------------------------------------------
 // Kernels
@@ -97,11 +70,14 @@ __global__ void k_cell_rank(const int32_t *__restrict__ unsorted, const int32_t 
     }
 }
 
+// Neighbour cell o (0..26) of cell c: offsets (o / 9 - 1, o / 3 % 3 - 1, o % 3 - 1), the x offset
+// outermost as in the reference's loop.  Computed, not read from a __constant__ table, so the kernels
+// need no per-device upload and give the same offsets on every GPU of the process.
 __device__ __forceinline__ int32_t nb_cell(int32_t c, int o, int64_t ncx, int64_t ncy, int64_t ncz) {
     int64_t cx = c % ncx, cy = (c / ncx) % ncy, cz = c / (ncx * ncy);
-    cx = wrap_index(cx + c_off27[o][0], ncx);
-    cy = wrap_index(cy + c_off27[o][1], ncy);
-    cz = wrap_index(cz + c_off27[o][2], ncz);
+    cx = wrap_index(cx + (o / 9 - 1), ncx);
+    cy = wrap_index(cy + ((o / 3) % 3 - 1), ncy);
+    cz = wrap_index(cz + (o % 3 - 1), ncz);
     return (int32_t)(cx + ncx * (cy + ncy * cz));
 }
 
@@ -993,8 +969,6 @@ static void *carve(char *&p, size_t bytes) {
 }
 
 int cell_bins_build(const int64_t *cell3, int64_t n, const int64_t *ncell, void *ws, CellBins &cb, cudaStream_t s) {
-    int rc = ensure_offsets();
-    if (rc) return rc;
     int64_t ncells = ncell[0] * ncell[1] * ncell[2];
     char *p = (char *)ws;
     cb.ncell[0] = ncell[0];
@@ -1014,7 +988,7 @@ int cell_bins_build(const int64_t *cell3, int64_t n, const int64_t *ncell, void 
     MPS_CUDA_TRY(cudaMemsetAsync(cb.cursor, 0, (size_t)ncells * 4, s));
     k_cell_lin<<<grid_for(n, 256), 256, 0, s>>>(cell3, n, ncell[0], ncell[1], ncell[2], cb.lin, cb.counts);
     MPS_LAUNCH_CHECK();
-    rc = exclusive_scan_i32_to_i64(cb.counts, cb.starts, ncells, scan_tmp, s);
+    int rc = exclusive_scan_i32_to_i64(cb.counts, cb.starts, ncells, scan_tmp, s);
     if (rc) return rc;
     k_cell_scatter<<<grid_for(n, 256), 256, 0, s>>>(cb.lin, n, cb.starts, cb.cursor, cb.unsorted);
     MPS_LAUNCH_CHECK();
@@ -1287,6 +1261,18 @@ extern "C" int mps_cell_list(const double *x, int64_t n, const double *box, doub
     return cell_assign(x, n, box, ncell, cell, (cudaStream_t)stream);
 }
 
+// The kernels index particles and cells with int32 (cell linear index, sorted ids) and the slot
+// arrays with 27 n entries: reject sizes whose products would wrap before anything is sized from them.
+static bool nl_sizes_ok(int64_t n, const int64_t *ncell) {
+    if (n < 0 || n > INT32_MAX / 27) return false;
+    int64_t ncells = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (ncell[d] < 1 || ncell[d] > INT32_MAX) return false;
+        if (__builtin_mul_overflow(ncells, ncell[d], &ncells)) return false;
+    }
+    return ncells <= INT32_MAX;
+}
+
 static size_t nl_layout(int64_t n, const int64_t *ncell, size_t *bins_bytes) {
     int64_t ncells = ncell[0] * ncell[1] * ncell[2];
     size_t b = cell_bins_bytes(n, ncells);
@@ -1298,6 +1284,7 @@ static size_t nl_layout(int64_t n, const int64_t *ncell, size_t *bins_bytes) {
 }
 
 extern "C" size_t mps_neighbor_list_workspace(int64_t n, const int64_t *ncell) {
+    if (!ncell || !nl_sizes_ok(n, ncell)) return SIZE_MAX;
     size_t bb;
     return nl_layout(n, ncell, &bb) + 256;
 }
@@ -1305,8 +1292,7 @@ extern "C" size_t mps_neighbor_list_workspace(int64_t n, const int64_t *ncell) {
 static int nl_common(const int64_t *cell, int64_t n, const int64_t *ncell, void *ws, size_t ws_bytes, CellBins &cb,
                      int64_t *&slot_cnt, int64_t *&slot_off, void *&scan_tmp, cudaStream_t s) {
     if (n < 0 || !ncell || !ws) return MPS_BAD_ARG;
-    for (int d = 0; d < 3; ++d)
-        if (ncell[d] < 1) return MPS_BAD_ARG;
+    if (!nl_sizes_ok(n, ncell)) return MPS_BAD_ARG;
     size_t bb;
     if (ws_bytes < nl_layout(n, ncell, &bb)) return MPS_BAD_ARG;
     int r = cell_bins_build(cell, n, ncell, ws, cb, s);

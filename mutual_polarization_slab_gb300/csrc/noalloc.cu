@@ -56,8 +56,11 @@ extern "C" int mps_neighbor_list_noalloc(const int64_t *cell, int64_t n, const i
     for (int d = 0; d < 3; ++d)
         if (ncell[d] < 1) return MPS_BAD_ARG;
     if (n == 0) return MPS_OK;
-    // size check first: nothing touches the GPU for an input that cannot fit
+    // size checks first: nothing touches the GPU for an input that cannot fit.  Cell counts whose
+    // product would overflow (or exceed the kernels' int32 cell index) are bad input, not a size
+    // that merely misses the scratch.
     const size_t need = mps_neighbor_list_workspace(n, ncell);
+    if (need == SIZE_MAX) return MPS_BAD_ARG;
     if (need > (size_t)MPS_NOALLOC_SCRATCH_BYTES) return MPS_SCRATCH_LIMIT;
     void *ws = nullptr;
     int rc = scratch_for_current_device(&ws);

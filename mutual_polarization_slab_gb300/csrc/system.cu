@@ -23,13 +23,25 @@
 
 using namespace mps;
 
-// cuFFT plans are cached per process, keyed by (type, grid, batch), so building a
-// new system for a new configuration of the same grid creates no plan.  Each
-// system owns its work area; the (work area, stream, exec) sequence is issued
-// under one mutex.
+// Ordinal of the current device: every process-wide cache below is keyed by it, because a cuFFT plan,
+// a device buffer and a timing all belong to the device that made them.
+static int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return dev;
+}
+
+// cuFFT plans are cached per process, keyed by (device, type, grid, batch), so
+// building a new system for a new configuration of the same grid creates no plan.
+// Each system owns its work area; the (work area, stream, exec) sequence is
+// issued under one mutex.
 struct PlanKey {
-    int type, nx, ny, nz, batch;
+    int dev, type, nx, ny, nz, batch;
     bool operator<(const PlanKey &o) const {
+        if (dev != o.dev) return dev < o.dev;
         if (type != o.type) return type < o.type;
         if (nx != o.nx) return nx < o.nx;
         if (ny != o.ny) return ny < o.ny;
@@ -45,9 +57,14 @@ static std::map<PlanKey, CachedPlan> g_plans;
 static std::mutex g_plan_mu;
 
 // Green's coefficients depend only on (grid, box, xi, eta): cached per process
-// (like the FFT plans) and shared by every system built on the same grid.
+// and device (like the FFT plans) and shared by every system built on the same
+// grid.  Each buffer is filled on the stream of the system that needed it first;
+// an event recorded there after the fill orders every other system's stream
+// behind it (cudaStreamWaitEvent) before that system first reads the buffer.
+// mps_kspace_cache_clear drops the cache (systems keep their references).
 struct GreenKey {
     int N[3];
+    int dev;
     double box[3], xi, eta[3];
     bool operator<(const GreenKey &o) const { return memcmp(this, &o, sizeof(GreenKey)) < 0; }
 };
@@ -56,13 +73,24 @@ struct GreenCoef {
     float *h32 = nullptr;
     float *hs32 = nullptr;   // H / |k|^2 of the gradient-form float32 operator (built on first use)
     float2 *tm6 = nullptr;   // double-float scale tensor H q q^T, 6 x Gc (built on first use)
+    cudaEvent_t ev_h = nullptr, ev_hs32 = nullptr, ev_tm6 = nullptr;   // recorded after each fill
     ~GreenCoef() {
         if (h64) cudaFree(h64);
         if (h32) cudaFree(h32);
         if (hs32) cudaFree(hs32);
         if (tm6) cudaFree(tm6);
+        if (ev_h) cudaEventDestroy(ev_h);
+        if (ev_hs32) cudaEventDestroy(ev_hs32);
+        if (ev_tm6) cudaEventDestroy(ev_tm6);
     }
 };
+
+// Records "buffer filled" on the filling stream.
+static int green_mark_filled(cudaEvent_t *ev, cudaStream_t st) {
+    if (!*ev) MPS_CUDA_TRY(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    MPS_CUDA_TRY(cudaEventRecord(*ev, st));
+    return MPS_OK;
+}
 static std::map<GreenKey, std::shared_ptr<GreenCoef>> g_green;
 static std::mutex g_green_mu;
 constexpr size_t kGreenCacheMax = 4;
@@ -161,6 +189,8 @@ struct mps_system {
     int resid_prec = MPS_FP64;   // operator of the refinement residuals
     float *g32 = nullptr;        // gradient factors dw_d/dr of the gradient-form operator, n x 3 x P
     int inner_prec = MPS_FP32;   // operator of the mixed solve's inner GMRES
+    // this system's stream has waited for the shared lazily built Green's buffers (hs32, tm6)
+    bool hs32_ready = false, tm6_ready = false;
 };
 
 static void free_system(mps_system *s) {
@@ -200,17 +230,18 @@ static void free_system(mps_system *s) {
 // configuration reuses the previous one's memory instead of mapping new pages.
 static void configure_pool_once() {
     static std::mutex mu;
-    static int done_dev = -1;
+    static std::vector<bool> done;   // per device ordinal
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return;
     std::lock_guard<std::mutex> lk(mu);
-    if (done_dev == dev) return;
+    if ((size_t)dev < done.size() && done[dev]) return;
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
         uint64_t thr = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
-    done_dev = dev;
+    if ((size_t)dev >= done.size()) done.resize(dev + 1, false);
+    done[dev] = true;
 }
 
 template <typename P>
@@ -250,7 +281,7 @@ static int dalloc_persistent(P **p, size_t bytes) {
 
 static int get_plan(cufftType type, const GridParams &gp, int batch, CachedPlan *out) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
-    PlanKey key{(int)type, gp.N[0], gp.N[1], gp.N[2], batch};
+    PlanKey key{current_device(), (int)type, gp.N[0], gp.N[1], gp.N[2], batch};
     auto it = g_plans.find(key);
     if (it != g_plans.end()) {
         *out = it->second;
@@ -375,6 +406,7 @@ static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStrea
 // double-float operator (spread); the float32 ones share tb32, the others tb64.
 enum TileUse { kTileRef32 = 0, kTileGrad32 = 1, kTileF64 = 2, kTileDF = 3 };
 struct TuneKey {
+    int dev;
     int N[3];
     int P;
     int use;
@@ -435,6 +467,7 @@ static int time_tiles(mps_system *s, int use, int tz, int nrhs, const double *m,
 static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     TuneKey key;
     memset(&key, 0, sizeof(key));
+    key.dev = current_device();
     for (int k = 0; k < 3; ++k) key.N[k] = s->gp.N[k];
     key.P = s->gp.P;
     key.use = use;
@@ -611,14 +644,18 @@ static int df_prepare(mps_system *s, cudaStream_t st, bool *use_tiles_out) {
     bool use_tiles = false;
     MPS_TRY(ensure_tiles(s, kTileDF, st, &use_tiles));
     MPS_TRY(ensure_grids(s, MPS_FP64, st));
-    {
+    if (!s->tm6_ready) {
         std::lock_guard<std::mutex> lk(g_green_mu);
         if (!s->green->tm6) {
             float2 *tm = nullptr;
             MPS_TRY(dalloc_persistent(&tm, sizeof(float2) * 6 * s->Gc));
             MPS_TRY(df_scale_table(s->gp, s->green->h64, tm, st));
+            MPS_TRY(green_mark_filled(&s->green->ev_tm6, st));
             s->green->tm6 = tm;
+        } else {
+            MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->green->ev_tm6, 0));   // filled by another system
         }
+        s->tm6_ready = true;
     }
     *use_tiles_out = use_tiles;
     return MPS_OK;
@@ -814,14 +851,18 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     MPS_TRY(ensure_tiles(s, kTileGrad32, st, &use_tiles));
     if (!use_tiles) return matvec_impl<float>(s, m, out, nrhs, st);
     MPS_TRY(ensure_grids(s, MPS_FP32, st));
-    {
+    if (!s->hs32_ready) {
         std::lock_guard<std::mutex> lk(g_green_mu);
         if (!s->green->hs32) {
             float *hs = nullptr;
             MPS_TRY(dalloc_persistent(&hs, sizeof(float) * s->Gc));
             MPS_TRY(grad_scale_coef(s->gp, s->green->h64, hs, st));
+            MPS_TRY(green_mark_filled(&s->green->ev_hs32, st));
             s->green->hs32 = hs;
+        } else {
+            MPS_CUDA_TRY(cudaStreamWaitEvent(st, s->green->ev_hs32, 0));   // filled by another system
         }
+        s->hs32_ready = true;
     }
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
@@ -1867,6 +1908,7 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     {
         GreenKey key;
         memset(&key, 0, sizeof(key));
+        key.dev = current_device();
         for (int k = 0; k < 3; ++k) {
             key.N[k] = s->gp.N[k];
             key.box[k] = d->box[k];
@@ -1877,11 +1919,13 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         auto it = g_green.find(key);
         if (it != g_green.end()) {
             s->green = it->second;
+            CR_TRY(cudaStreamWaitEvent(st, s->green->ev_h, 0) == cudaSuccess ? MPS_OK : MPS_CUDA_ERR);
         } else {
             auto gc = std::make_shared<GreenCoef>();
             CR_TRY(dalloc_persistent(&gc->h64, sizeof(double) * s->Gc));
             CR_TRY(dalloc_persistent(&gc->h32, sizeof(float) * s->Gc));
             CR_TRY(green_half(s->gp, gc->h64, gc->h32, st));
+            CR_TRY(green_mark_filled(&gc->ev_h, st));
             if (g_green.size() >= kGreenCacheMax) g_green.clear();  // systems keep their own reference
             g_green[key] = gc;
             s->green = gc;
@@ -2261,6 +2305,12 @@ extern "C" int mps_field_map_sizes(const double *x_e, int64_t n_e, const double 
     }
     cleanup();
     return rc_;
+}
+
+extern "C" int mps_kspace_cache_clear(void) {
+    std::lock_guard<std::mutex> lk(g_green_mu);
+    g_green.clear();   // systems that hold coefficients keep them until they are destroyed
+    return MPS_OK;
 }
 
 extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms) {
