@@ -99,9 +99,12 @@ def grid_for(box, xi, tol, fft_friendly=True):
 
 
 def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None,
-                        fft_friendly=True):
+                        fft_friendly=True, return_moments=False, solver_tol=None):
     """C (K, 3, 3) (row i = mean dipole for the unit field along i) of one
-    configuration for every contrast scaling, all 3K solves in one batch."""
+    configuration for every contrast scaling, all 3K solves in one batch.
+    ``tol`` sets the spectral parameters (cutoff, grid, support) and, unless
+    ``solver_tol`` is given, the GMRES tolerance too.  Returns (C, converged), or
+    (C, converged, moments (3K, N, 3) on the device) with ``return_moments``."""
     import torch
 
     from .sizes import PolydisperseSystem, spectral_parameters
@@ -130,13 +133,14 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
         b = eye[None, :, None, :].expand(K, 3, n, 3).reshape(3 * K, n, 3).contiguous()
         x0 = (amp[:, None, :, None] * eye[None, :, None, :]).reshape(3 * K, n, 3).contiguous()
         diag_index = [k for k in range(K) for _ in range(3)]
-        sol, info = sysm.solve(b, x0, tol=tol, restart=min(3 * n, 30), maxit=100 if precision != "mixed" else 8,
+        sol, info = sysm.solve(b, x0, tol=tol if solver_tol is None else solver_tol, restart=min(3 * n, 30),
+                               maxit=100 if precision != "mixed" else 8,
                                precision=precision, diag_index=diag_index)
         C = sol.reshape(K, 3, n, 3).mean(dim=2).cpu().numpy()
         conv = all(i.converged for i in info)
     finally:
         sysm.close()
-    return C, conv
+    return (C, conv, sol) if return_moments else (C, conv)
 
 
 def _solve_concurrently(todo: List[Configuration], solve: Callable, workers: int) -> dict:

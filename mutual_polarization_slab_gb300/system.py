@@ -27,6 +27,14 @@ def as_device(a, dtype=torch.float64) -> torch.Tensor:
     return torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dtype, device="cuda")
 
 
+def clear_kspace_cache():
+    """Drop the process's cached Green's coefficients and scale tensors (shared by
+    systems built on the same device, grid, box, xi and eta), so the next system
+    recomputes its k-space data as the reference does on every ``capacitance()``
+    call (``CPU - Ewald test/capacitance.py:385``).  Existing systems keep theirs."""
+    L.check(L.lib().mps_kspace_cache_clear())
+
+
 @dataclass
 class SolveInfo:
     converged: bool

@@ -137,3 +137,18 @@ def test_c1_tensor(golden_c1):
     assert np.linalg.norm(S - g["S"].real) / np.linalg.norm(g["S"].real) < 1e-7
     # the tensor is symmetric
     assert np.abs(C - C.T).max() < 1e-8 * np.abs(C).max()
+
+
+def test_threaded_real_operator_matches_single_thread():
+    """Geometry.field_real_many (threads over grid components and particle chunks,
+    scipy FFTs with workers) is the same operator as field_real, to rounding."""
+    from mutual_polarization_slab_gb300.workloads import rsa
+    x, box, _ = rsa(2500, 0.3, seed=12)
+    xi, rc = 0.7, 5.5
+    perp, para, rv = ew.default_table(xi)
+    g = ew.Geometry(x, np.full(x.shape[0], 9.0), box, xi, rc, [40, 40, 40], 8, perp, para, rv, 0.7)
+    M = np.random.default_rng(3).standard_normal((3, x.shape[0], 3))
+    ref = np.stack([g.field_real(M[i]) for i in range(3)])
+    for threads in (1, 5):
+        got = g.field_real_many(M, threads=threads)
+        assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
