@@ -874,7 +874,18 @@ __global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ 
                 const dfv d = s2 * y;
                 const dfv rh[3] = {r[0] * y, r[1] * y, r[2] * y};
                 dfv A(0.f, 0.f), B(0.f, 0.f);
-                const int64_t i = df_search(tab.rvf, tab.ntab, d.hi, tab.inv_dr);
+                int64_t i = df_search(tab.rvf, tab.ntab, d.hi, tab.inv_dr);
+                // The float search can land one segment off when d lies within a float rounding of a node;
+                // settle the bracket r_{i-1} < d <= r_i (the reference's searchsorted 'left') in double-float,
+                // so the coupling is interpolated inside its segment instead of extrapolated across the node.
+                if (i > 1 && i < tab.ntab) {
+                    const dfv lo = d - df_lo(tab.seg_r[i]);
+                    if (lo.hi < 0.f || (lo.hi == 0.f && lo.lo <= 0.f)) --i;
+                }
+                if (i > 0 && i + 1 < tab.ntab) {
+                    const dfv hi = d - df_lo(tab.seg_r[i + 1]);
+                    if (hi.hi > 0.f || (hi.hi == 0.f && hi.lo > 0.f)) ++i;
+                }
                 if (i <= 0 || i >= tab.ntab) {
                     atomicExch(err, 1);
                 } else {

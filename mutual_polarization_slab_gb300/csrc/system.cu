@@ -465,6 +465,14 @@ static int time_tiles(mps_system *s, int use, int tz, int nrhs, const double *m,
 }
 
 static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
+    // MPS_TILE_DEPTH=4 or 8 fixes the depth instead of timing (A/B comparisons and tests); not cached
+    if (const char *fd = getenv("MPS_TILE_DEPTH")) {
+        const int d = atoi(fd);
+        if ((d == 4 || d == 8) && tiles_supported(s->gp, d)) {
+            *tz = d;
+            return MPS_OK;
+        }
+    }
     TuneKey key;
     memset(&key, 0, sizeof(key));
     key.dev = current_device();
