@@ -56,67 +56,96 @@ def dilute_guess(eps_p, phi, Hhat):
 
 
 def gmres_restarted(matvec: Callable, b, x0, tol: float, restart: int, maxit: int, verbose: int = 0):
-    """Restarted GMRES for a user matvec on device vectors (capacitance.py:60-199).
+    """Restarted GMRES for a caller's matvec (the reference's ``gmres_restarted``,
+    ``CPU - Ewald test/capacitance.py:60-199``): same arguments, same return value
+    ``(x, flag, relres)`` (flag 0 when ``||b - A x|| / ||b|| <= tol``).
 
-    Same controls and return value ``(x, flag, relres)``; modified Gram-Schmidt,
-    Givens rotations, all in float64/complex128 on the GPU."""
-    bt = as_device(b, torch.complex128).reshape(-1)
-    x = as_device(x0, torch.complex128).reshape(-1).clone()
-    nb = torch.linalg.vector_norm(bt).item()
-    asnp = not isinstance(b, torch.Tensor)
-    if nb == 0.0:
-        return (x.cpu().numpy() if asnp else x), 0, 0.0
+    Each cycle builds a Krylov basis on the GPU (modified Gram-Schmidt, complex
+    Givens rotations for the small least-squares problem) and ends with the
+    cycle's best iterate: the least-squares solution over the columns up to the
+    last strict drop of the residual estimate; when no column improved on the
+    cycle's start, over all of them.  numpy in, numpy out; CUDA tensors stay on
+    the device."""
+    on_host = not isinstance(b, torch.Tensor)
+    rhs = as_device(b, torch.complex128).reshape(-1)
+    sol = as_device(x0, torch.complex128).reshape(-1).clone()
+    bnorm = torch.linalg.vector_norm(rhs).item()
 
-    def mv(v):
-        out = matvec(v.cpu().numpy() if asnp else v)
-        return as_device(out, torch.complex128).reshape(-1)
+    def result(flag, rr):
+        return (sol.cpu().numpy() if on_host else sol), flag, rr
 
-    t0 = time.perf_counter()
-    relres = math.inf
-    for outer in range(int(maxit)):
-        r = bt - mv(x)
-        beta = torch.linalg.vector_norm(r).item()
-        relres = beta / nb
+    if bnorm == 0.0:
+        return result(0, 0.0)
+
+    def apply(v):
+        return as_device(matvec(v.cpu().numpy() if on_host else v), torch.complex128).reshape(-1)
+
+    started = time.perf_counter()
+    n_apply = 0
+    for cycle in range(int(maxit)):
+        resid = rhs - apply(sol)
+        n_apply += 1
+        rnorm = torch.linalg.vector_norm(resid).item()
         if verbose >= 2:
-            print(f"    GMRES outer {outer + 1}/{maxit}: relres={relres:.3e}", flush=True)
-        if relres <= tol:
-            return (x.cpu().numpy() if asnp else x), 0, relres
-        V = torch.zeros((restart + 1, bt.numel()), dtype=torch.complex128, device="cuda")
-        H = np.zeros((restart + 1, restart), dtype=np.complex128)
-        V[0] = r / beta
-        g = np.zeros(restart + 1, dtype=np.complex128)
-        g[0] = beta
-        cs = np.zeros(restart, dtype=np.complex128)
-        sn = np.zeros(restart, dtype=np.complex128)
-        k = 0
-        for j in range(restart):
-            w = mv(V[j])
-            for i in range(j + 1):
-                H[i, j] = torch.vdot(V[i], w).item()
-                w = w - H[i, j] * V[i]
-            H[j + 1, j] = torch.linalg.vector_norm(w).item()
-            if H[j + 1, j] != 0:
-                V[j + 1] = w / H[j + 1, j]
-            for i in range(j):
-                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
-                H[i + 1, j] = -np.conj(sn[i]) * H[i, j] + cs[i] * H[i + 1, j]
-                H[i, j] = t
-            den = math.hypot(abs(H[j, j]), abs(H[j + 1, j]))
-            cs[j], sn[j] = (1.0, 0.0) if den == 0 else (H[j, j] / den, H[j + 1, j] / den)
-            H[j, j] = cs[j] * H[j, j] + sn[j] * H[j + 1, j]
-            H[j + 1, j] = 0
-            g[j + 1] = -np.conj(sn[j]) * g[j]
-            g[j] = cs[j] * g[j]
-            k = j + 1
-            if abs(g[j + 1]) / nb <= tol:
+            print(f"    [gmres] cycle {cycle + 1} of {maxit}: relative residual {rnorm / bnorm:.3e}", flush=True)
+        if rnorm / bnorm <= tol:
+            if verbose >= 1:
+                print(f"    [gmres] converged: relative residual {rnorm / bnorm:.3e}, {cycle + 1} cycles, "
+                      f"{n_apply} matvecs, {time.perf_counter() - started:.2f} s", flush=True)
+            return result(0, rnorm / bnorm)
+        basis = [resid / rnorm]
+        hess = np.zeros((restart + 1, restart), dtype=np.complex128)   # rotated in place: upper triangle
+        rot = []                                                          # (c, s) of each Givens rotation
+        proj = np.zeros(restart + 1, dtype=np.complex128)                 # rotated projection of the residual
+        proj[0] = rnorm
+        best_est, best_cols, done_cols, hit = rnorm / bnorm, 0, 0, False
+        for col in range(restart):
+            w = apply(basis[col])
+            n_apply += 1
+            for i, v in enumerate(basis):                                 # modified Gram-Schmidt
+                hess[i, col] = torch.vdot(v, w).item()
+                w = w - hess[i, col] * v
+            wn = torch.linalg.vector_norm(w).item()
+            hess[col + 1, col] = wn
+            basis.append(w / wn if wn != 0.0 else torch.zeros_like(w))
+            for i, (c, sg) in enumerate(rot):                             # earlier rotations on the new column
+                top, bot = hess[i, col], hess[i + 1, col]
+                hess[i, col] = c * top + sg * bot
+                hess[i + 1, col] = -np.conj(sg) * top + c * bot
+            # complex Givens rotation with a real cosine, c = |top| / rho, s = (top / |top|) conj(bot) / rho: unitary
+            # for complex entries too (for real data it agrees with the reference's c = top / rho up to a common
+            # sign, which leaves the least-squares solution unchanged)
+            top, bot = hess[col, col], hess[col + 1, col]
+            scale = math.hypot(abs(top), abs(bot))
+            if scale == 0.0:
+                c, sg = 1.0, 0.0
+            elif top == 0:
+                c, sg = 0.0, np.conj(bot) / abs(bot)
+            else:
+                c, sg = abs(top) / scale, (top / abs(top)) * np.conj(bot) / scale
+            rot.append((c, sg))
+            hess[col, col] = c * top + sg * bot
+            hess[col + 1, col] = 0.0
+            proj[col], proj[col + 1] = c * proj[col], -np.conj(sg) * proj[col]
+            done_cols = col + 1
+            est = abs(proj[col + 1]) / bnorm
+            if verbose >= 3:
+                print(f"      [gmres] step {col + 1}: estimated residual {est:.3e}", flush=True)
+            if est < best_est:
+                best_est, best_cols = est, col + 1
+            if est <= tol:
+                hit = True
                 break
-        y = np.linalg.solve(np.triu(H[:k, :k]), g[:k])
-        x = x + (torch.as_tensor(y, device="cuda")[:, None] * V[:k]).sum(dim=0)
-    r = bt - mv(x)
-    relres = torch.linalg.vector_norm(r).item() / nb
+        k = done_cols if hit else (best_cols or done_cols)
+        coef = np.linalg.lstsq(hess[:k, :k], proj[:k], rcond=None)[0]
+        sol = sol + (torch.as_tensor(coef, device=sol.device)[:, None] * torch.stack(basis[:k])).sum(dim=0)
+    resid = rhs - apply(sol)
+    n_apply += 1
+    rr = torch.linalg.vector_norm(resid).item() / bnorm
     if verbose >= 1:
-        print(f"    GMRES NOT converged: relres={relres:.3e} time={time.perf_counter() - t0:.2f}s", flush=True)
-    return (x.cpu().numpy() if asnp else x), 1, relres
+        print(f"    [gmres] not converged: relative residual {rr:.3e} after {maxit} cycles, {n_apply} matvecs, "
+              f"{time.perf_counter() - started:.2f} s", flush=True)
+    return result(1, rr)
 
 
 def _np_or_t(t, asnp):
@@ -132,7 +161,11 @@ def magnetic_dipole(x, lambdap, H, box, p1, p2, Ngrid, h, P, xi, eta, rc, mold, 
     ``restart`` / ``maxit`` default to the reference's ``min(3N, 10)`` /
     ``min(3N, 100)``; ``precision='mixed'`` runs float64 iterative refinement
     with float32-operator GMRES corrections (``maxit`` then counts refinement
-    steps).  Returns (N,3) complex128 (numpy in, numpy out)."""
+    steps).  ``use_scipy_gmres`` chooses, in the reference, between SciPy's
+    ``gmres`` and its own ``gmres_restarted``; both are restarted GMRES with the
+    same relative-residual stopping rule, and here both choices run the device
+    GMRES (``mps_gmres``), which keeps each cycle's best iterate like
+    ``gmres_restarted``.  Returns (N,3) complex128 (numpy in, numpy out)."""
     asnp = not isinstance(x, torch.Tensor)
     xd = as_device(x).reshape(-1, 3)
     N = xd.shape[0]

@@ -1120,7 +1120,8 @@ struct GmresState {
     double *beta;   // [r]
     double *bnorm;  // [r]
     double *res;    // [r] residual estimate / true relres
-    int32_t *kcount;  // [r]
+    int32_t *kcount;  // [r] columns of the cycle's best iterate so far (strictly smallest residual estimate)
+    int32_t *kfull;   // [r] columns built in the cycle
     double *y;      // [r][restart]
 };
 
@@ -1134,6 +1135,7 @@ __global__ void k_cycle_start(GmresState st, int restart, int nrhs) {
     st.g[r * (restart + 1)] = b;
     st.res[r] = st.bnorm[r] > 0 ? b / st.bnorm[r] : 0.0;
     st.kcount[r] = 0;
+    st.kfull[r] = 0;
 }
 
 // Arnoldi column j: H[:,j] = h1 + h2, H[j+1,j] = ||w||, then Givens rotations.
@@ -1167,8 +1169,15 @@ __global__ void k_arnoldi_givens(GmresState st, int restart, int j, int nrhs, co
     const double gj = g[j];
     g[j] = cs[j] * gj;
     g[j + 1] = -sn[j] * gj;
-    st.res[r] = st.bnorm[r] > 0 ? fabs(g[j + 1]) / st.bnorm[r] : 0.0;
-    st.kcount[r] = j + 1;
+    // the cycle keeps its best iterate: the least-squares solution over the first k columns, k where the
+    // residual estimate last decreased strictly (EW/capacitance.py:174-191); the estimate never rises in exact
+    // arithmetic, so k = j + 1 unless it stagnates
+    const double est = st.bnorm[r] > 0 ? fabs(g[j + 1]) / st.bnorm[r] : 0.0;
+    st.kfull[r] = j + 1;
+    if (est < st.res[r]) {
+        st.res[r] = est;
+        st.kcount[r] = j + 1;
+    }
 }
 
 // Coefficients u (length k+1) of the least-squares residual b - A x_k = V_{k+1} u:
@@ -1194,7 +1203,11 @@ __global__ void k_backsolve(GmresState st, int restart, int nrhs) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrhs) return;
     const int ld = restart + 1;
-    const int k = st.kcount[r];
+    int k = st.kcount[r];
+    if (k == 0) {   // no step improved on the cycle's start: the full cycle's least-squares solution, as the reference
+        k = st.kfull[r];
+        st.kcount[r] = k;
+    }
     const double *H = st.H + (int64_t)r * ld * restart;
     const double *g = st.g + r * ld;
     double *y = st.y + r * restart;
@@ -1265,7 +1278,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     bytes += 256 + sizeof(double) * (size_t)nrhs * ld;                // g
     bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * kMaxCols);    // h1 h2
     bytes += 4 * (256 + sizeof(double) * (size_t)nrhs);               // nrm2 beta bnorm res
-    bytes += 2 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount frozen
+    bytes += 3 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount kfull frozen
     bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
     bytes += 256 + multidot_bytes(n3, nrhs);                          // partial + tickets
     bytes += 256 + sizeof(double) * (size_t)nrhs * (kMaxCols + 1);    // u
@@ -1286,6 +1299,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     S.bnorm = (double *)carve_ws(p, sizeof(double) * nrhs);
     S.res = (double *)carve_ws(p, sizeof(double) * nrhs);
     S.kcount = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    S.kfull = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
     int32_t *frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
     S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
     double *partial = (double *)carve_ws(p, multidot_bytes(n3, nrhs));

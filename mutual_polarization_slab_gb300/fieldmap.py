@@ -84,20 +84,22 @@ def _pairs_real(xe, xp, p, box, rc, perp, para, rv, p1, p2):
     return out
 
 
-def field_map(x_E, x_p, p, box, xi, *pairs):
+def field_map(x_E, x_p, p, box, xi, *pairs, errortol=ERRORTOL):
     """Field at the probe points (``FieldMap.m:1-59``).
 
     x_E (N_E, 3) probe positions, x_p (N_p, 3) particle positions, p (N_p, 3)
     dipoles, box (3,), xi.  ``pairs`` may hold (p1, p2), a probe/particle
     neighbour list with 1-based indices (p1 into x_E, p2 into x_p) as FieldMap's
     varargin; without it the neighbours within rc are found on the device.
-    Raises ``ValueError`` when rc exceeds half the box (FieldMap.m:36-39)."""
+    ``errortol`` (keyword only, not in the reference) replaces FieldMap's fixed
+    spectral tolerance 1e-3.  Raises ``ValueError`` when rc exceeds half the box
+    (FieldMap.m:36-39)."""
     asnp = _is_np(x_E, x_p, p)
     xe = as_device(x_E).reshape(-1, 3).contiguous()
     xp = as_device(x_p).reshape(-1, 3).contiguous()
     pd = as_device(p).reshape(-1, 3).contiguous()
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    rc, Ngrid, h, P, eta = field_parameters(box, xi)
+    rc, Ngrid, h, P, eta = field_parameters(box, xi, errortol)
     if np.any(rc > box / 2):
         raise ValueError("Real space cutoff (rc = %.3f) larger than half the box size (%.3f, %.3f, %.3f). "
                          "Accuracy to specified error tolerance not guaranteed." % (rc, *box))
@@ -133,19 +135,20 @@ def quad_tables_probe(r, xi):
     return torch.cat((dip[2].reshape(1, -1), dip[3].reshape(1, -1), quad), dim=0).contiguous()
 
 
-def field_map_quadrupole(x_E, x_p, p, Q, box, xi, return_gradient=False):
+def field_map_quadrupole(x_E, x_p, p, Q, box, xi, return_gradient=False, *, errortol=ERRORTOL):
     """Field at probe points from dipoles ``p`` (N_p, 3) and quadrupoles ``Q``
     (N_p, 5: xx xy xz yy yz) at ``x_p`` (``Compute_Field_Quadrupole/FieldMap.m:1-58``):
     E (N_E, 3) with FieldMap's sign; with ``return_gradient`` also the field
     gradient G (N_E, 5) its MatrixVectorMultiply computes.  Separation table
     r = 0, 1e-4 .. 10 (FieldMap.m:22); the reference's r = 0 row divides by zero,
-    here it holds the solver's r = 0 values (only separations below 1e-4 use it)."""
+    here it holds the solver's r = 0 values (only separations below 1e-4 use it).
+    ``errortol`` (keyword only) replaces the fixed spectral tolerance 1e-3."""
     asnp = _is_np(x_E, x_p, p, Q)
     xe = as_device(x_E).reshape(-1, 3).contiguous()
     xp = as_device(x_p).reshape(-1, 3).contiguous()
     sq = torch.cat((as_device(p).reshape(-1, 3), as_device(Q).reshape(-1, 5)), dim=1).contiguous()
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    rc, Ngrid, h, P, eta = field_parameters(box, xi)
+    rc, Ngrid, h, P, eta = field_parameters(box, xi, errortol)
     if np.any(rc > box / 2):
         raise ValueError("Real space cutoff (rc = %.3f) larger than half the box size (%.3f, %.3f, %.3f). "
                          "Accuracy to specified error tolerance not guaranteed." % (rc, *box))
@@ -171,12 +174,13 @@ def _colon(a, step, b):
     return a + step * np.arange(k + 1, dtype=np.float64)
 
 
-def field_map_sizes(x_E, x_p, a, p, box, xi):
+def field_map_sizes(x_E, x_p, a, p, box, xi, *, errortol=ERRORTOL):
     """Field at probe points from dipoles ``p`` of spheres of radii ``a``
     (``Compute_Field_Sizes/FieldMap.m:1-43``, ``ComputeField.m``, ``RealSpace.m``):
     probes count as spheres of the smallest radius; the real-space table runs over
     r = 0.5 : 1e-3 : rc + 1e-2 (FieldMap.m:31), so a probe closer than 0.5 to a
-    sphere centre raises ``ValueError`` as the reference's table lookup fails."""
+    sphere centre raises ``ValueError`` as the reference's table lookup fails.
+    ``errortol`` (keyword only) replaces the fixed tolerance 1e-3 (also the table step)."""
     from . import sizes as S
 
     asnp = _is_np(x_E, x_p, p)
@@ -185,7 +189,7 @@ def field_map_sizes(x_E, x_p, a, p, box, xi):
     pd = as_device(p).reshape(-1, 3).contiguous()
     a_np = np.asarray(a.cpu() if isinstance(a, torch.Tensor) else a, dtype=np.float64).reshape(-1)
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    tol = ERRORTOL
+    tol = float(errortol)
     lt = math.sqrt(-math.log(tol))
     rc = lt / xi
     if np.any(rc > box / 2):

@@ -78,10 +78,11 @@ def real_part_pairs(x_E, x_p, p, box, rc, perp, para, rvals, pairs=None):
     return out
 
 
-def field_map(x_E, x_p, p, box, xi):
-    """E = -(Hk + Hr) at the probes (FieldMap.m:1-59); complex (the reference's pipeline)."""
+def field_map(x_E, x_p, p, box, xi, errortol=ERRORTOL):
+    """E = -(Hk + Hr) at the probes (FieldMap.m:1-59); complex (the reference's pipeline).
+    errortol: FieldMap's fixed 1e-3 unless given."""
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    rc, Ngrid, h, P, eta = field_parameters(box, xi)
+    rc, Ngrid, h, P, eta = field_parameters(box, xi, errortol)
     if np.any(rc > box / 2):
         raise ValueError("Real space cutoff larger than half the box size")
     r_table = np.arange(1, 10001, dtype=np.float64) * 1e-3
@@ -117,14 +118,14 @@ def quad_tables_probe(r, xi):
     return out
 
 
-def field_map_quadrupole(x_E, x_p, S, Q, box, xi):
+def field_map_quadrupole(x_E, x_p, S, Q, box, xi, errortol=ERRORTOL):
     """E (N_E, 3) and G (N_E, 5) at the probes with FieldMap's sign, complex (the
     reference's pipeline)."""
     from . import quadrupole_oracle as qo
     x_E = np.asarray(x_E, dtype=np.float64)
     x_p = np.asarray(x_p, dtype=np.float64)
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    rc, Ngrid, h, P, eta = field_parameters(box, xi)
+    rc, Ngrid, h, P, eta = field_parameters(box, xi, errortol)
     if np.any(rc > box / 2):
         raise ValueError("Real space cutoff larger than half the box size")
     r_table = np.arange(1, 100001, dtype=np.float64) * 1e-4
@@ -161,7 +162,7 @@ def field_map_quadrupole(x_E, x_p, S, Q, box, xi):
 # ---------------------------------------------------------------------------
 # Polydisperse field map (Compute_Field_Sizes/FieldMap.m:1-43, ComputeField.m:1-40, RealSpace.m:1-77)
 # ---------------------------------------------------------------------------
-def field_map_sizes(x_E, x_p, a, p, box, xi):
+def field_map_sizes(x_E, x_p, a, p, box, xi, errortol=ERRORTOL):
     """E (N_E, 3) with FieldMap's sign; probes are spheres of the smallest radius."""
     from . import polydisperse_oracle as po
     x_E = np.asarray(x_E, dtype=np.float64)
@@ -169,7 +170,7 @@ def field_map_sizes(x_E, x_p, a, p, box, xi):
     p = np.asarray(p, dtype=np.float64)
     a = np.asarray(a, dtype=np.float64).reshape(-1)
     box = np.asarray(box, dtype=np.float64).reshape(3)
-    tol = ERRORTOL
+    tol = float(errortol)
     rc, Ngrid, h, P, eta = po.spectral_parameters(box, xi, tol)
     if np.any(rc > box / 2):
         raise ValueError("Real space cutoff larger than half the box size")

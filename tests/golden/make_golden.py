@@ -170,12 +170,42 @@ def case_forces(ew, cap):
     return out
 
 
+def case_gmres(ew, cap):
+    """The reference's own restarted GMRES (capacitance.gmres_restarted) on small
+    dense problems: a converging solve, one stopped by maxit (the best-iterate
+    update of each cycle decides x), and a stagnating one (a cyclic shift: no
+    column improves on the cycle's start)."""
+    rng = np.random.default_rng(23)
+    n = 60
+    # real data, as the reference's solver receives it (its complex Givens rotation, c = a / rho with complex
+    # a, is not unitary, so genuinely complex systems are outside what it solves)
+    A = 4.0 * np.eye(n) + 0.35 * rng.normal(size=(n, n))
+    b = rng.normal(size=n)
+    x0 = np.zeros(n, dtype=np.complex128)
+    out = dict(A=A, b=b, x0=x0)
+    for tag, (tol, restart, maxit) in {"conv": (1e-10, 10, 50), "stop": (1e-14, 5, 2)}.items():
+        x, flag, relres = cap.gmres_restarted(lambda v: A @ v, b, x0, tol, restart, maxit)
+        out[f"x_{tag}"], out[f"flag_{tag}"], out[f"relres_{tag}"] = x, flag, relres
+        out[f"ctl_{tag}"] = np.array([tol, restart, maxit])
+    m = 12
+    S = np.roll(np.eye(m), 1, axis=0)      # S e_i = e_{i+1}
+    bs = np.zeros(m, dtype=np.complex128)
+    bs[0] = 1.0
+    x, flag, relres = cap.gmres_restarted(lambda v: S @ v, bs, np.zeros(m, dtype=np.complex128), 1e-8, 5, 3)
+    out.update(S=S, bs=bs, x_stag=x, flag_stag=flag, relres_stag=relres)
+    return out
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MPS_REFERENCE_ROOT")
     if not ref_root:
-        raise SystemExit("usage: make_golden.py <reference root>")
+        raise SystemExit("usage: make_golden.py <reference root> [case ...]")
     ew, cap = _import_reference(ref_root)
-    for name, fn in (("small", case_small), ("c1", case_c1), ("forces", case_forces)):
+    cases = (("small", case_small), ("c1", case_c1), ("forces", case_forces), ("gmres", case_gmres))
+    wanted = set(sys.argv[2:])
+    for name, fn in cases:
+        if wanted and name not in wanted:
+            continue
         t0 = time.perf_counter()
         d = fn(ew, cap)
         np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **d)

@@ -303,3 +303,42 @@ def test_contrast_batch_diag_index(golden_small):
                           para, rv, 1.0)
         res = geo.field_real(xb[k]) - b[k]
         assert np.abs(res).max() < 1e-9
+
+
+def test_gmres_restarted_matches_the_reference_solver():
+    """The drop-in gmres_restarted against the reference's own gmres_restarted
+    (tests/golden/golden_gmres.npz, recorded by make_golden.py): a converging
+    solve, one stopped by maxit, whose x is each cycle's best iterate, and a
+    stagnating cyclic shift (no column improves on a cycle's start)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_gmres.npz"))
+    A = g["A"]
+    for tag in ("conv", "stop"):
+        tol, restart, maxit = g[f"ctl_{tag}"]
+        x, flag, relres = gcap.gmres_restarted(lambda v: A @ v, g["b"], g["x0"], float(tol), int(restart),
+                                               int(maxit))
+        assert flag == int(g[f"flag_{tag}"])
+        ref = g[f"x_{tag}"]
+        assert np.abs(x - ref).max() <= 1e-9 * np.abs(ref).max(), tag
+        if tag == "stop":
+            assert abs(relres - float(g["relres_stop"])) <= 1e-8 * float(g["relres_stop"])
+        else:
+            assert relres <= float(tol)
+    S = g["S"]
+    x, flag, relres = gcap.gmres_restarted(lambda v: S @ v, g["bs"], np.zeros(S.shape[0], dtype=complex), 1e-8, 5, 3)
+    assert flag == int(g["flag_stag"]) == 1
+    np.testing.assert_allclose(x, g["x_stag"], atol=1e-14)
+    assert abs(relres - float(g["relres_stag"])) <= 1e-12
+
+
+def test_gmres_restarted_solves_complex_systems():
+    """Complex (non-real) systems converge to the direct solution: the drop-in's
+    Givens rotation is unitary for complex entries."""
+    rng = np.random.default_rng(29)
+    n = 50
+    A = 4.0 * np.eye(n) + 0.3 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x, flag, relres = gcap.gmres_restarted(lambda v: A @ v, b, np.zeros(n, dtype=complex), 1e-12, 10, 50)
+    assert flag == 0 and relres <= 1e-12
+    ref = np.linalg.solve(A, b)
+    assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max()
