@@ -172,15 +172,15 @@ def run_gpu(args):
     lib = _lib.lib()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def make_system(prof=False):
+    def make_system(prof=False, inner=None):
         s = SpectralEwaldSystem(xd, epsd, w["box"], w["xi"], w["rc"], w["Ngrid"], w["P"], perp, para, rv,
-                                slab_factor=0.0, max_rhs=3)
+                                slab_factor=0.0, max_rhs=3, inner=inner)
         if prof:
             s.profile(True)
         return s
 
     def step_mixed(prof=False):
-        s = make_system(prof)
+        s = make_system(prof, inner=args.inner_grid if args.inner == "grad" else None)
         sol, info = s.solve(b, x0, tol=tol, restart=restart, maxit=args.maxref, precision="mixed",
                             inner_tol=args.inner_tol, inner_maxit=args.inner_maxit,
                             residual_precision=args.resid, inner_operator=args.inner)
@@ -245,7 +245,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    s_setup = make_system()
+    s_setup = make_system(inner=args.inner_grid if args.inner == "grad" else None)
     # first matvec of a system bins the particles into tiles (the inner operator of the solve)
     s_setup.matvec(b[:1], precision="fp32grad" if args.inner == "grad" else "fp32")
     e1.record()
@@ -259,8 +259,9 @@ def run_gpu(args):
     torch.cuda.synchronize()
     st = s_prof.stage_times()
     tuning = s_prof.tuning()
+    inner_disc = s_prof.inner
     s_prof.close()
-    roof = roofline(w, st, args.inner)
+    roof = roofline(w, st, args.inner, inner_disc)
 
     # --- plain float64 GMRES drop-in (reference solver structure) + accuracy of the mixed result
     ms_fp64, _, (sol_64, info_64) = timed(step_fp64_plain, max(1, min(args.steps, 2)), 1)
@@ -302,6 +303,10 @@ def run_gpu(args):
         "speedup_vs_fp64_plain": ms_fp64 / ms_mixed,
         "setup_ms_incl_first_fp32_matvec": setup_ms,
         "autotuned_tiles": tuning,
+        "inner_discretisation": ({"grid": [int(v) for v in inner_disc[0]], "P": int(inner_disc[1]),
+                                  "what": "grid and support of the float32 gradient-form inner operator; the "
+                                          "refinement residuals use the workload's own grid and P"}
+                                 if inner_disc is not None else None),
     }
     if not args.no_extra:
         out["quadrupole"] = workload_quadrupole(args)
@@ -329,16 +334,20 @@ def measured_traffic(kernel, n, ngrid):
     return None
 
 
-def roofline(w, st, inner="grad"):
+def roofline(w, st, inner="grad", inner_disc=None):
     """Dominant kernel (largest stage time of this library's kernels in the fp32 matvec) vs HBM peak.
     Algorithmic bytes per launch, R = 3 vectors, s = 4 bytes: the grids written or read once
     (3R grids for the reference discretisation, R for the gradient form), plus per particle its
     moments / fields (24 R), stencil start (12) and separable factors (3P s; twice for the gradient
-    form, which also reads dw/dr)."""
+    form, which also reads dw/dr).  ``inner_disc`` = (grid, P) of the float32 operator when it runs on
+    its own (coarser) grid."""
     n, P = w["n"], w["P"]
-    G = int(np.prod(w["Ngrid"]))
-    nx = int(w["Ngrid"][0])
-    Gc = (nx // 2 + 1) * int(w["Ngrid"][1]) * int(w["Ngrid"][2])
+    ngrid = w["Ngrid"]
+    if inner_disc is not None:
+        ngrid, P = inner_disc
+    G = int(np.prod(ngrid))
+    nx = int(ngrid[0])
+    Gc = (nx // 2 + 1) * int(ngrid[1]) * int(ngrid[2])
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -368,8 +377,9 @@ def roofline(w, st, inner="grad"):
     kname = {"spread": "k_spread_grad_tiled" if inner == "grad" else "k_spread_tiled",
              "contract": "k_contract_grad_warp" if inner == "grad" else "k_contract_tiled + gather",
              "scale": "k_scale_cs" if inner == "grad" else "k_scale_half"}.get(top, top)
-    traffic = measured_traffic(kname, n, w["Ngrid"])
-    return {"bound": "hbm", "kernel": f"{kname} (fp32, 3 vectors)", "achieved": achieved, "peak": peak,
+    traffic = measured_traffic(kname, n, ngrid)
+    return {"bound": "hbm", "kernel": f"{kname} (fp32, 3 vectors, {int(ngrid[0])}x{int(ngrid[1])}x{int(ngrid[2])} "
+                                      f"grid, P={P})", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
             "algorithmic_bytes_per_launch": algo[top], "avg_launch_ms": avg_ms, "launches": cnt,
             "traffic": traffic,
@@ -398,7 +408,7 @@ def run_e2e(args, w, world):
                                              Ngrid=w["Ngrid"], P=w["P"], restart=args.restart, maxit=args.maxref,
                                              precision="mixed", inner_tol=args.inner_tol,
                                              inner_maxit=args.inner_maxit, residual_precision=args.resid,
-                                             inner_operator=args.inner)
+                                             inner_operator=args.inner, inner_grid=args.inner_grid)
         return C, S
 
     for _ in range(max(1, args.warmup - 1)):
@@ -790,6 +800,9 @@ def main():
                     help="operator of the refinement residual: double-float FFTs (df) or cuFFT float64")
     ap.add_argument("--inner", default="grad", choices=["reference", "grad"],
                     help="inner float32 operator: the reference discretisation or its gradient form")
+    ap.add_argument("--inner-grid", dest="inner_grid", default="auto", type=lambda v: None if v == "same" else v,
+                    help="auto: the gradient-form inner operator on a coarser grid when one is cheaper; same: the "
+                         "system's grid")
     ap.add_argument("--inner-tol", dest="inner_tol", type=float, default=1e-4)
     ap.add_argument("--inner-maxit", dest="inner_maxit", type=int, default=3)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true", help="skip the CPU baseline leg")

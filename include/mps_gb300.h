@@ -252,6 +252,13 @@ typedef struct mps_system_desc {
      * is complex, stored as 6 float64 per particle (Re m_x, Re m_y, Re m_z, Im m_x, Im m_y, Im m_z),
      * and max_rhs counts complex vectors.  mps_matvec_complex and mps_adjoint_forces are not available. */
     const double *lambdap_imag;
+    /* Inner discretisation of the float32 gradient-form operator (MPS_FP32_GRAD, the mixed solve's inner      */
+    /* operator; kind MPS_DIPOLE): inner_P > 0 gives it its own grid inner_Ngrid and support inner_P (spectral */
+    /* splitting P (h xi)^2 / pi of that grid, the same xi and pair sum).  A coarser grid makes every inner    */
+    /* matvec cheaper; the refinement residuals still use the system's own grid, so the mixed solve converges  */
+    /* to the same solution.  inner_P = 0: the system's grid.  No counterpart in the reference.                */
+    int64_t inner_Ngrid[3];
+    int32_t inner_P;
 } mps_system_desc;
 
 enum mps_operator_kind { MPS_DIPOLE = 0, MPS_DIPOLE_QUADRUPOLE = 1, MPS_POLYDISPERSE = 2 };

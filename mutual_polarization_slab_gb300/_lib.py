@@ -46,6 +46,7 @@ class SystemDesc(C.Structure):
         ("Ngrid", i64 * 3), ("P", i32), ("eta", f64 * 3), ("perp", p), ("para", p), ("rvals", p),
         ("n_tab", i64), ("slab_factor", f64), ("max_rhs", i32), ("kind", i32), ("quad_tables", p),
         ("radius", p), ("radius_class", p), ("n_class", i32), ("sizes_tables", p), ("lambdap_imag", p),
+        ("inner_Ngrid", i64 * 3), ("inner_P", i32),
     ]
 
 

@@ -152,10 +152,16 @@ def _np_or_t(t, asnp):
     return t.cpu().numpy() if asnp else t
 
 
+def _inner(precision, inner_operator, inner_grid):
+    """The system's inner discretisation: ``inner_grid`` ("auto", None or (Ngrid, P)) matters only for the
+    mixed solve with the gradient-form inner operator."""
+    return inner_grid if precision == "mixed" and inner_operator == "grad" else None
+
+
 def magnetic_dipole(x, lambdap, H, box, p1, p2, Ngrid, h, P, xi, eta, rc, mold, offset, offsetxyz, Hperp, Hpara,
                     rvals, errortol, real_precomp=None, grid_precomp=None, k_precomp=None, slab_factor=1.0,
                     use_scipy_gmres=True, verbose=0, *, restart=None, maxit=None, precision="fp64",
-                    inner_tol=1e-4, inner_maxit=4, system=None, return_info=False):
+                    inner_tol=1e-4, inner_maxit=4, system=None, return_info=False, inner_grid="auto"):
     """Solve A m = tile(H, N) for the moments (capacitance.py:205-321) on the GPU.
 
     ``restart`` / ``maxit`` default to the reference's ``min(3N, 10)`` /
@@ -170,7 +176,8 @@ def magnetic_dipole(x, lambdap, H, box, p1, p2, Ngrid, h, P, xi, eta, rc, mold, 
     xd = as_device(x).reshape(-1, 3)
     N = xd.shape[0]
     sysm = system or SpectralEwaldSystem(xd, lambdap, box, xi, rc, Ngrid, P, Hperp, Hpara, rvals,
-                                         slab_factor=slab_factor, eta=eta, max_rhs=1)
+                                         slab_factor=slab_factor, eta=eta, max_rhs=1,
+                                         inner=_inner(precision, "grad", inner_grid))
     Hv = torch.as_tensor(np.real(np.asarray(H.cpu() if isinstance(H, torch.Tensor) else H)).astype(np.float64).reshape(3),
                          device="cuda")
     b = Hv.repeat(N, 1)
@@ -200,7 +207,7 @@ def _resolve_params(box, xi, errortol, rc, Ngrid, P):
 
 def capacitance(x, lambdap, box, Sguess, xi, errortol, dipoletable1, dipoletable2, rtable, offset, offsetxyz, Hhat,
                 slab_factor=1.0, use_scipy_gmres=True, verbose=0, *, rc=None, Ngrid=None, P=None, restart=None,
-                maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4):
+                maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4, inner_grid="auto"):
     """Induced dipoles and C = mean(S . Hhat) for one field direction (capacitance.py:327-418)."""
     asnp = not isinstance(x, torch.Tensor)
     box = np.asarray(box, dtype=np.float64).reshape(3)
@@ -209,7 +216,7 @@ def capacitance(x, lambdap, box, Sguess, xi, errortol, dipoletable1, dipoletable
         raise ValueError("Real-space cutoff exceeds half the box size; tolerance unmet.")
     t0 = time.perf_counter()
     sysm = SpectralEwaldSystem(x, lambdap, box, xi, rc, Ngrid, P, dipoletable1, dipoletable2, rtable,
-                               slab_factor=slab_factor, eta=eta, max_rhs=1)
+                               slab_factor=slab_factor, eta=eta, max_rhs=1, inner=_inner(precision, "grad", inner_grid))
     if verbose >= 1:
         print(f"Capacitance: N={sysm.n} rc={rc:.3f} Ngrid={tuple(Ngrid.tolist())} P={P} "
               f"Ncell={tuple(sysm.ncell.tolist())} pairs(kept)={sysm.n_pairs}", flush=True)
@@ -257,13 +264,17 @@ def run_capacitance(x, box, eps_p, xi, H0, errortol=1e-5, slab_factor=1.0, use_s
 def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None, dipoletable2=None, rtable=None,
                        offset=None, offsetxyz=None, *, slab_factor=0.0, rc=None, Ngrid=None, P=None, restart=None,
                        maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4, batched=True, system=None,
-                       residual_precision="df", inner_operator="grad"):
+                       residual_precision="df", inner_operator="grad", inner_grid="auto"):
     """3x3 capacitance tensor for unit fields along x, y, z (Capacitance_Hetero/Capacitance_Tensor.m:23-59).
 
     ``batched=True`` solves the three directions together (one batched matvec
     per iteration); each starts from ``Sguess`` rotated onto its field axis.
     ``batched=False`` follows the reference: sequential solves, each warm-started
     from the previous solution with columns permuted [z, x, y].
+    With ``precision='mixed'`` and the gradient-form inner operator,
+    ``inner_grid="auto"`` runs the inner solves on a coarser grid when one is
+    cheaper (``system.inner_grid``; None keeps the system's grid); the
+    refinement residuals keep the system's grid.
     Returns (C (3,3), S (N,3,3)) with row i of C the mean moment for field i.
     The MATLAB driver has no slab term, hence ``slab_factor=0`` by default."""
     asnp = not isinstance(x, torch.Tensor)
@@ -274,7 +285,8 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
     xd = as_device(x).reshape(-1, 3)
     N = xd.shape[0]
     sysm = system or SpectralEwaldSystem(xd, lambdap, box, xi, rc, Ngrid, P, dipoletable1, dipoletable2, rtable,
-                                         slab_factor=slab_factor, eta=eta, max_rhs=3)
+                                         slab_factor=slab_factor, eta=eta, max_rhs=3,
+                                         inner=_inner(precision, inner_operator, inner_grid))
     restart = min(3 * N, 10) if restart is None else int(restart)
     maxit = min(3 * N, 100) if maxit is None else int(maxit)
     g0 = as_device(np.real(Sguess) if not isinstance(Sguess, torch.Tensor) else Sguess.real).reshape(N, 3)
@@ -310,7 +322,8 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
 
 
 def capacitance_tensor_spectrum(x, box, eps_p, xi, errortol=1e-3, *, slab_factor=0.0, rc=None, Ngrid=None, P=None,
-                                restart=None, maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4):
+                                restart=None, maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4,
+                                inner_grid="auto"):
     """Tensor for every permittivity column of ``eps_p (N, N_k)`` and every frame of
     ``x (N,3[,F])`` (Capacitance_Hetero/CapacitanceTensorSpectrum.m:15-62).
     ``eps_p`` may be complex (frequency-dependent permittivities); C and p are then complex.
@@ -341,7 +354,8 @@ def capacitance_tensor_spectrum(x, box, eps_p, xi, errortol=1e-3, *, slab_factor
     for f in range(F):
         lam = eps.T.copy()                                   # (K, N) permittivity sets
         sysm = SpectralEwaldSystem(xn[:, :, f], lam, box, xi, rc, Ngrid, P, perp, para, rv,
-                                   slab_factor=slab_factor, eta=eta, max_rhs=3 * K)
+                                   slab_factor=slab_factor, eta=eta, max_rhs=3 * K,
+                                   inner=_inner(precision, "grad", inner_grid))
         b = torch.zeros((3 * K, N, 3), dtype=tdt, device="cuda")
         x0 = torch.zeros_like(b)
         diag_index = []

@@ -103,6 +103,24 @@ struct StageEvents {
     int precision;
 };
 
+// A coarser discretisation for the float32 gradient-form operator (the mixed solve's inner operator): its own
+// grid, support P and spectral splitting eta, the same xi and the same pair sum.  The inner solves only have to
+// reach 1e-4 .. 1e-3 of their right-hand sides, and every refinement residual uses the reference operator, so
+// the inner grid is chosen for speed: its distance from the reference operator (about 2e-4 relative at a
+// 3e-5 rule with P = 8) only costs the refinement a little more drift, bounded below.
+struct InnerGrid {
+    GridParams gp;
+    int64_t Gc = 0;
+    int32_t *start = nullptr;
+    double *w64 = nullptr;
+    float *w32 = nullptr, *g32 = nullptr;
+    TileBins tb;
+    float *grid = nullptr;   // max_rhs x G
+    void *spec = nullptr;    // max_rhs x Gc complex
+    std::shared_ptr<GreenCoef> green;
+    bool hs32_ready = false;
+};
+
 struct mps_system {
     cudaStream_t stream = nullptr;   // creation stream: stream-ordered allocations and frees
     int64_t n = 0;
@@ -191,6 +209,7 @@ struct mps_system {
     int inner_prec = MPS_FP32;   // operator of the mixed solve's inner GMRES
     // this system's stream has waited for the shared lazily built Green's buffers (hs32, tm6)
     bool hs32_ready = false, tm6_ready = false;
+    InnerGrid *inner = nullptr;      // coarser inner discretisation of the gradient-form operator, or null
 };
 
 static void free_system(mps_system *s) {
@@ -222,6 +241,13 @@ static void free_system(mps_system *s) {
     tile_bins_free(s->tb32, s->stream);
     if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
     if (s->partial32) cudaFreeAsync(s->partial32, s->stream);
+    if (InnerGrid *ig = s->inner) {
+        void *ip[] = {ig->start, ig->w64, ig->w32, ig->g32, ig->grid, ig->spec};
+        for (void *q : ip)
+            if (q) cudaFreeAsync(q, s->stream);
+        tile_bins_free(ig->tb, s->stream);
+        delete ig;
+    }
     delete s;
 }
 
@@ -316,9 +342,10 @@ static int ensure_work(mps_system *s, size_t need, cudaStream_t st) {
 }
 
 // Runs one cached plan on this system's work area and stream.
-static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *out, int dir, cudaStream_t st) {
+static int exec_plan_gp(mps_system *s, const GridParams &gp, cufftType type, int batch, void *in, void *out, int dir,
+                        cudaStream_t st) {
     CachedPlan cp;
-    MPS_TRY(get_plan(type, s->gp, batch, &cp));
+    MPS_TRY(get_plan(type, gp, batch, &cp));
     MPS_TRY(ensure_work(s, cp.work, st));
     std::lock_guard<std::mutex> lk(g_plan_mu);
     CUFFT_TRY(cufftSetWorkArea(cp.h, s->fft_work));
@@ -334,6 +361,10 @@ static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *o
         default: return MPS_BAD_ARG;
     }
     return MPS_OK;
+}
+
+static int exec_plan(mps_system *s, cufftType type, int batch, void *in, void *out, int dir, cudaStream_t st) {
+    return exec_plan_gp(s, s->gp, type, batch, in, out, dir, st);
 }
 
 static int ensure_grids(mps_system *s, int precision, cudaStream_t st) {
@@ -847,10 +878,13 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
 
 // Gradient form of the float32 operator (gradop.cu): one scalar grid per vector.
 
+static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st);
+
 static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     // the gradient form exists for the dipole operator only: the others run their own float32 operator
     if (s->kind == MPS_DIPOLE_QUADRUPOLE) return matvec_quad<float>(s, m, out, nrhs, st);
     if (s->kind == MPS_POLYDISPERSE) return matvec_cs<float>(s, m, out, nrhs, st);
+    if (s->inner) return matvec_grad_inner(s, m, out, nrhs, st);
     if (!s->g32 && s->w64) {
         MPS_TRY(dalloc(&s->g32, sizeof(float) * 3 * s->n * s->gp.P, st));
         MPS_TRY(grad_factors(s->x, s->n, s->gp, s->w64, s->g32, st));
@@ -900,6 +934,50 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
             MPS_TRY(contract_grad_warp(s->grid32, s->n, nrhs, s->order, s->start, s->w32, s->g32, s->gp, out, st));
         }
     }
+    STAGE_MARK(6);
+    if (beside)
+        MPS_TRY(pair_sum_join(s, out, nrhs, st));
+    else
+        MPS_TRY(real_space_f32(s, m, out, nrhs, st));
+    STAGE_MARK(7);
+    return MPS_OK;
+}
+
+// The gradient-form operator on the inner grid: the same stages as matvec_grad with the inner grid's geometry,
+// tiles, grids, Green's coefficient and FFT plans (its tiles, weights and factors are built with the system).
+static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
+    InnerGrid &ig = *s->inner;
+    if (!ig.grid) MPS_TRY(dalloc(&ig.grid, (size_t)s->max_rhs * ig.gp.G * sizeof(float), st));
+    if (!ig.spec) MPS_TRY(dalloc(&ig.spec, (size_t)s->max_rhs * ig.Gc * 2 * sizeof(float), st));
+    if (!ig.hs32_ready) {
+        std::lock_guard<std::mutex> lk(g_green_mu);
+        if (!ig.green->hs32) {
+            float *hs = nullptr;
+            MPS_TRY(dalloc_persistent(&hs, sizeof(float) * ig.Gc));
+            MPS_TRY(grad_scale_coef(ig.gp, ig.green->h64, hs, st));
+            MPS_TRY(green_mark_filled(&ig.green->ev_hs32, st));
+            ig.green->hs32 = hs;
+        } else {
+            MPS_CUDA_TRY(cudaStreamWaitEvent(st, ig.green->ev_hs32, 0));   // filled by another system
+        }
+        ig.hs32_ready = true;
+    }
+    const double vol = s->box[0] * s->box[1] * s->box[2];
+    StageEvents *ev = nullptr;
+    MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
+    const bool beside = pair_sum_beside(ev);
+    if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
+    STAGE_MARK(1);
+    MPS_TRY(spread_grad_tiled(m, s->n, nrhs, ig.start, ig.w32, ig.g32, ig.gp, ig.tb, ig.grid, st));
+    STAGE_MARK(2);
+    MPS_TRY(exec_plan_gp(s, ig.gp, CUFFT_R2C, nrhs, ig.grid, ig.spec, 0, st));
+    STAGE_MARK(3);
+    MPS_TRY(scale_cs<float>(ig.spec, nrhs, ig.gp, ig.green->hs32, st));
+    STAGE_MARK(4);
+    MPS_TRY(exec_plan_gp(s, ig.gp, CUFFT_C2R, nrhs, ig.spec, ig.grid, 0, st));
+    STAGE_MARK(5);
+    MPS_TRY(contract_grad_warp(ig.grid, s->n, nrhs, s->order, ig.start, ig.w32, ig.g32, ig.gp, out, st));
     STAGE_MARK(6);
     if (beside)
         MPS_TRY(pair_sum_join(s, out, nrhs, st));
@@ -1593,7 +1671,9 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
     // relative distance from the reference operator is measured at 5e-6..1.1e-4
     // for supports P = 10..8).  The drift adds up over the corrections since the
     // last true residual; when it could exceed the target, one true residual decides.
-    constexpr double kGradMismatch = 3e-4;
+    // the coarser inner grid (when the system has one) adds its discretisation's distance, about 2e-4 at the
+    // inner grids chosen here, to the gradient form's own: a bound twice as wide
+    const double kGradMismatch = s->inner ? 6e-4 : 3e-4;
     bool estimated = false;
     std::vector<double> drift(nrhs, 0.0);
     for (step = 1; e == MPS_OK; ++step) {
@@ -1694,6 +1774,37 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// The Green's coefficients of a grid from the process cache (keyed by device, grid, box, xi, eta), computed on
+// stream st and entered in the cache when absent; a cached entry filled on another stream is waited for.
+static int acquire_green(const GridParams &gp, const double *box, double xi, int64_t Gc,
+                         std::shared_ptr<GreenCoef> &out, cudaStream_t st) {
+    GreenKey key;
+    memset(&key, 0, sizeof(key));
+    key.dev = current_device();
+    for (int k = 0; k < 3; ++k) {
+        key.N[k] = gp.N[k];
+        key.box[k] = box[k];
+        key.eta[k] = gp.eta[k];
+    }
+    key.xi = xi;
+    std::lock_guard<std::mutex> lk(g_green_mu);
+    auto it = g_green.find(key);
+    if (it != g_green.end()) {
+        out = it->second;
+        MPS_CUDA_TRY(cudaStreamWaitEvent(st, out->ev_h, 0));
+        return MPS_OK;
+    }
+    auto gc = std::make_shared<GreenCoef>();
+    MPS_TRY(dalloc_persistent(&gc->h64, sizeof(double) * Gc));
+    MPS_TRY(dalloc_persistent(&gc->h32, sizeof(float) * Gc));
+    MPS_TRY(green_half(gp, gc->h64, gc->h32, st));
+    MPS_TRY(green_mark_filled(&gc->ev_h, st));
+    if (g_green.size() >= kGreenCacheMax) g_green.clear();  // systems keep their own reference
+    g_green[key] = gc;
+    out = gc;
+    return MPS_OK;
+}
+
 extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps_stream_t stream) {
     if (!d || !out) return MPS_BAD_ARG;
     *out = nullptr;
@@ -1927,33 +2038,27 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CR_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P, st));
     CR_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P, st));
     CR_TRY(grid_geometry(s->x, n, s->gp, s->start, s->w64, s->w32, st));
-    {
-        GreenKey key;
-        memset(&key, 0, sizeof(key));
-        key.dev = current_device();
-        for (int k = 0; k < 3; ++k) {
-            key.N[k] = s->gp.N[k];
-            key.box[k] = d->box[k];
-            key.eta[k] = s->gp.eta[k];
-        }
-        key.xi = d->xi;
-        std::lock_guard<std::mutex> lk(g_green_mu);
-        auto it = g_green.find(key);
-        if (it != g_green.end()) {
-            s->green = it->second;
-            CR_TRY(cudaStreamWaitEvent(st, s->green->ev_h, 0) == cudaSuccess ? MPS_OK : MPS_CUDA_ERR);
-        } else {
-            auto gc = std::make_shared<GreenCoef>();
-            CR_TRY(dalloc_persistent(&gc->h64, sizeof(double) * s->Gc));
-            CR_TRY(dalloc_persistent(&gc->h32, sizeof(float) * s->Gc));
-            CR_TRY(green_half(s->gp, gc->h64, gc->h32, st));
-            CR_TRY(green_mark_filled(&gc->ev_h, st));
-            if (g_green.size() >= kGreenCacheMax) g_green.clear();  // systems keep their own reference
-            g_green[key] = gc;
-            s->green = gc;
-        }
-        s->h64 = s->green->h64;
-        s->h32 = s->green->h32;
+    CR_TRY(acquire_green(s->gp, d->box, d->xi, s->Gc, s->green, st));
+    s->h64 = s->green->h64;
+    s->h32 = s->green->h32;
+    // the inner grid of the gradient-form operator, when asked for (dipole operator, tiled kernels)
+    if (d->inner_P > 0) {
+        for (int k = 0; k < 3; ++k)
+            if (d->inner_Ngrid[k] < d->inner_P) CR_TRY(MPS_BAD_ARG);
+        if (d->inner_P > kMaxP) CR_TRY(MPS_BAD_ARG);
+        s->inner = new InnerGrid();
+        InnerGrid &ig = *s->inner;
+        ig.gp = make_grid_params(d->inner_Ngrid, d->box, d->xi, nullptr, d->inner_P);
+        if (!tiles_supported(ig.gp, 8)) CR_TRY(MPS_BAD_ARG);
+        ig.Gc = (int64_t)(ig.gp.N[0] / 2 + 1) * ig.gp.N[1] * ig.gp.N[2];
+        CR_TRY(dalloc(&ig.start, sizeof(int32_t) * 3 * n, st));
+        CR_TRY(dalloc(&ig.w64, sizeof(double) * 3 * n * ig.gp.P, st));
+        CR_TRY(dalloc(&ig.w32, sizeof(float) * 3 * n * ig.gp.P, st));
+        CR_TRY(dalloc(&ig.g32, sizeof(float) * 3 * n * ig.gp.P, st));
+        CR_TRY(grid_geometry(s->x, n, ig.gp, ig.start, ig.w64, ig.w32, st));
+        CR_TRY(grad_factors(s->x, n, ig.gp, ig.w64, ig.g32, st));
+        CR_TRY(tile_bins_build(ig.start, n, ig.gp, 8, ig.tb, st));
+        CR_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, st));
     }
 #undef CR_TRY
     *out = s;

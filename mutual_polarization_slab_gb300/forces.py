@@ -73,9 +73,10 @@ class EnergyResult:
 
 
 def polarization_energy(x, beta, box, H0, xi, rc, Ngrid, P, *, tol=1e-10, restart=30, maxit=200, precision="fp64",
-                        guess=None, slab_factor=0.0, tables=None, system=None) -> EnergyResult:
+                        guess=None, slab_factor=0.0, tables=None, system=None, inner_grid="auto") -> EnergyResult:
     """Solve A(x) m = H0 for spheres of contrast ``beta`` (scalar or (N,)) and
-    return E = -1/2 sum m . H0 with its gradients."""
+    return E = -1/2 sum m . H0 with its gradients.  ``inner_grid`` as in
+    ``capacitance.capacitance_tensor`` (mixed precision only)."""
     xd = as_device(x).reshape(-1, 3)
     n = xd.shape[0]
     b = as_device(np.broadcast_to(np.asarray(beta.cpu() if isinstance(beta, torch.Tensor) else beta,
@@ -85,7 +86,7 @@ def polarization_energy(x, beta, box, H0, xi, rc, Ngrid, P, *, tol=1e-10, restar
         tables = capacitance.default_table(xi)
     perp, para, rv = tables
     sysm = system or SpectralEwaldSystem(xd, eps, box, xi, rc, Ngrid, P, perp, para, rv, slab_factor=slab_factor,
-                                         max_rhs=1)
+                                         max_rhs=1, inner=inner_grid if precision == "mixed" else None)
     h0 = torch.as_tensor(np.asarray(H0, dtype=np.float64).reshape(3), device="cuda")
     rhs = h0.repeat(n, 1)
     x0 = None if guess is None else as_device(guess).reshape(n, 3)
@@ -146,7 +147,7 @@ class BrownianDynamics:
         eps = eps_from_beta(self.beta)
         perp, para, rv = self.tables
         s = SpectralEwaldSystem(self.x, eps, self.box, self.xi, self.rc, self.Ngrid, self.P, perp, para, rv,
-                                slab_factor=0.0, max_rhs=1)
+                                slab_factor=0.0, max_rhs=1, inner="auto" if self.precision == "mixed" else None)
         try:
             if self.m is None or self.step_count % self.pol_every == 0:
                 rhs = torch.as_tensor(self.H0, device="cuda").repeat(self.n, 1)

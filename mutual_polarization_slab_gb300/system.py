@@ -57,6 +57,45 @@ def spectral_parameters(box, xi, errortol):
     return rc, Ngrid, h, P, eta
 
 
+# cuFFT runs sizes 2^a 3^b 5^c fastest; the inner grid takes the smallest of these with b + c <= 2 (128, 144,
+# 160, 192, 200, ...) at or above the tolerance rule's size
+def _fast_size(n: int) -> int:
+    m = max(int(n), 1)
+    while True:
+        k = m
+        b = c = 0
+        while k % 2 == 0:
+            k //= 2
+        while k % 3 == 0:
+            k //= 3
+            b += 1
+        while k % 5 == 0:
+            k //= 5
+            c += 1
+        if k == 1 and b + c <= 2:
+            return m
+        m += 1
+
+
+def inner_grid(box, xi, Ngrid, P, tol=3e-5, min_P=8):
+    """Coarser discretisation for the float32 gradient-form inner operator of the
+    mixed solve: the grid of the tolerance rule at ``tol`` (rounded up to a fast
+    FFT size) with support ``max(min_P, rule)``, capped by the system's own
+    ``P``; None when it would not be clearly smaller than the system's grid
+    ``Ngrid``.  The refinement residuals use the system's own grid, so the solve
+    still converges to that operator's solution; the inner grid only has to be
+    good enough for corrections (about 2e-4 from the reference operator at P = 8)."""
+    box = np.asarray(box, dtype=np.float64).reshape(3)
+    Ngrid = np.asarray(Ngrid, dtype=np.int64).reshape(3)
+    lt = math.sqrt(-math.log(tol))
+    ng = np.array([_fast_size(math.ceil(1.0 + L * 2.0 * xi * lt / math.pi)) for L in box], dtype=np.int64)
+    Pi = min(int(P), max(int(min_P), int(math.ceil(-2.0 * math.log(tol) / math.pi))))
+    ng = np.maximum(ng, 16)
+    if np.prod(ng) >= 0.8 * np.prod(Ngrid) or np.any(ng > Ngrid):
+        return None
+    return ng, Pi
+
+
 def fft_size(n: int) -> int:
     """Smallest m >= n whose prime factors are 2, 3 and 5 (radices cuFFT runs
     fast; few such sizes, so many configurations share their plans)."""
@@ -85,6 +124,11 @@ class SpectralEwaldSystem:
     ``Capacitance_Quadrupole/MatrixVectorMultiply.m``: 8 unknowns per sphere,
     stored per particle as (Sx, Sy, Sz, Qxx, Qxy, Qxz, Qyy, Qyz); it has no slab term.
 
+    ``inner`` sets the discretisation of the float32 gradient-form operator
+    (the mixed solve's inner operator, dipole systems): None uses the system's
+    grid, ``(Ngrid_in, P_in)`` a grid of its own, ``"auto"`` the coarser grid of
+    ``inner_grid`` when there is one.
+
     With ``radius`` (N radii) it is the polydisperse operator of
     ``Capacitance_Sizes/ComputeField.m`` (scalar eta, no slab term; ``perp``,
     ``para`` unused).  ``sizes_tables`` ((2, M(M+1)/2, n_tab) on ``rvals``) with
@@ -94,7 +138,8 @@ class SpectralEwaldSystem:
     """
 
     def __init__(self, x, lambdap, box, xi, rc, Ngrid, P, perp, para, rvals, slab_factor=1.0, eta=None,
-                 max_rhs=3, quad_tables=None, radius=None, radius_class=None, n_class=0, sizes_tables=None):
+                 max_rhs=3, quad_tables=None, radius=None, radius_class=None, n_class=0, sizes_tables=None,
+                 inner=None):
         lib = L.lib()
         self._lib = lib
         self._h = C.c_void_p(0)
@@ -181,6 +226,16 @@ class SpectralEwaldSystem:
         d.n_class = int(n_class)
         d.sizes_tables = self.sizes_tables.data_ptr() if self.sizes_tables is not None else None
         d.lambdap_imag = self.lambdap_imag.data_ptr() if self.lambdap_imag is not None else None
+        if isinstance(inner, str) and inner == "auto":
+            inner = inner_grid(self.box, self.xi, self.Ngrid, self.P) if self.kind == L.MPS_DIPOLE else None
+        self.inner = None
+        if inner is not None:
+            if self.kind != L.MPS_DIPOLE:
+                raise ValueError("an inner grid is available for the dipole operator")
+            ng_in, p_in = inner
+            self.inner = (np.asarray(ng_in, dtype=np.int64).reshape(3), int(p_in))
+            d.inner_Ngrid = (C.c_int64 * 3)(*self.inner[0])
+            d.inner_P = self.inner[1]
         if self.cplx and self.kind != L.MPS_DIPOLE:
             raise ValueError("complex permittivities are supported for the dipole operator")
         L.check(lib.mps_system_create(C.byref(d), C.byref(self._h), L.stream_handle()), "mps_system_create")

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     missing = [name for name in _declared() if not hasattr(lib, name)]
     assert not missing, f"not exported: {missing}"
     assert set(_declared()) == set(_lib.EXPORTS) | set(n for n in _declared() if n in _lib.EXPORTS)
-    assert lib.mps_abi_version() == 3
+    assert lib.mps_abi_version() == 4
     assert lib.mps_status_string(3).decode().startswith("pair separation")
 
 

@@ -9,8 +9,9 @@ xi = 4 / rc, fully periodic -- the workload bench.py times.
   reference discretisation 2e-5 (max-norm relative); the gradient form of the
   float32 operator differs from the reference discretisation by the sampling
   error of the Gaussian's derivative, 3e-5 relative in the 2-norm;
-* the mixed-precision tensor solve (the headline solve, tol 1e-7) and a float64
-  GPU solve (tol 1e-11): their true residuals under the ORACLE operator,
+* the mixed-precision tensor solve (the headline solve, tol 1e-7, inner solves
+  on the coarser inner grid) and a float64 GPU solve (tol 1e-11): their true
+  residuals under the ORACLE operator,
   ||b - A_oracle m|| / ||b|| per field direction, and the mixed moments against
   the float64 ones (<= 1e-6, the mixed-precision bound)."""
 import math
@@ -43,8 +44,12 @@ def headline():
     # the oracle's own tables on both sides: the comparison is of the operators, not of two table builds
     # (the GPU's tables agree with the reference's to 1e-12 relative, tests/test_gpu_parity.py)
     s = SpectralEwaldSystem(x, eps, box, xi, rc, [GRID] * 3, P, perp, para, rv, slab_factor=0.0, max_rhs=3)
-    yield dict(x=x, box=box, xi=xi, rc=rc, eps=eps, geo=geo, sys=s)
+    # the headline solve's system: its mixed solve runs the inner operator on the coarser inner grid
+    s_in = SpectralEwaldSystem(x, eps, box, xi, rc, [GRID] * 3, P, perp, para, rv, slab_factor=0.0, max_rhs=3,
+                               inner="auto")
+    yield dict(x=x, box=box, xi=xi, rc=rc, eps=eps, geo=geo, sys=s, sys_inner=s_in)
     s.close()
+    s_in.close()
 
 
 def _maxrel(a, b):
@@ -72,8 +77,9 @@ def test_tensor_solves_true_residual_under_oracle(headline):
     eye = torch.eye(3, dtype=torch.float64, device="cuda")
     b = eye[:, None, :].expand(3, N, 3).contiguous()
     x0 = torch.stack([amp[:, None] * eye[i] for i in range(3)]).contiguous()
-    m_mix, info_mix = s.solve(b, x0, tol=1e-7, restart=30, maxit=8, precision="mixed", inner_tol=1e-4,
-                              inner_maxit=3)
+    assert headline["sys_inner"].inner is not None
+    m_mix, info_mix = headline["sys_inner"].solve(b, x0, tol=1e-7, restart=30, maxit=8, precision="mixed",
+                                                  inner_tol=1e-4, inner_maxit=3)
     m_64, info_64 = s.solve(b, x0, tol=1e-11, restart=30, maxit=100, precision="fp64")
     assert all(i.converged for i in info_mix) and all(i.converged for i in info_64)
     bh = b.cpu().numpy()
