@@ -106,8 +106,8 @@ struct StageEvents {
 // A coarser discretisation for the float32 gradient-form operator (the mixed solve's inner operator): its own
 // grid, support P and spectral splitting eta, the same xi and the same pair sum.  The inner solves only have to
 // reach 1e-4 .. 1e-3 of their right-hand sides, and every refinement residual uses the reference operator, so
-// the inner grid is chosen for speed: its distance from the reference operator (about 2e-4 relative at a
-// 3e-5 rule with P = 8) only costs the refinement a little more drift, bounded below.
+// the inner grid is chosen for speed as long as its distance from the reference operator stays inside the
+// refinement's drift bound (the grid of the tolerance rule at 2.5e-4 with the system's support P: 3e-5..6e-5).
 struct InnerGrid {
     GridParams gp;
     int64_t Gc = 0;
@@ -1671,9 +1671,9 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
     // relative distance from the reference operator is measured at 5e-6..1.1e-4
     // for supports P = 10..8).  The drift adds up over the corrections since the
     // last true residual; when it could exceed the target, one true residual decides.
-    // the coarser inner grid (when the system has one) adds its discretisation's distance, about 2e-4 at the
-    // inner grids chosen here, to the gradient form's own: a bound twice as wide
-    const double kGradMismatch = s->inner ? 6e-4 : 3e-4;
+    // A coarser inner grid (when the system has one) adds its discretisation's distance to the gradient form's
+    // own; the inner grids chosen by the Python layer keep it at 3e-5..6e-5 (measured), inside the same bound.
+    constexpr double kGradMismatch = 3e-4;
     bool estimated = false;
     std::vector<double> drift(nrhs, 0.0);
     for (step = 1; e == MPS_OK; ++step) {

@@ -112,7 +112,7 @@ def test_inner_grid_operator_and_mixed_solve():
     eps = np.full(n, 19.0)
     xi, rc, P = 0.7, 5.5, 10
     perp, para, rv = gcap.default_table(xi)
-    inner = (np.array([32, 30, 36]), 8)
+    inner = (np.array([32, 30, 36]), 10)
     s = SpectralEwaldSystem(x, eps, box, xi, rc, (48, 48, 48), P, perp, para, rv, slab_factor=0.0, max_rhs=3,
                             inner=inner)
     m = np.random.default_rng(2).standard_normal((3, n, 3))
