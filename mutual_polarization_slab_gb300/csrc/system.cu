@@ -499,7 +499,7 @@ static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     // MPS_TILE_DEPTH=4 or 8 fixes the depth instead of timing (A/B comparisons and tests); not cached
     if (const char *fd = getenv("MPS_TILE_DEPTH")) {
         const int d = atoi(fd);
-        if ((d == 4 || d == 8) && tiles_supported(s->gp, d)) {
+        if ((d == 4 || d == 8 || (d == 16 && use == kTileGrad32)) && tiles_supported(s->gp, d)) {
             *tz = d;
             return MPS_OK;
         }
@@ -925,7 +925,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     {
         // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing); default: warp gather
         const char *e = getenv("MPS_GRAD_CONTRACT");
-        if (e && strcmp(e, "tiled") == 0) {
+        if (e && strcmp(e, "tiled") == 0 && s->tb32.tz != 16) {
             if (!s->partial32)
                 MPS_TRY(dalloc(&s->partial32, (size_t)s->tb32.nentries * 9 * sizeof(float), st));
             MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tb32, s->partial32,
@@ -2057,7 +2057,10 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         CR_TRY(dalloc(&ig.g32, sizeof(float) * 3 * n * ig.gp.P, st));
         CR_TRY(grid_geometry(s->x, n, ig.gp, ig.start, ig.w64, ig.w32, st));
         CR_TRY(grad_factors(s->x, n, ig.gp, ig.w64, ig.g32, st));
-        CR_TRY(tile_bins_build(ig.start, n, ig.gp, 8, ig.tb, st));
+        int tz_in = 8;   // MPS_TILE_DEPTH=16 selects depth-16 tiles for the inner grid's spread (A/B timing)
+        if (const char *fd = getenv("MPS_TILE_DEPTH"))
+            if (atoi(fd) == 16 && tiles_supported(ig.gp, 16)) tz_in = 16;
+        CR_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, st));
         CR_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, st));
     }
 #undef CR_TRY

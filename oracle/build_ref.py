@@ -4,8 +4,10 @@ Checker only: the built module pins ``oracle/dipole_forces_oracle.py`` (tests
 and golden-vector generation in this checkout).  It compiles the single source
 file ``CPU - HOOMD simulation test/dipole_forces_ext/_dipole_forces_ext.cpp``
 where it lies, with g++ and the installed pybind11 headers; nothing is copied.
-Skipped (returns None) when the reference tree or pybind11 is absent, e.g. on
-a machine that only runs the GPU tests.
+The reference checkout is named by the argument or the MPS_REFERENCE_ROOT
+environment variable.  Skipped (returns None) when neither names an existing
+reference tree, or pybind11 is absent, e.g. on a machine that only runs the
+GPU tests.
 """
 from __future__ import annotations
 
@@ -20,7 +22,9 @@ SRC_REL = os.path.join("CPU - HOOMD simulation test", "dipole_forces_ext", "_dip
 
 
 def build(ref_root=None):
-    ref_root = ref_root or os.environ.get("MPS_REFERENCE_ROOT", "/root/reference")
+    ref_root = ref_root or os.environ.get("MPS_REFERENCE_ROOT")
+    if not ref_root:
+        return None
     src = os.path.join(ref_root, SRC_REL)
     if not os.path.exists(src):
         return None

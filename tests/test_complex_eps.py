@@ -91,3 +91,28 @@ def test_complex_spectrum_api():
     assert np.abs(Cs.real - C0).max() <= 1e-6 * np.abs(C0).max()
     assert np.abs(Cs.imag).max() <= 1e-6 * np.abs(C0).max()
     assert np.abs(C.imag).max() > 1e-3 * np.abs(C.real).max()
+
+
+def test_single_sphere_complex_polarisability_is_clausius_mossotti():
+    """One sphere per cubic cell: the lattice sum of a cubic lattice vanishes and the
+    conducting boundary adds phi m / (4 pi), so m = 4 pi beta / (1 - beta phi) H0
+    with beta = (eps - 1) / (eps + 2) exactly (the real-eps case agrees to the Ewald
+    tolerance, 4e-9).  With a complex eps this is the complex polarisability: an
+    analytic pin of the complex semantics independent of the restatement."""
+    L = 20.0
+    box = np.full(3, L)
+    x = np.array([[L / 2, L / 2, L / 2]])
+    xi, tol = 0.5, 1e-10
+    rc, Ng, _, P, _ = co.spectral_parameters(box, xi, tol)
+    perp, para, rv = gcap.default_table(xi)
+    phi = 4.0 * np.pi / (3.0 * L ** 3)
+    for eps in (5.0 + 2.0j, 28.0 + 9.0j, 3.0 - 0.5j):
+        s = SpectralEwaldSystem(x, np.array([eps]), box, xi, rc, Ng, P, perp, para, rv, slab_factor=0.0, max_rhs=1)
+        m, info = s.solve(np.array([[0.0, 0.0, 1.0]], dtype=complex), None, tol=1e-12, restart=10, maxit=20,
+                          precision="fp64")
+        s.close()
+        beta = (eps - 1.0) / (eps + 2.0)
+        pred = 4.0 * np.pi * beta / (1.0 - beta * phi)
+        m = m.cpu().numpy()[0]
+        assert abs(m[2] - pred) <= 1e-7 * abs(pred), (eps, m[2], pred)
+        assert abs(m[0]) + abs(m[1]) <= 1e-12 * abs(pred)

@@ -152,3 +152,26 @@ def test_threaded_real_operator_matches_single_thread():
     for threads in (1, 5):
         got = g.field_real_many(M, threads=threads)
         assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_single_sphere_polarisability_is_clausius_mossotti():
+    """One sphere per cubic cell: m = 4 pi beta / (1 - beta phi) H0, beta = (eps - 1)/(eps + 2),
+    for real and complex eps (the cubic lattice sum vanishes; the conducting boundary adds
+    phi m / (4 pi)): the oracle's operator with the dielectric term of a complex eps."""
+    import math
+    L = 20.0
+    box = np.full(3, L)
+    x = np.array([[L / 2, L / 2, L / 2]])
+    xi = 0.5
+    rc, Ng, _, P, _ = co.spectral_parameters(box, xi, 1e-10)
+    perp, para, rv = ew.default_table(xi)
+    g = ew.Geometry(x, np.array([2.0]), box, xi, rc, Ng, P, perp, para, rv, 0.0)
+    A2 = np.stack([g.field_real(np.eye(3)[c][None])[0] for c in range(3)], axis=1)
+    phi = 4.0 * math.pi / (3.0 * L ** 3)
+    d = lambda e: -3.0 / (4.0 * math.pi * (1.0 - e))
+    for eps in (5.0, 28.0, 5.0 + 2.0j, 3.0 - 0.5j):
+        A = A2 + (d(eps) - d(2.0)) * np.eye(3)
+        m = np.linalg.solve(A, np.array([0.0, 0.0, 1.0]))
+        beta = (eps - 1.0) / (eps + 2.0)
+        pred = 4.0 * math.pi * beta / (1.0 - beta * phi)
+        assert abs(m[2] - pred) <= 1e-7 * abs(pred), (eps, m[2], pred)
