@@ -405,11 +405,13 @@ int mps_system_stage_times(mps_system *sys, double *ms, int64_t *count);
  * coefficients keep them until destroyed.  Host only; no GPU work. */
 int mps_kspace_cache_clear(void);
 
-/* Tile depth the autotuner chose for the tiled kernels: tile_depth[0] for the
- * float64-width tiles (float64 or double-float spread, whichever ran first),
- * [1] for the float32 tiles (gradient-form spread, or the reference-form spread
- * + contract) (0 = not used yet); ms[4] = the timed candidates (depth 4, depth 8)
- * of those kernels, float64-width then float32, -1 where not timed. */
+/* Tile depth of the tiled kernels: tile_depth[0] for the float64-width tiles
+ * (float64 or double-float spread, whichever ran first, timed by the
+ * autotuner), [1] for the float32 tiles (the gradient-form spread -- on the
+ * inner grid when the system has one, depth 16 where the grid allows it, not
+ * timed -- or the reference-form spread + contract) (0 = not used yet);
+ * ms[4] = the timed candidates (depth 4, depth 8) of those kernels,
+ * float64-width then float32, -1 where not timed. */
 int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms);
 
 #ifdef __cplusplus

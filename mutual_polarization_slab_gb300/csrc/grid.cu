@@ -140,14 +140,19 @@ __global__ void __launch_bounds__(256) k_contract(const T *__restrict__ grid, in
 // Green's coefficient over the R2C half spectrum (Nz, Ny, Nx/2+1), including the
 // 1/G of the unnormalised inverse transform:
 //   H(k) = 9 pi / (2|k|) J_{3/2}(|k|)^2 exp(-sum_d (1-eta_d) k_d^2 / (4 xi^2)) / |k|^2 / G
+// With J_{3/2}(k) = sqrt(2 / (pi k)) (sin k / k - cos k) this is
+//   9 (sin k - k cos k)^2 exp(...) / k^6,
+// one sincos, one square root and one division per point (float64 issue is what this kernel costs).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double green_coef(double kx, double ky, double kz, const GridParams &gp) {
     const double k2 = kx * kx + ky * ky + kz * kz;
     if (k2 == 0.0) return 0.0;
     const double kk = sqrt(k2);
-    const double J = sqrt(2.0 / (MPS_PI * kk)) * (sin(kk) / kk - cos(kk));
+    double sk, ck;
+    sincos(kk, &sk, &ck);
+    const double u = sk - kk * ck;
     const double etak2 = (1.0 - gp.eta[0]) * kx * kx + (1.0 - gp.eta[1]) * ky * ky + (1.0 - gp.eta[2]) * kz * kz;
-    double H = (9.0 * MPS_PI) / (2.0 * kk) * (J * J) * exp(-etak2 / (4.0 * gp.xi * gp.xi)) / k2;
+    double H = 9.0 * u * u * exp(-etak2 / (4.0 * gp.xi * gp.xi)) / (k2 * k2 * k2);
     if (!isfinite(H)) H = 0.0;
     return H;
 }

@@ -2461,7 +2461,7 @@ extern "C" int mps_kspace_cache_clear(void) {
 extern "C" int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms) {
     if (!sys || !tile_depth || !ms) return MPS_BAD_ARG;
     tile_depth[0] = sys->tb64.tz;
-    tile_depth[1] = sys->tbg.mem ? sys->tbg.tz : sys->tb32.tz;
+    tile_depth[1] = sys->inner ? sys->inner->tb.tz : (sys->tbg.mem ? sys->tbg.tz : sys->tb32.tz);
     for (int p = 0; p < 2; ++p) {
         TuneKey key;
         memset(&key, 0, sizeof(key));
