@@ -414,6 +414,18 @@ int mps_kspace_cache_clear(void);
  * float64-width then float32, -1 where not timed. */
 int mps_system_tuning(const mps_system *sys, int32_t *tile_depth, float *ms);
 
+/* GMRES step graphs of a system (no reference counterpart: the reference's
+ * GMRES loop, EW/capacitance.py:60-199, runs on the host).  mps_gmres runs the
+ * Arnoldi steps of a cycle as one CUDA graph launch -- a while-conditional node
+ * whose body is one step (matvec, Gram-Schmidt, Givens update, next basis
+ * vector, device-side convergence test) -- once a matvec of that precision and
+ * batch width has run outside a capture; the host reads the convergence
+ * estimates once per launch instead of once per step.  built = graphs
+ * instantiated, failed = configurations whose capture the runtime refused
+ * (those keep host-driven steps).  The environment variable
+ * MPS_GMRES_GRAPH=0 selects the host-driven steps. */
+int mps_system_graphs(const mps_system *sys, int32_t *built, int32_t *failed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,7 @@ EXPORTS = (
     "mps_real_space_fast", "mps_pre_calculations", "mps_grid_kernel", "mps_spread_fast", "mps_contract_fast",
     "mps_precompute_kspace", "mps_scale_fast", "mps_system_create", "mps_system_destroy", "mps_system_info",
     "mps_matvec", "mps_matvec_complex", "mps_gmres", "mps_kernel_launches", "mps_system_profile",
-    "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning",
+    "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning", "mps_system_graphs",
     "mps_dipole_forces", "mps_quad_table", "mps_sizes_table", "mps_adjoint_forces",
     "mps_real_space_table_probe", "mps_field_map", "mps_quad_table_probe", "mps_field_map_quad",
     "mps_field_map_sizes", "mps_kspace_cache_clear",
@@ -90,6 +90,7 @@ _SIGS = {
     "mps_system_stage_times": (C.c_int, [p, PD, P64]),
     "mps_neighbor_list_noalloc": (C.c_int, [p, i64, P64, p, p, i64, P64, p]),
     "mps_system_tuning": (C.c_int, [p, C.POINTER(i32), C.POINTER(C.c_float)]),
+    "mps_system_graphs": (C.c_int, [p, C.POINTER(i32), C.POINTER(i32)]),
     "mps_kspace_cache_clear": (C.c_int, []),
     "mps_dipole_forces": (C.c_int, [p, p, i64, PD, f64, f64, i32, p, p, p]),
     "mps_quad_table": (C.c_int, [p, i64, f64, p, p]),

@@ -11,7 +11,24 @@ namespace mps {
 static char g_last_error[512] = "";
 static std::atomic<unsigned long long> g_launches{0};
 
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static thread_local long long t_captured = -1;   // >= 0 while this thread captures a graph
+
+void count_launch() {
+    if (t_captured >= 0) {
+        ++t_captured;
+        return;
+    }
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void capture_count_begin() { t_captured = 0; }
+long long capture_count_end() {
+    const long long c = t_captured;
+    t_captured = -1;
+    return c < 0 ? 0 : c;
+}
+void add_launches(long long k) {
+    if (k > 0) g_launches.fetch_add((unsigned long long)k, std::memory_order_relaxed);
+}
 
 void set_last_error(cudaError_t e, const char *what, const char *file, int line) {
     snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);

@@ -34,6 +34,12 @@ constexpr int kWarp = 32;
 
 void set_last_error(cudaError_t e, const char *what, const char *file, int line);
 void count_launch();
+// Kernels enqueued while this thread captures a CUDA graph are not launches:
+// between capture_count_begin and capture_count_end count_launch counts them
+// for the caller (the launches per graph execution) instead of the process total.
+void capture_count_begin();
+long long capture_count_end();
+void add_launches(long long k);
 
 inline unsigned grid_for(int64_t work, int block, int64_t cap = 152 * 32) {
     int64_t g = (work + block - 1) / block;
@@ -67,6 +73,32 @@ __device__ __forceinline__ int fft_freq(int i, int n) {
     int p = i + c;
     if (p >= n) p -= n;
     return p - c;
+}
+
+// Quarter of an R2C half spectrum (Nx/2+1, Ny, Nz; x fastest): the points with
+// iy <= Ny/2 and iz <= Nz/2.  Index N - i has frequency -fft_freq(i, N), so a
+// coefficient that depends on k only through kx^2, ky^2, kz^2 is the same at
+// (ix, +-iy, +-iz); mirror_points calls f(linear index, sy, sz) once for each
+// distinct such point, sy / sz = -1 where the y / z index was mirrored.
+struct HalfQuarter {
+    int Nxh, Ny, Nz, Nyq, Nzq;
+    __host__ __device__ explicit HalfQuarter(const int N[3])
+        : Nxh(N[0] / 2 + 1), Ny(N[1]), Nz(N[2]), Nyq(N[1] / 2 + 1), Nzq(N[2] / 2 + 1) {}
+    __host__ __device__ int64_t size() const { return (int64_t)Nxh * Nyq * Nzq; }
+    __device__ void point(int64_t t, int *ix, int *iy, int *iz) const {
+        *ix = (int)(t % Nxh);
+        *iy = (int)((t / Nxh) % Nyq);
+        *iz = (int)(t / ((int64_t)Nxh * Nyq));
+    }
+};
+
+template <class F>
+__device__ __forceinline__ void mirror_points(const HalfQuarter &q, int ix, int iy, int iz, F &&f) {
+    const int my = (q.Ny - iy) % q.Ny, mz = (q.Nz - iz) % q.Nz;
+    const int na = my == iy ? 1 : 2, nb = mz == iz ? 1 : 2;
+    for (int a = 0; a < na; ++a)
+        for (int b = 0; b < nb; ++b)
+            f(((int64_t)(b ? mz : iz) * q.Ny + (a ? my : iy)) * q.Nxh + ix, a ? -1 : 1, b ? -1 : 1);
 }
 
 __device__ __forceinline__ int64_t wrap_index(int64_t i, int64_t n) {

@@ -501,12 +501,17 @@ __global__ void k_fft_z_scale(typename A::S *__restrict__ spec, int nrhs, GridPa
 
 // Symmetric scale tensor H q q^T per half-spectrum point, Nyquist rule applied,
 // as double-float entries (00, 01, 02, 11, 12, 22): computed once per grid in
-// float64 so the double-float z pass only reads it.
+// float64 so the double-float z pass only reads it.  One thread per point of the
+// spectrum's quarter (iy <= Ny/2, iz <= Nz/2): a mirrored point has H and the
+// Nyquist flags of the original and q_y (q_z) negated exactly, so its entries are
+// the original's with the signs of q_I q_J.
 __global__ void k_df_tm6(GridParams gp, const double *__restrict__ H, float2 *__restrict__ tm6) {
-    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2], Nxh = Nx / 2 + 1;
-    const int64_t Gc = (int64_t)Nxh * Ny * Nz;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc; t += (int64_t)gridDim.x * blockDim.x) {
-        const int kx = (int)(t % Nxh), ky = (int)((t / Nxh) % Ny), kz = (int)(t / ((int64_t)Nxh * Ny));
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const HalfQuarter hq(gp.N);
+    const int64_t Gq = hq.size();
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gq; t += (int64_t)gridDim.x * blockDim.x) {
+        int kx, ky, kz;
+        hq.point(t, &kx, &ky, &kz);
         const double qx = fft_freq(kx, Nx) * gp.kfac[0];
         const double qy = fft_freq(ky, Ny) * gp.kfac[1];
         const double qz = fft_freq(kz, Nz) * gp.kfac[2];
@@ -520,19 +525,26 @@ __global__ void k_df_tm6(GridParams gp, const double *__restrict__ H, float2 *__
         }
         const bool ny3[3] = {(Nx % 2 == 0) && (kx == Nx / 2), (Ny % 2 == 0) && (ky == Ny / 2),
                              (Nz % 2 == 0) && (kz == Nz / 2)};
-        const double h = H[t];
+        const double h = H[((int64_t)kz * Ny + ky) * hq.Nxh + kx];
         const int I[6] = {0, 0, 0, 1, 1, 2}, J[6] = {0, 1, 2, 1, 2, 2};
+        float2 e6[6];
         for (int e = 0; e < 6; ++e) {
             const double v = (ny3[I[e]] == ny3[J[e]]) ? h * q[I[e]] * q[J[e]] : 0.0;
             const dfr d = dfrom(v);
-            tm6[6 * t + e] = make_float2(d.hi, d.lo);
+            e6[e] = make_float2(d.hi, d.lo);
         }
+        mirror_points(hq, kx, ky, kz, [&](int64_t i, int sy, int sz) {
+            const int sg[3] = {1, sy, sz};
+            for (int e = 0; e < 6; ++e) {
+                const float2 v = e6[e];
+                tm6[6 * i + e] = sg[I[e]] * sg[J[e]] > 0 ? v : make_float2(-v.x, -v.y);
+            }
+        });
     }
 }
 
 int df_scale_table(const GridParams &gp, const double *H, float2 *tm6, cudaStream_t s) {
-    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
-    k_df_tm6<<<grid_for(Gc, 256), 256, 0, s>>>(gp, H, tm6);
+    k_df_tm6<<<grid_for(HalfQuarter(gp.N).size(), 256), 256, 0, s>>>(gp, H, tm6);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

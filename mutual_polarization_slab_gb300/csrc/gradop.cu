@@ -46,19 +46,21 @@ __global__ void k_grad_factors(const double *__restrict__ x, int64_t n, GridPara
     }
 }
 
-// H / |k|^2 on the half spectrum (float32), H including 1/G; zero at k = 0.
+// H / |k|^2 on the half spectrum (float32), H including 1/G; zero at k = 0.  One
+// thread per point of the spectrum's quarter, written to its mirrored points (same
+// |k|^2 and H there).
 __global__ void k_grad_scale_coef(GridParams gp, const double *__restrict__ H, float *__restrict__ hs) {
-    const int Nxh = gp.N[0] / 2 + 1;
-    const int64_t Gc = (int64_t)Nxh * gp.N[1] * gp.N[2];
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc; t += (int64_t)gridDim.x * blockDim.x) {
-        const int ix = (int)(t % Nxh);
-        const int iy = (int)((t / Nxh) % gp.N[1]);
-        const int iz = (int)(t / ((int64_t)Nxh * gp.N[1]));
+    const HalfQuarter q(gp.N);
+    const int64_t Gq = q.size();
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gq; t += (int64_t)gridDim.x * blockDim.x) {
+        int ix, iy, iz;
+        q.point(t, &ix, &iy, &iz);
         const double kx = fft_freq(ix, gp.N[0]) * gp.kfac[0];
         const double ky = fft_freq(iy, gp.N[1]) * gp.kfac[1];
         const double kz = fft_freq(iz, gp.N[2]) * gp.kfac[2];
         const double k2 = kx * kx + ky * ky + kz * kz;
-        hs[t] = k2 > 0 ? (float)(H[t] / k2) : 0.f;
+        const float v = k2 > 0 ? (float)(H[((int64_t)iz * q.Ny + iy) * q.Nxh + ix] / k2) : 0.f;
+        mirror_points(q, ix, iy, iz, [&](int64_t i, int, int) { hs[i] = v; });
     }
 }
 
@@ -402,8 +404,7 @@ int grad_factors(const double *x, int64_t n, const GridParams &gp, const double 
 }
 
 int grad_scale_coef(const GridParams &gp, const double *H, float *hs, cudaStream_t s) {
-    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
-    k_grad_scale_coef<<<grid_for(Gc, 256), 256, 0, s>>>(gp, H, hs);
+    k_grad_scale_coef<<<grid_for(HalfQuarter(gp.N).size(), 256), 256, 0, s>>>(gp, H, hs);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

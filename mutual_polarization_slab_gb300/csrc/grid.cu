@@ -157,20 +157,25 @@ __device__ __forceinline__ double green_coef(double kx, double ky, double kz, co
     return H;
 }
 
+// One thread per point of the spectrum's quarter (iy <= Ny/2, iz <= Nz/2), written
+// to its mirrored points as well: H depends on ky, kz only through their squares,
+// and the mirrored frequencies are exact negations, so every copy is the value the
+// point would compute itself (a quarter of the float64 sincos / exp work).
 __global__ void k_green_half(GridParams gp, double *__restrict__ h64, float *__restrict__ h32) {
-    const int Nxh = gp.N[0] / 2 + 1;
-    const int64_t Gc = (int64_t)Nxh * gp.N[1] * gp.N[2];
+    const HalfQuarter q(gp.N);
+    const int64_t Gq = q.size();
     const double invG = 1.0 / (double)gp.G;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc; t += (int64_t)gridDim.x * blockDim.x) {
-        const int ix = (int)(t % Nxh);
-        const int iy = (int)((t / Nxh) % gp.N[1]);
-        const int iz = (int)(t / ((int64_t)Nxh * gp.N[1]));
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gq; t += (int64_t)gridDim.x * blockDim.x) {
+        int ix, iy, iz;
+        q.point(t, &ix, &iy, &iz);
         const double kx = fft_freq(ix, gp.N[0]) * gp.kfac[0];
         const double ky = fft_freq(iy, gp.N[1]) * gp.kfac[1];
         const double kz = fft_freq(iz, gp.N[2]) * gp.kfac[2];
         const double H = green_coef(kx, ky, kz, gp) * invG;
-        h64[t] = H;
-        if (h32) h32[t] = (float)H;
+        mirror_points(q, ix, iy, iz, [&](int64_t i, int, int) {
+            h64[i] = H;
+            if (h32) h32[i] = (float)H;
+        });
     }
 }
 
@@ -422,8 +427,7 @@ int grid_geometry(const double *x, int64_t n, const GridParams &gp, int32_t *sta
 }
 
 int green_half(const GridParams &gp, double *h64, float *h32, cudaStream_t s) {
-    const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
-    k_green_half<<<grid_for(Gc, 256), 256, 0, s>>>(gp, h64, h32);
+    k_green_half<<<grid_for(HalfQuarter(gp.N).size(), 256), 256, 0, s>>>(gp, h64, h32);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }

@@ -121,6 +121,19 @@ struct InnerGrid {
     bool hs32_ready = false;
 };
 
+// The Arnoldi steps of one GMRES configuration (precision, batch width, restart,
+// Gram-Schmidt passes) of a system as an executable CUDA graph, with the
+// persistent GMRES workspace whose addresses its kernels hold.
+struct ArnoldiGraph {
+    int precision = 0, nrhs = 0, restart = 0;
+    bool reorth = false;
+    char *ws = nullptr;
+    size_t ws_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    long long body_launches = 0;   // this library's kernels per step (one execution of the loop body)
+    bool failed = false;           // capture not possible here: the steps stay host-driven
+};
+
 struct mps_system {
     cudaStream_t stream = nullptr;   // creation stream: stream-ordered allocations and frees
     int64_t n = 0;
@@ -211,7 +224,20 @@ struct mps_system {
     // this system's stream has waited for the shared lazily built Green's buffers (hs32, tm6)
     bool hs32_ready = false, tm6_ready = false;
     InnerGrid *inner = nullptr;      // coarser inner discretisation of the gradient-form operator, or null
+    // Arnoldi-step graphs (captured on their own stream once every lazily built buffer of the matvec exists:
+    // after the first matvec of that precision and batch width outside a capture)
+    std::vector<ArnoldiGraph> graphs;
+    cudaStream_t cap = nullptr;
+    cudaEvent_t ev_graph = nullptr;  // recorded after each graph launch (destroying the graphs waits on it)
+    std::vector<std::pair<int, int>> mv_seen;   // (precision, batch width) of the matvecs run so far
+    int32_t *host_step = nullptr;    // pinned: the step counter read back after a graph launch
 };
+
+static bool matvec_seen(const mps_system *s, int precision, int nrhs) {
+    for (const auto &p : s->mv_seen)
+        if (p.first == precision && p.second == nrhs) return true;
+    return false;
+}
 
 static void free_system(mps_system *s) {
     if (!s) return;
@@ -238,6 +264,15 @@ static void free_system(mps_system *s) {
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->ev_res) cudaEventDestroy(s->ev_res);
     if (s->ev_diag) cudaEventDestroy(s->ev_diag);
+    if (s->ev_graph) {
+        cudaEventSynchronize(s->ev_graph);
+        cudaEventDestroy(s->ev_graph);
+    }
+    for (auto &g : s->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.ws) cudaFreeAsync(g.ws, s->stream);
+    }
+    if (s->cap) cudaStreamDestroy(s->cap);
     tile_bins_free(s->tb64, s->stream);
     tile_bins_free(s->tb32, s->stream);
     tile_bins_free(s->tbg, s->stream);
@@ -1057,7 +1092,10 @@ static int matvec_cplx(mps_system *s, const double *m6, double *out6, int nc, in
 }
 
 static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st) {
-    return s->cplx ? matvec_cplx(s, m, out, nrhs, precision, st) : matvec_real(s, m, out, nrhs, precision, st);
+    const int rc =
+        s->cplx ? matvec_cplx(s, m, out, nrhs, precision, st) : matvec_real(s, m, out, nrhs, precision, st);
+    if (rc == MPS_OK && !matvec_seen(s, precision, nrhs)) s->mv_seen.push_back({precision, nrhs});
+    return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -1072,14 +1110,17 @@ constexpr int kMaxCols = 64;
 // partial[r][blk][c] = sum over the block's rows of V_r[c][i] * w_r[i]; the last
 // block of each system to finish (ticket counter, threadfence pattern) sums the
 // partials in block order and writes out[r][c]: one launch, fixed summation order.
+// With jd non-null the column count is ncols + *jd (the Arnoldi step held on the
+// device by a captured graph).
 __global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restrict__ V, int64_t ldv, int64_t vstride,
                                                           int ncols, const double *__restrict__ w, int64_t wstride,
                                                           int64_t n3, double *__restrict__ partial, int nblk,
                                                           unsigned *__restrict__ tickets, double *__restrict__ out,
-                                                          int64_t ostride) {
+                                                          int64_t ostride, const int32_t *__restrict__ jd) {
     __shared__ double red[kDotThreads / 32][kMaxCols];
     __shared__ bool last;
     const int r = blockIdx.y;
+    if (jd) ncols += *jd;   // graph form: the column count follows the device step counter
     const double *Vr = V + r * vstride;
     const double *wr = w + r * wstride;
     const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
@@ -1124,9 +1165,10 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restri
 // w_r[i] -= sum_c V_r[c][i] * h_r[c]
 __global__ void k_sub_basis(const double *__restrict__ V, int64_t ldv, int64_t vstride, int ncols,
                             const double *__restrict__ h, int64_t hstride, double *__restrict__ w, int64_t wstride,
-                            int64_t n3) {
+                            int64_t n3, const int32_t *__restrict__ jd = nullptr) {
     __shared__ double hs[kMaxCols];
     const int r = blockIdx.y;
+    if (jd) ncols += *jd;
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) hs[c] = h[(int64_t)r * hstride + c];
     __syncthreads();
     const double *Vr = V + r * vstride;
@@ -1229,10 +1271,12 @@ __global__ void k_cycle_start(GmresState st, int restart, int nrhs) {
 }
 
 // Arnoldi column j: H[:,j] = h1 + h2, H[j+1,j] = ||w||, then Givens rotations.
-__global__ void k_arnoldi_givens(GmresState st, int restart, int j, int nrhs, const int32_t *__restrict__ frozen) {
+__global__ void k_arnoldi_givens(GmresState st, int restart, int j, int nrhs, const int32_t *__restrict__ frozen,
+                                 const int32_t *__restrict__ jd = nullptr) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrhs) return;
     if (frozen[r]) return;
+    if (jd) j = *jd;
     const int ld = restart + 1;
     double *Hc = st.H + (int64_t)r * ld * restart + (int64_t)j * ld;
     for (int i = 0; i <= j; ++i) Hc[i] = st.h1[r * kMaxCols + i] + st.h2[r * kMaxCols + i];
@@ -1319,11 +1363,13 @@ static char *carve_ws(char *&p, size_t bytes) {
 // holds nrhs * nblk * kMaxCols partials followed by nrhs zeroed tickets
 // (multidot_bytes / multidot_init).
 static int multidot(const double *V, int64_t ldv, int64_t vstride, int ncols, const double *w, int64_t wstride,
-                    int64_t n3, int nrhs, double *partial, double *out, int64_t ostride, cudaStream_t s) {
+                    int64_t n3, int nrhs, double *partial, double *out, int64_t ostride, cudaStream_t s,
+                    const int32_t *jd = nullptr) {
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     unsigned *tickets = (unsigned *)(partial + (size_t)nrhs * nblk * kMaxCols);
     dim3 g(nblk, nrhs);
-    k_multidot<<<g, kDotThreads, 0, s>>>(V, ldv, vstride, ncols, w, wstride, n3, partial, nblk, tickets, out, ostride);
+    k_multidot<<<g, kDotThreads, 0, s>>>(V, ldv, vstride, ncols, w, wstride, n3, partial, nblk, tickets, out, ostride,
+                                         jd);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
@@ -1336,6 +1382,204 @@ static size_t multidot_bytes(int64_t n3, int nrhs) {
 static int multidot_init(double *partial, int64_t n3, int nrhs, cudaStream_t s) {
     const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     MPS_CUDA_TRY(cudaMemsetAsync(partial + (size_t)nrhs * nblk * kMaxCols, 0, sizeof(unsigned) * (size_t)nrhs, s));
+    return MPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Arnoldi steps as one CUDA graph launch.  A while-conditional node repeats the
+// step body -- matvec of vin, Gram-Schmidt against V[0..j], Givens update, the
+// next basis vector (also copied to vin), loop control -- with the step index j
+// held on the device (jd).  The loop control freezes the systems whose residual
+// estimate reached the tolerance and ends the loop when all are frozen or j
+// reaches restart: j grows by one per execution, so the loop ends after at most
+// restart - j0 steps.  The host reads the estimates once per graph launch.
+// ---------------------------------------------------------------------------
+
+// V[j+1]_r = w_r / nrm_r (j = *jd; zero norm -> zero vector), copied to vin as well.
+__global__ void k_next_basis(const double *__restrict__ w, double *__restrict__ V, int64_t ldv,
+                             const int32_t *__restrict__ jd, const double *__restrict__ nrm, double *__restrict__ vin,
+                             int64_t n3) {
+    const int r = blockIdx.y;
+    const double v = nrm[r];
+    const double f = v != 0.0 ? 1.0 / v : 0.0;
+    double *dst = V + (int64_t)(*jd + 1) * ldv + (int64_t)r * n3;
+    double *d2 = vin + (int64_t)r * n3;
+    const double *src = w + (int64_t)r * n3;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = src[i] * f;
+        dst[i] = x;
+        d2[i] = x;
+    }
+}
+
+// End of a step: freeze the systems that reached the tolerance, advance j, and
+// repeat the body while some system is active and j < restart.
+__global__ void k_loop_ctrl(const double *__restrict__ res, int32_t *__restrict__ frozen,
+                            const double *__restrict__ tol, int nrhs, int32_t *__restrict__ jd, int restart,
+                            cudaGraphConditionalHandle h) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double t = *tol;
+    bool active = false;
+    for (int r = 0; r < nrhs; ++r) {
+        if (!frozen[r] && res[r] <= t) frozen[r] = 1;
+        active = active || !frozen[r];
+    }
+    const int j = *jd + 1;
+    *jd = j;
+    cudaGraphSetConditional(h, (active && j < restart) ? 1u : 0u);
+}
+
+__global__ void k_graph_enter(int32_t *__restrict__ jd, int j0, double *__restrict__ tol_d, double tol) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *jd = j0;
+        *tol_d = tol;
+    }
+}
+
+// Workspace of gmres_core (the graph form adds vin, jd and the device tolerance).
+struct GmresWs {
+    double *V, *w, *vin, *partial, *u, *tol_d;
+    int32_t *frozen, *jd;
+    GmresState S;
+};
+
+static size_t gmres_ws_bytes(int64_t n3, int nrhs, int restart) {
+    const int ld = restart + 1;
+    const int64_t ldv = (int64_t)nrhs * n3;
+    size_t bytes = 0;
+    bytes += 256 + sizeof(double) * (size_t)ld * ldv;                 // V
+    bytes += 2 * (256 + sizeof(double) * (size_t)ldv);                // w vin
+    bytes += 256 + sizeof(double) * (size_t)nrhs * ld * restart;      // H
+    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * restart);     // cs sn
+    bytes += 256 + sizeof(double) * (size_t)nrhs * ld;                // g
+    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * kMaxCols);    // h1 h2
+    bytes += 4 * (256 + sizeof(double) * (size_t)nrhs);               // nrm2 beta bnorm res
+    bytes += 3 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount kfull frozen
+    bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
+    bytes += 256 + multidot_bytes(n3, nrhs);                          // partial + tickets
+    bytes += 256 + sizeof(double) * (size_t)nrhs * (kMaxCols + 1);    // u
+    bytes += 2 * (256 + sizeof(double));                              // jd tol_d
+    return bytes;
+}
+
+static GmresWs gmres_ws_carve(char *base, int64_t n3, int nrhs, int restart) {
+    const int ld = restart + 1;
+    const int64_t ldv = (int64_t)nrhs * n3;
+    char *p = base;
+    GmresWs g;
+    g.V = (double *)carve_ws(p, sizeof(double) * (size_t)ld * ldv);
+    g.w = (double *)carve_ws(p, sizeof(double) * (size_t)ldv);
+    g.vin = (double *)carve_ws(p, sizeof(double) * (size_t)ldv);
+    g.S.H = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld * restart);
+    g.S.cs = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    g.S.sn = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    g.S.g = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld);
+    g.S.h1 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
+    g.S.h2 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
+    g.S.nrm2 = (double *)carve_ws(p, sizeof(double) * nrhs);
+    g.S.beta = (double *)carve_ws(p, sizeof(double) * nrhs);
+    g.S.bnorm = (double *)carve_ws(p, sizeof(double) * nrhs);
+    g.S.res = (double *)carve_ws(p, sizeof(double) * nrhs);
+    g.S.kcount = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    g.S.kfull = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    g.frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
+    g.S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
+    g.partial = (double *)carve_ws(p, multidot_bytes(n3, nrhs));
+    g.u = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * (kMaxCols + 1));
+    g.jd = (int32_t *)carve_ws(p, sizeof(double));
+    g.tol_d = (double *)carve_ws(p, sizeof(double));
+    return g;
+}
+
+// Graph form on unless MPS_GMRES_GRAPH=0 (host-driven steps, kept for A/B timing); never while stage
+// profiling records events inside the matvecs.
+static bool graphs_enabled(const mps_system *s) {
+    if (s->profile) return false;
+    const char *v = getenv("MPS_GMRES_GRAPH");
+    return !(v && v[0] == '0');
+}
+
+static int matvec_any(mps_system *s, const double *m, double *out, int nrhs, int precision, cudaStream_t st);
+
+// Captures the step body for g's configuration on the system's capture stream
+// and instantiates it.  A capture the runtime refuses (or any error inside it)
+// marks g failed and returns MPS_OK: the caller keeps the host-driven steps.
+static int arnoldi_graph_build(mps_system *s, ArnoldiGraph &g, const GmresWs &W, int64_t n3) {
+    const int nrhs = g.nrhs, restart = g.restart;
+    const int64_t ldv = (int64_t)nrhs * n3;
+    if (!s->cap) MPS_CUDA_TRY(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    MPS_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};   // the rest zero
+    cudaGraphNode_t node;
+    cudaError_t ce = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    if (ce == cudaSuccess) {
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    }
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(graph);
+        g.failed = true;
+        return MPS_OK;
+    }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs = s->cap;
+    const dim3 vgrid(grid_for(n3, 256, 152 * 8), nrhs);
+    capture_count_begin();
+    ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    int e = ce == cudaSuccess ? MPS_OK : MPS_CUDA_ERR;
+    if (e == MPS_OK) {
+        auto launched = [&]() { return cudaGetLastError() == cudaSuccess ? MPS_OK : MPS_CUDA_ERR; };
+        e = matvec_any(s, W.vin, W.w, nrhs, g.precision, cs);
+        if (e == MPS_OK) e = multidot(W.V, ldv, n3, 1, W.w, n3, n3, nrhs, W.partial, W.S.h1, kMaxCols, cs, W.jd);
+        if (e == MPS_OK) {
+            k_sub_basis<<<vgrid, 256, 0, cs>>>(W.V, ldv, n3, 1, W.S.h1, kMaxCols, W.w, n3, n3, W.jd);
+            count_launch();
+            e = launched();
+        }
+        if (e == MPS_OK && g.reorth) {
+            e = multidot(W.V, ldv, n3, 1, W.w, n3, n3, nrhs, W.partial, W.S.h2, kMaxCols, cs, W.jd);
+            if (e == MPS_OK) {
+                k_sub_basis<<<vgrid, 256, 0, cs>>>(W.V, ldv, n3, 1, W.S.h2, kMaxCols, W.w, n3, n3, W.jd);
+                count_launch();
+                e = launched();
+            }
+        }
+        if (e == MPS_OK) e = multidot(W.w, n3, n3, 1, W.w, n3, n3, nrhs, W.partial, W.S.nrm2, 1, cs);
+        if (e == MPS_OK) {
+            k_arnoldi_givens<<<(nrhs + 31) / 32, 32, 0, cs>>>(W.S, restart, 0, nrhs, W.frozen, W.jd);
+            count_launch();
+            e = launched();
+        }
+        if (e == MPS_OK) {
+            k_next_basis<<<vgrid, 256, 0, cs>>>(W.w, W.V, ldv, W.jd, W.S.nrm2, W.vin, n3);
+            count_launch();
+            e = launched();
+        }
+        if (e == MPS_OK) {
+            k_loop_ctrl<<<1, 32, 0, cs>>>(W.S.res, W.frozen, W.tol_d, nrhs, W.jd, restart, h);
+            count_launch();
+            e = launched();
+        }
+        cudaGraph_t out = nullptr;
+        ce = cudaStreamEndCapture(cs, &out);
+        if (ce != cudaSuccess) e = MPS_CUDA_ERR;
+    }
+    const long long per_step = capture_count_end();
+    cudaGraphExec_t exec = nullptr;
+    if (e == MPS_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) e = MPS_CUDA_ERR;
+    cudaGraphDestroy(graph);
+    if (e != MPS_OK) {
+        cudaGetLastError();   // a refused capture leaves no sticky error; clear the recorded one
+        g.failed = true;
+        return MPS_OK;
+    }
+    g.exec = exec;
+    g.body_launches = per_step;
     return MPS_OK;
 }
 
@@ -1357,50 +1601,46 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
                       int precision, int *conv, double *relres_out, int *cycles_out, int *mv_count,
                       cudaStream_t st, GmresFlags fl = GmresFlags()) {
     const int64_t n3 = (int64_t)s->ndof * s->n;
-    const int ld = restart + 1;
-    const int nblk = (int)((n3 + kDotChunk - 1) / kDotChunk);
     const int64_t ldv = (int64_t)nrhs * n3;
-    size_t bytes = 0;
-    bytes += 256 + sizeof(double) * (size_t)ld * ldv;                 // V
-    bytes += 256 + sizeof(double) * (size_t)ldv;                      // w
-    bytes += 256 + sizeof(double) * (size_t)nrhs * ld * restart;      // H
-    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * restart);     // cs sn
-    bytes += 256 + sizeof(double) * (size_t)nrhs * ld;                // g
-    bytes += 2 * (256 + sizeof(double) * (size_t)nrhs * kMaxCols);    // h1 h2
-    bytes += 4 * (256 + sizeof(double) * (size_t)nrhs);               // nrm2 beta bnorm res
-    bytes += 3 * (256 + sizeof(int32_t) * (size_t)nrhs);              // kcount kfull frozen
-    bytes += 256 + sizeof(double) * (size_t)nrhs * restart;           // y
-    bytes += 256 + multidot_bytes(n3, nrhs);                          // partial + tickets
-    bytes += 256 + sizeof(double) * (size_t)nrhs * (kMaxCols + 1);    // u
+    // The graph form keeps one persistent workspace per configuration (its kernels hold the addresses);
+    // otherwise the workspace lives for this call.
+    ArnoldiGraph *ag = nullptr;
+    if (graphs_enabled(s)) {
+        for (auto &g : s->graphs)
+            if (g.precision == precision && g.nrhs == nrhs && g.restart == restart && g.reorth == fl.reorth) ag = &g;
+        if (!ag) {
+            ArnoldiGraph g;
+            g.precision = precision;
+            g.nrhs = nrhs;
+            g.restart = restart;
+            g.reorth = fl.reorth;
+            g.ws_bytes = gmres_ws_bytes(n3, nrhs, restart);
+            MPS_CUDA_TRY(cudaMallocAsync((void **)&g.ws, g.ws_bytes, st));
+            s->graphs.push_back(g);
+            ag = &s->graphs.back();
+        }
+        if (ag->failed) ag = nullptr;
+    }
     char *base = nullptr;
-    MPS_CUDA_TRY(cudaMallocAsync((void **)&base, bytes, st));
-    char *p = base;
-    double *V = (double *)carve_ws(p, sizeof(double) * (size_t)ld * ldv);
-    double *w = (double *)carve_ws(p, sizeof(double) * (size_t)ldv);
-    GmresState S;
-    S.H = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld * restart);
-    S.cs = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
-    S.sn = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
-    S.g = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * ld);
-    S.h1 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
-    S.h2 = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * kMaxCols);
-    S.nrm2 = (double *)carve_ws(p, sizeof(double) * nrhs);
-    S.beta = (double *)carve_ws(p, sizeof(double) * nrhs);
-    S.bnorm = (double *)carve_ws(p, sizeof(double) * nrhs);
-    S.res = (double *)carve_ws(p, sizeof(double) * nrhs);
-    S.kcount = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
-    S.kfull = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
-    int32_t *frozen = (int32_t *)carve_ws(p, sizeof(int32_t) * nrhs);
-    S.y = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * restart);
-    double *partial = (double *)carve_ws(p, multidot_bytes(n3, nrhs));
-    double *u = (double *)carve_ws(p, sizeof(double) * (size_t)nrhs * (kMaxCols + 1));
+    if (ag) {
+        base = ag->ws;
+    } else {
+        MPS_CUDA_TRY(cudaMallocAsync((void **)&base, gmres_ws_bytes(n3, nrhs, restart), st));
+    }
+    const GmresWs W = gmres_ws_carve(ag ? ag->ws : base, n3, nrhs, restart);
+    double *V = W.V;
+    double *w = W.w;
+    GmresState S = W.S;
+    int32_t *frozen = W.frozen;
+    double *partial = W.partial;
+    double *u = W.u;
     {
         int e = multidot_init(partial, n3, nrhs, st);
         if (e == MPS_OK && !fl.reorth &&
             cudaMemsetAsync(S.h2, 0, sizeof(double) * (size_t)nrhs * kMaxCols, st) != cudaSuccess)
             e = MPS_CUDA_ERR;
         if (e) {
-            cudaFreeAsync(base, st);
+            if (!ag) cudaFreeAsync(base, st);
             return e;
         }
     }
@@ -1411,8 +1651,11 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
     int rc = MPS_OK;
     const dim3 vgrid(grid_for(n3, 256, 152 * 8), nrhs);
     int cyc = 0;
+    auto release = [&]() {
+        if (!ag) cudaFreeAsync(base, st);
+    };
     auto fail = [&](int code) {
-        cudaFreeAsync(base, st);
+        release();
         return code;
     };
 #define GM_TRY(expr)                       \
@@ -1480,7 +1723,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         // system: the estimate after step j, extrapolated from the last two, is above 2 tol for some active
         // system.  The wait then overlaps that matvec instead of leaving the GPU idle; a wrong guess costs one
         // discarded matvec (w is rewritten before it is read again).
-        const bool may_speculate = precision == MPS_FP32 || precision == MPS_FP32_GRAD;
+        const bool may_speculate = !ag && (precision == MPS_FP32 || precision == MPS_FP32_GRAD);
         std::vector<double> hlast(hres, hres + nrhs), hprev(nrhs, -1.0);
         auto likely_continues = [&]() {
             for (int r = 0; r < nrhs; ++r) {
@@ -1492,6 +1735,28 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         };
         bool queued = false;   // step j's matvec already queued into w
         for (int j = 0; j < restart; ++j) {
+            // graph form: the remaining steps of the cycle in one launch, once a matvec of this precision and
+            // batch width has run outside a capture (every lazily built buffer and FFT plan exists)
+            if (ag && !ag->failed && !queued && (ag->exec || matvec_seen(s, precision, nrhs))) {
+                if (!ag->exec) GM_TRY(arnoldi_graph_build(s, *ag, W, n3));
+                if (ag->exec) {
+                    GM_CUDA(cudaMemcpyAsync(W.vin, V + (int64_t)j * ldv, sizeof(double) * ldv,
+                                            cudaMemcpyDeviceToDevice, st));
+                    k_graph_enter<<<1, 32, 0, st>>>(W.jd, j, W.tol_d, tol);
+                    GM_LAUNCH();
+                    GM_CUDA(cudaGraphLaunch(ag->exec, st));
+                    if (!s->ev_graph) GM_CUDA(cudaEventCreateWithFlags(&s->ev_graph, cudaEventDisableTiming));
+                    GM_CUDA(cudaEventRecord(s->ev_graph, st));
+                    GM_CUDA(cudaMemcpyAsync(hres, S.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+                    GM_CUDA(cudaMemcpyAsync(hfrozen, frozen, sizeof(int32_t) * nrhs, cudaMemcpyDeviceToHost, st));
+                    GM_CUDA(cudaMemcpyAsync(s->host_step, W.jd, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+                    GM_CUDA(cudaStreamSynchronize(st));
+                    const int steps = *s->host_step - j;
+                    *mv_count += steps;
+                    add_launches(ag->body_launches * steps);
+                    break;
+                }
+            }
             if (!queued) {
                 GM_TRY(matvec_any(s, V + (int64_t)j * ldv, w, nrhs, precision, st));
                 ++*mv_count;
@@ -1573,7 +1838,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
             if (!conv[r]) rc = MPS_NOT_CONVERGED;
         }
         *cycles_out = cyc;
-        cudaFreeAsync(base, st);
+        release();
         return rc;
     }
     // final true residual
@@ -1594,7 +1859,7 @@ static int gmres_core(mps_system *s, const double *b, double *x, int nrhs, doubl
         }
     }
     *cycles_out = cyc;
-    cudaFreeAsync(base, st);
+    release();
 #undef GM_TRY
 #undef GM_CUDA
 #undef GM_LAUNCH
@@ -1884,11 +2149,12 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * s->max_rhs, st));
     {
         const size_t ints = ((size_t)2 * s->max_rhs + 1) & ~(size_t)1;   // even: the doubles stay 8-byte aligned
-        if (cudaMallocHost((void **)&s->diag_idx_host, sizeof(int32_t) * ints + sizeof(double) * 6 * s->max_rhs) !=
-            cudaSuccess)
+        if (cudaMallocHost((void **)&s->diag_idx_host,
+                           sizeof(int32_t) * ints + sizeof(double) * (6 * s->max_rhs + 1)) != cudaSuccess)
             CR_TRY(MPS_NO_MEMORY);
         s->host_frozen = s->diag_idx_host + s->max_rhs;
         s->host_scr = reinterpret_cast<double *>(s->diag_idx_host + ints);
+        s->host_step = reinterpret_cast<int32_t *>(s->host_scr + 6 * s->max_rhs);
     }
     if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     // cell list + pair CSR
@@ -2455,6 +2721,16 @@ extern "C" int mps_field_map_sizes(const double *x_e, int64_t n_e, const double 
 extern "C" int mps_kspace_cache_clear(void) {
     std::lock_guard<std::mutex> lk(g_green_mu);
     g_green.clear();   // systems that hold coefficients keep them until they are destroyed
+    return MPS_OK;
+}
+
+extern "C" int mps_system_graphs(const mps_system *sys, int32_t *built, int32_t *failed) {
+    if (!sys || !built || !failed) return MPS_BAD_ARG;
+    *built = *failed = 0;
+    for (const auto &g : sys->graphs) {
+        if (g.exec) ++*built;
+        if (g.failed) ++*failed;
+    }
     return MPS_OK;
 }
 

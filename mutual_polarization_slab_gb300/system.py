@@ -291,6 +291,15 @@ class SpectralEwaldSystem:
         return {"fp64": {"tile": [16, 16, int(tz[0])], "ms_depth4": ms[0], "ms_depth8": ms[1]},
                 "fp32": {"tile": [16, 16, int(tz[1])], "ms_depth4": ms[2], "ms_depth8": ms[3]}}
 
+    def graphs(self):
+        """GMRES step graphs of this system: (instantiated, refused by the runtime).
+        The solves run each cycle's Arnoldi steps as one CUDA graph launch once a
+        matvec of that precision and batch width has run; MPS_GMRES_GRAPH=0 in the
+        environment keeps the host-driven steps."""
+        built, failed = C.c_int32(0), C.c_int32(0)
+        L.check(self._lib.mps_system_graphs(self._h, C.byref(built), C.byref(failed)))
+        return int(built.value), int(failed.value)
+
     # -- operator ---------------------------------------------------------
     def _diag_arg(self, nrhs, diag_index):
         if diag_index is None:
