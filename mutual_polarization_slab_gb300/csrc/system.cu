@@ -233,6 +233,44 @@ struct mps_system {
     int32_t *host_step = nullptr;    // pinned: the step counter read back after a graph launch
 };
 
+// Pinned host blocks of destroyed systems, kept for the next system (cudaMallocHost and cudaFreeHost cost a
+// few hundred microseconds each; a configuration loop would pay them for every system).  Pinned memory is not
+// tied to a device.
+static std::mutex g_pinned_mu;
+static std::multimap<size_t, void *> g_pinned_free;
+
+static void *pinned_take(size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        auto it = g_pinned_free.lower_bound(bytes);
+        if (it != g_pinned_free.end() && it->first <= 2 * bytes + 4096) {
+            void *p = it->second;
+            g_pinned_free.erase(it);
+            return p;
+        }
+    }
+    void *p = nullptr;
+    // the block's size is kept in front of it so it can go back to the free list
+    if (cudaMallocHost(&p, bytes + 64) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    *reinterpret_cast<size_t *>(p) = bytes;
+    return static_cast<char *>(p) + 64;
+}
+
+static void pinned_give(void *q) {
+    if (!q) return;
+    void *p = static_cast<char *>(q) - 64;
+    const size_t bytes = *reinterpret_cast<size_t *>(p);
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    if (g_pinned_free.size() >= 64) {   // bound what is kept
+        cudaFreeHost(p);
+        return;
+    }
+    g_pinned_free.emplace(bytes, q);
+}
+
 static bool matvec_seen(const mps_system *s, int precision, int nrhs) {
     for (const auto &p : s->mv_seen)
         if (p.first == precision && p.second == nrhs) return true;
@@ -257,7 +295,7 @@ static void free_system(mps_system *s) {
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s->stream);
     if (s->ev_diag) cudaEventSynchronize(s->ev_diag);   // the last index upload reads the pinned block
-    if (s->diag_idx_host) cudaFreeHost(s->diag_idx_host);
+    if (s->diag_idx_host) pinned_give(s->diag_idx_host);
     if (s->rs_buf) cudaFreeAsync(s->rs_buf, s->stream);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -2149,9 +2187,9 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * s->max_rhs, st));
     {
         const size_t ints = ((size_t)2 * s->max_rhs + 1) & ~(size_t)1;   // even: the doubles stay 8-byte aligned
-        if (cudaMallocHost((void **)&s->diag_idx_host,
-                           sizeof(int32_t) * ints + sizeof(double) * (6 * s->max_rhs + 1)) != cudaSuccess)
-            CR_TRY(MPS_NO_MEMORY);
+        const size_t pinned = sizeof(int32_t) * ints + sizeof(double) * (6 * s->max_rhs + 1);
+        s->diag_idx_host = static_cast<int32_t *>(pinned_take(pinned));
+        if (!s->diag_idx_host) CR_TRY(MPS_NO_MEMORY);
         s->host_frozen = s->diag_idx_host + s->max_rhs;
         s->host_scr = reinterpret_cast<double *>(s->diag_idx_host + ints);
         s->host_step = reinterpret_cast<int32_t *>(s->host_scr + 6 * s->max_rhs);

@@ -15,6 +15,9 @@
 // (EW/ewald.py:370-467) up to summation order.
 #include "tiles.cuh"
 
+#include <climits>
+#include <algorithm>
+
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -85,34 +88,80 @@ __global__ void k_tile_fill(const int32_t *__restrict__ start, int64_t n, TileGe
     }
 }
 
-// One warp per tile: order the tile's particles by id and record, for each
-// particle, where its entry for this tile landed.
-__global__ void k_tile_rank(const int32_t *__restrict__ unsorted, const int64_t *__restrict__ tstart, int64_t ntiles,
-                            const int32_t *__restrict__ start, TileGeom tg, const int64_t *__restrict__ pstart,
-                            int32_t *__restrict__ entries, int32_t *__restrict__ pentry) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t t = warp; t < ntiles; t += nw) {
+// One block per tile: order the tile's particles by id (bitonic sort in shared
+// memory for up to kSortCap entries, else a rank count over the whole list) and
+// record, for each particle, where its entry for this tile landed.  The atomics
+// of k_tile_fill leave the unsorted order arbitrary; the sorted order makes every
+// tiled kernel's sums deterministic.
+constexpr int kSortCap = 4096;
+constexpr int kSortThreads = 256;
+
+__device__ __forceinline__ void tile_entry_out(int32_t v, int64_t pos, int tx, int ty, int tzi,
+                                               const int32_t *__restrict__ start, const TileGeom &tg,
+                                               const int64_t *__restrict__ pstart, int32_t *__restrict__ entries,
+                                               int32_t *__restrict__ pentry) {
+    entries[pos] = v;
+    int L[3][kMaxTileList];
+    int c[3];
+    for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * (int64_t)v + d], tg.P, tg.N[d], tg.T[d], L[d]);
+    int ix = 0, iy = 0, iz = 0;
+    while (ix < c[0] && L[0][ix] != tx) ++ix;
+    while (iy < c[1] && L[1][iy] != ty) ++iy;
+    while (iz < c[2] && L[2][iz] != tzi) ++iz;
+    pentry[pstart[v] + ((int64_t)iz * c[1] + iy) * c[0] + ix] = (int32_t)pos;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_tile_sort(const int32_t *__restrict__ unsorted,
+                                                            const int64_t *__restrict__ tstart, int64_t ntiles,
+                                                            const int32_t *__restrict__ start, TileGeom tg,
+                                                            const int64_t *__restrict__ pstart,
+                                                            int32_t *__restrict__ entries,
+                                                            int32_t *__restrict__ pentry) {
+    __shared__ int32_t key[kSortCap];
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t s0 = tstart[t];
         const int len = (int)(tstart[t + 1] - s0);
+        if (len == 0) continue;
         const int tx = (int)(t % tg.nt[0]), ty = (int)((t / tg.nt[0]) % tg.nt[1]),
                   tzi = (int)(t / ((int64_t)tg.nt[0] * tg.nt[1]));
-        for (int e = lane; e < len; e += 32) {
-            const int32_t v = unsorted[s0 + e];
-            int rank = 0;
-            for (int j = 0; j < len; ++j) rank += (unsorted[s0 + j] < v);
-            entries[s0 + rank] = v;
-            int L[3][kMaxTileList];
-            int c[3];
-            for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * (int64_t)v + d], tg.P, tg.N[d], tg.T[d], L[d]);
-            int ix = 0, iy = 0, iz = 0;
-            while (ix < c[0] && L[0][ix] != tx) ++ix;
-            while (iy < c[1] && L[1][iy] != ty) ++iy;
-            while (iz < c[2] && L[2][iz] != tzi) ++iz;
-            pentry[pstart[v] + ((int64_t)iz * c[1] + iy) * c[0] + ix] = (int32_t)(s0 + rank);
+        if (len <= kSortCap) {
+            int L = 1;
+            while (L < len) L <<= 1;
+            __syncthreads();   // the previous tile's reads of key are done
+            for (int i = threadIdx.x; i < L; i += blockDim.x) key[i] = i < len ? unsorted[s0 + i] : INT_MAX;
+            __syncthreads();
+            for (int k = 2; k <= L; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const int32_t a = key[i], b = key[ixj];
+                            if ((a > b) == ((i & k) == 0)) {
+                                key[i] = b;
+                                key[ixj] = a;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (int e = threadIdx.x; e < len; e += blockDim.x)
+                tile_entry_out(key[e], s0 + e, tx, ty, tzi, start, tg, pstart, entries, pentry);
+        } else {
+            // ids are distinct within a tile: an entry's rank is the count of smaller ids
+            for (int e = threadIdx.x; e < len; e += blockDim.x) {
+                const int32_t v = unsorted[s0 + e];
+                int rank = 0;
+                for (int j = 0; j < len; ++j) rank += (unsorted[s0 + j] < v);
+                tile_entry_out(v, s0 + rank, tx, ty, tzi, start, tg, pstart, entries, pentry);
+            }
         }
     }
+}
+
+// out[n] = out[n - 1] + in[n - 1]: the total after an exclusive scan of n >= 1 counts.
+template <typename Tin>
+__global__ void k_scan_total(const Tin *__restrict__ in, int64_t *__restrict__ out, int64_t n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = out[n - 1] + (int64_t)in[n - 1];
 }
 
 static char *carve_t(char *&p, size_t bytes) {
@@ -121,17 +170,28 @@ static char *carve_t(char *&p, size_t bytes) {
     return (char *)u;
 }
 
+// Upper bound of the distinct tiles along one axis that P consecutive nodes (mod N) touch: a window of P nodes
+// spans at most (P - 1) / T + 2 tiles of T, one more where it wraps past a partial last tile.
+static int64_t axis_tile_bound(int N, int T, int P) {
+    const int64_t nt = (N + T - 1) / T;
+    return std::min<int64_t>(nt, (P - 1) / T + 2 + (N % T != 0 ? 1 : 0));
+}
+
+// Tile lists without a host round trip: the entry arrays are sized by the per-particle bound (nentries holds that
+// capacity), the offsets and totals stay on the device.
 int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s) {
     tile_bins_free(tb, s);
-    if (!tiles_supported(gp, tz)) return MPS_BAD_ARG;
+    if (!tiles_supported(gp, tz) || n < 1) return MPS_BAD_ARG;
     TileGeom tg;
     tg.P = gp.P;
     tg.T[0] = kTileX;
     tg.T[1] = kTileY;
     tg.T[2] = tz;
+    int64_t per = 1;
     for (int d = 0; d < 3; ++d) {
         tg.N[d] = gp.N[d];
         tg.nt[d] = (gp.N[d] + tg.T[d] - 1) / tg.T[d];
+        per *= axis_tile_bound(gp.N[d], tg.T[d], gp.P);
     }
     tb.tz = tz;
     tb.ntx = tg.nt[0];
@@ -139,63 +199,44 @@ int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int t
     tb.ntz = tg.nt[2];
     tb.ntiles = (int64_t)tg.nt[0] * tg.nt[1] * tg.nt[2];
     const int64_t T = tb.ntiles;
-    // temporaries
-    int32_t *tcount = nullptr, *cursor = nullptr, *unsorted = nullptr;
-    int64_t *pcount = nullptr;
-    void *scan_tmp = nullptr;
-    size_t tmp_bytes = 256 * 5 + (size_t)T * 4 * 2 + (size_t)n * 8 + scan_workspace(std::max(T, n) + 1);
+    const int64_t Emax = n * per;
+    tb.nentries = Emax;
+    // temporaries: tile counts and cursors, per-particle counts, scan scratch, the unsorted lists
+    size_t tmp_bytes = 256 * 5 + (size_t)T * 4 * 2 + (size_t)n * 8 + scan_workspace(std::max(T, n) + 1) +
+                       (size_t)Emax * 4;
     char *tmp = nullptr;
     MPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, tmp_bytes, s));
     char *p = tmp;
-    tcount = (int32_t *)carve_t(p, (size_t)T * 4);
-    cursor = (int32_t *)carve_t(p, (size_t)T * 4);
-    pcount = (int64_t *)carve_t(p, (size_t)n * 8);
-    scan_tmp = carve_t(p, scan_workspace(std::max(T, n) + 1));
+    int32_t *tcount = (int32_t *)carve_t(p, (size_t)T * 4);
+    int32_t *cursor = (int32_t *)carve_t(p, (size_t)T * 4);
+    int64_t *pcount = (int64_t *)carve_t(p, (size_t)n * 8);
+    void *scan_tmp = carve_t(p, scan_workspace(std::max(T, n) + 1));
+    int32_t *unsorted = (int32_t *)carve_t(p, (size_t)Emax * 4);
+    // persistent arrays
+    size_t bytes = 256 * 4 + (size_t)(T + 1) * 8 + (size_t)Emax * 4 + (size_t)(n + 1) * 8 + (size_t)Emax * 4;
+    MPS_CUDA_TRY(cudaMallocAsync(&tb.mem, bytes, s));
+    p = (char *)tb.mem;
+    tb.tile_start = (int64_t *)carve_t(p, (size_t)(T + 1) * 8);
+    tb.entries = (int32_t *)carve_t(p, (size_t)Emax * 4);
+    tb.pstart = (int64_t *)carve_t(p, (size_t)(n + 1) * 8);
+    tb.pentry = (int32_t *)carve_t(p, (size_t)Emax * 4);
     MPS_CUDA_TRY(cudaMemsetAsync(tcount, 0, (size_t)T * 4, s));
     MPS_CUDA_TRY(cudaMemsetAsync(cursor, 0, (size_t)T * 4, s));
     k_tile_count<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tcount, pcount);
     MPS_LAUNCH_CHECK();
-    // sizes: total entries
-    int64_t *tstart_tmp = nullptr, *pstart_tmp = nullptr;
-    MPS_CUDA_TRY(cudaMallocAsync((void **)&tstart_tmp, (size_t)(T + 1) * 8, s));
-    MPS_CUDA_TRY(cudaMallocAsync((void **)&pstart_tmp, (size_t)(n + 1) * 8, s));
-    int r = exclusive_scan_i32_to_i64(tcount, tstart_tmp, T, scan_tmp, s);
+    int r = exclusive_scan_i32_to_i64(tcount, tb.tile_start, T, scan_tmp, s);
     if (r) return r;
-    r = exclusive_scan_i64(pcount, pstart_tmp, n, scan_tmp, s);
+    k_scan_total<int32_t><<<1, 32, 0, s>>>(tcount, tb.tile_start, T);
+    MPS_LAUNCH_CHECK();
+    r = exclusive_scan_i64(pcount, tb.pstart, n, scan_tmp, s);
     if (r) return r;
-    int64_t last_t, last_c, last_p, last_pc;
-    int32_t lc;
-    MPS_CUDA_TRY(cudaMemcpyAsync(&last_t, tstart_tmp + T - 1, 8, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(&lc, tcount + T - 1, 4, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(&last_p, pstart_tmp + n - 1, 8, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(&last_pc, pcount + n - 1, 8, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaStreamSynchronize(s));
-    last_c = lc;
-    const int64_t E = last_t + last_c;
-    tb.nentries = E;
-    (void)last_pc;
-    // persistent arrays
-    size_t bytes = 256 * 5 + (size_t)(T + 1) * 8 + (size_t)E * 4 + (size_t)(n + 1) * 8 + (size_t)E * 4 +
-                   (size_t)E * 4;
-    MPS_CUDA_TRY(cudaMallocAsync(&tb.mem, bytes, s));
-    p = (char *)tb.mem;
-    tb.tile_start = (int64_t *)carve_t(p, (size_t)(T + 1) * 8);
-    tb.entries = (int32_t *)carve_t(p, (size_t)E * 4);
-    tb.pstart = (int64_t *)carve_t(p, (size_t)(n + 1) * 8);
-    tb.pentry = (int32_t *)carve_t(p, (size_t)E * 4);
-    unsorted = (int32_t *)carve_t(p, (size_t)E * 4);
-    MPS_CUDA_TRY(cudaMemcpyAsync(tb.tile_start, tstart_tmp, (size_t)T * 8, cudaMemcpyDeviceToDevice, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(tb.tile_start + T, &E, 8, cudaMemcpyHostToDevice, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(tb.pstart, pstart_tmp, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(tb.pstart + n, &E, 8, cudaMemcpyHostToDevice, s));
+    k_scan_total<int64_t><<<1, 32, 0, s>>>(pcount, tb.pstart, n);
+    MPS_LAUNCH_CHECK();
     k_tile_fill<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tb.tile_start, cursor, unsorted);
     MPS_LAUNCH_CHECK();
-    k_tile_rank<<<grid_for(T * 32, 256), 256, 0, s>>>(unsorted, tb.tile_start, T, start, tg, tb.pstart, tb.entries,
-                                                      tb.pentry);
+    k_tile_sort<<<grid_for(T, 1, 152 * 8), kSortThreads, 0, s>>>(unsorted, tb.tile_start, T, start, tg, tb.pstart,
+                                                                 tb.entries, tb.pentry);
     MPS_LAUNCH_CHECK();
-    MPS_CUDA_TRY(cudaStreamSynchronize(s));  // host scalars above must outlive the copies
-    cudaFreeAsync(tstart_tmp, s);
-    cudaFreeAsync(pstart_tmp, s);
     cudaFreeAsync(tmp, s);
     return MPS_OK;
 }
