@@ -211,6 +211,8 @@ __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, do
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r][0] = acc[r][1] = acc[r][2] = (T)0;
         const int64_t e0 = row_ptr[a], e1 = row_ptr[a + 1];
+        // two entries per lane in flight: the loop waits on its neighbour gathers (same order of the sums)
+#pragma unroll 2
         for (int64_t e = e0 + lane; e < e1; e += G) {
             const int32_t b = pd.nbr[e];
             const T av = pd.A[e], ba = pd.BA[e];

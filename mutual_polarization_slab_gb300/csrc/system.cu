@@ -1169,6 +1169,8 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(const double *__restri
         wv[k] = i < n3 ? wr[i] : 0.0;
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // columns interleaved in fours: the loads of the next columns overlap this column's shuffle reduction
+#pragma unroll 4
     for (int c = 0; c < ncols; ++c) {
         const double *Vc = Vr + (int64_t)c * ldv;
         double acc = 0.0;
