@@ -2122,6 +2122,52 @@ static int acquire_green(const GridParams &gp, const double *box, double xi, int
     return MPS_OK;
 }
 
+// Grid geometry (start nodes, separable weights), Green's coefficients and the inner grid of a dipole or
+// quadrupole system, on stream gs: none of it depends on the pair list, so the caller runs it on the side stream
+// beside the pair-list construction.
+static int setup_grids(mps_system *s, const mps_system_desc *d, cudaStream_t gs) {
+    const int64_t n = d->n;
+#define GS_TRY(expr)                   \
+    do {                               \
+        const int _r = (expr);         \
+        if (_r != MPS_OK) return _r;   \
+    } while (0)
+    GS_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n, gs));
+    GS_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P, gs));
+    GS_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P, gs));
+    GS_TRY(grid_geometry(s->x, n, s->gp, s->start, s->w64, s->w32, gs));
+    GS_TRY(acquire_green(s->gp, d->box, d->xi, s->Gc, s->green, gs));
+    s->h64 = s->green->h64;
+    s->h32 = s->green->h32;
+    // the inner grid of the gradient-form operator, when asked for (dipole operator, tiled kernels)
+    if (d->inner_P > 0) {
+        for (int k = 0; k < 3; ++k)
+            if (d->inner_Ngrid[k] < d->inner_P) GS_TRY(MPS_BAD_ARG);
+        if (d->inner_P > kMaxP) GS_TRY(MPS_BAD_ARG);
+        s->inner = new InnerGrid();
+        InnerGrid &ig = *s->inner;
+        ig.gp = make_grid_params(d->inner_Ngrid, d->box, d->xi, nullptr, d->inner_P);
+        if (!tiles_supported(ig.gp, 8)) GS_TRY(MPS_BAD_ARG);
+        ig.Gc = (int64_t)(ig.gp.N[0] / 2 + 1) * ig.gp.N[1] * ig.gp.N[2];
+        GS_TRY(dalloc(&ig.start, sizeof(int32_t) * 3 * n, gs));
+        GS_TRY(dalloc(&ig.w64, sizeof(double) * 3 * n * ig.gp.P, gs));
+        GS_TRY(dalloc(&ig.w32, sizeof(float) * 3 * n * ig.gp.P, gs));
+        GS_TRY(dalloc(&ig.g32, sizeof(float) * 3 * n * ig.gp.P, gs));
+        GS_TRY(grid_geometry(s->x, n, ig.gp, ig.start, ig.w64, ig.w32, gs));
+        GS_TRY(grad_factors(s->x, n, ig.gp, ig.w64, ig.g32, gs));
+        // depth 16 as for the system's own gradient-form tiles (tuned_depth); MPS_TILE_DEPTH overrides it
+        int tz_in = tiles_supported(ig.gp, 16) ? 16 : 8;
+        if (const char *fd = getenv("MPS_TILE_DEPTH")) {
+            const int dz = atoi(fd);
+            if ((dz == 4 || dz == 8 || dz == 16) && tiles_supported(ig.gp, dz)) tz_in = dz;
+        }
+        GS_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, gs));
+        GS_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, gs));
+    }
+#undef GS_TRY
+    return MPS_OK;
+}
+
 extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps_stream_t stream) {
     if (!d || !out) return MPS_BAD_ARG;
     *out = nullptr;
@@ -2197,6 +2243,16 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         s->host_step = reinterpret_cast<int32_t *>(s->host_scr + 6 * s->max_rhs);
     }
     if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
+    // grids and k-space on the side stream, beside the pair list below (joined before returning)
+    const bool grids_on_side = s->kind != MPS_POLYDISPERSE;
+    if (grids_on_side) {
+        if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventRecord(s->ev_fork, st) != cudaSuccess || cudaStreamWaitEvent(s->side, s->ev_fork, 0) != cudaSuccess)
+            CR_TRY(MPS_CUDA_ERR);
+        CR_TRY(setup_grids(s, d, s->side));
+    }
     // cell list + pair CSR
     compute_ncell(d->box, d->rc, s->ncell);
     const int64_t ncells = s->ncell[0] * s->ncell[1] * s->ncell[2];
@@ -2351,38 +2407,11 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         *out = s;
         return MPS_OK;
     }
-    // grid geometry + Green's coefficients
-    CR_TRY(dalloc(&s->start, sizeof(int32_t) * 3 * n, st));
-    CR_TRY(dalloc(&s->w64, sizeof(double) * 3 * n * d->P, st));
-    CR_TRY(dalloc(&s->w32, sizeof(float) * 3 * n * d->P, st));
-    CR_TRY(grid_geometry(s->x, n, s->gp, s->start, s->w64, s->w32, st));
-    CR_TRY(acquire_green(s->gp, d->box, d->xi, s->Gc, s->green, st));
-    s->h64 = s->green->h64;
-    s->h32 = s->green->h32;
-    // the inner grid of the gradient-form operator, when asked for (dipole operator, tiled kernels)
-    if (d->inner_P > 0) {
-        for (int k = 0; k < 3; ++k)
-            if (d->inner_Ngrid[k] < d->inner_P) CR_TRY(MPS_BAD_ARG);
-        if (d->inner_P > kMaxP) CR_TRY(MPS_BAD_ARG);
-        s->inner = new InnerGrid();
-        InnerGrid &ig = *s->inner;
-        ig.gp = make_grid_params(d->inner_Ngrid, d->box, d->xi, nullptr, d->inner_P);
-        if (!tiles_supported(ig.gp, 8)) CR_TRY(MPS_BAD_ARG);
-        ig.Gc = (int64_t)(ig.gp.N[0] / 2 + 1) * ig.gp.N[1] * ig.gp.N[2];
-        CR_TRY(dalloc(&ig.start, sizeof(int32_t) * 3 * n, st));
-        CR_TRY(dalloc(&ig.w64, sizeof(double) * 3 * n * ig.gp.P, st));
-        CR_TRY(dalloc(&ig.w32, sizeof(float) * 3 * n * ig.gp.P, st));
-        CR_TRY(dalloc(&ig.g32, sizeof(float) * 3 * n * ig.gp.P, st));
-        CR_TRY(grid_geometry(s->x, n, ig.gp, ig.start, ig.w64, ig.w32, st));
-        CR_TRY(grad_factors(s->x, n, ig.gp, ig.w64, ig.g32, st));
-        // depth 16 as for the system's own gradient-form tiles (tuned_depth); MPS_TILE_DEPTH overrides it
-        int tz_in = tiles_supported(ig.gp, 16) ? 16 : 8;
-        if (const char *fd = getenv("MPS_TILE_DEPTH")) {
-            const int dz = atoi(fd);
-            if ((dz == 4 || dz == 8 || dz == 16) && tiles_supported(ig.gp, dz)) tz_in = dz;
-        }
-        CR_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, st));
-        CR_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, st));
+    // the grid and k-space set-up ran on the side stream beside the pair list: join it
+    if (grids_on_side) {
+        if (cudaEventRecord(s->ev_join, s->side) != cudaSuccess ||
+            cudaStreamWaitEvent(st, s->ev_join, 0) != cudaSuccess)
+            CR_TRY(MPS_CUDA_ERR);
     }
 #undef CR_TRY
     *out = s;
