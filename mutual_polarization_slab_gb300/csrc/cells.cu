@@ -804,17 +804,57 @@ __device__ __forceinline__ void store_pair_df(PairData<dfv> &pd, PairData<float>
     pf.rz[w] = rh[2].hi;
 }
 
-// Same traversal and pair order as k_csr_fill.
-__global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ x, const float *__restrict__ xf,
-                                                     const float2 *__restrict__ xdf, PairScreen ps,
-                                                     const int32_t *__restrict__ sorted,
-                                                     const int32_t *__restrict__ lin,
-                                                     const int32_t *__restrict__ counts,
-                                                     const int64_t *__restrict__ starts, int64_t n, int64_t ncx,
-                                                     int64_t ncy, int64_t ncz, const int64_t *__restrict__ off27,
-                                                     DfTab tab, PairData<dfv> pdf, PairData<float> p32,
-                                                     int *__restrict__ err) {
-    const int lane = threadIdx.x & 31;
+// Double-float couplings of one kept pair from its (minimum-image) separation r.
+__device__ __forceinline__ void df_pair_out(const DfTab &tab, PairData<dfv> &pdf, PairData<float> &p32, int64_t wp,
+                                            int32_t b, const dfv r[3], int *__restrict__ err) {
+    const dfv s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const dfv y = df_rsqrt(s2);
+    const dfv d = s2 * y;
+    const dfv rh[3] = {r[0] * y, r[1] * y, r[2] * y};
+    dfv A(0.f, 0.f), B(0.f, 0.f);
+    int64_t i = df_search(tab.rvf, tab.ntab, d.hi, tab.inv_dr);
+    // The float search can land one segment off when d lies within a float rounding of a node;
+    // settle the bracket r_{i-1} < d <= r_i (the reference's searchsorted 'left') in double-float,
+    // so the coupling is interpolated inside its segment instead of extrapolated across the node.
+    if (i > 1 && i < tab.ntab) {
+        const dfv lo = d - df_lo(tab.seg_r[i]);
+        if (lo.hi < 0.f || (lo.hi == 0.f && lo.lo <= 0.f)) --i;
+    }
+    if (i > 0 && i + 1 < tab.ntab) {
+        const dfv hi = d - df_lo(tab.seg_r[i + 1]);
+        if (hi.hi > 0.f || (hi.hi == 0.f && hi.lo > 0.f)) ++i;
+    }
+    if (i <= 0 || i >= tab.ntab) {
+        atomicExch(err, 1);
+    } else {
+        const float4 sr = tab.seg_r[i], sp = tab.seg_perp[i], sq = tab.seg_para[i];
+        const dfv tt = (d - df_lo(sr)) * df_hi(sr);
+        A = df_lo(sp) + tt * df_hi(sp);
+        B = df_lo(sq) + tt * df_hi(sq);
+    }
+    store_pair_df(pdf, p32, wp, b, A, B, rh, d);
+}
+
+// Same traversal and pair order as k_csr_fill.  About one candidate in six is
+// kept, so the screened candidates go to a per-warp queue in shared memory (in
+// traversal order) and the double-float couplings are computed 32 kept pairs at
+// a time, one per lane, instead of by the few lanes of each round that kept one.
+constexpr int kFillWarps = 8;
+
+__global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *__restrict__ x,
+                                                                 const float *__restrict__ xf,
+                                                                 const float2 *__restrict__ xdf, PairScreen ps,
+                                                                 const int32_t *__restrict__ sorted,
+                                                                 const int32_t *__restrict__ lin,
+                                                                 const int32_t *__restrict__ counts,
+                                                                 const int64_t *__restrict__ starts, int64_t n,
+                                                                 int64_t ncx, int64_t ncy, int64_t ncz,
+                                                                 const int64_t *__restrict__ off27, DfTab tab,
+                                                                 PairData<dfv> pdf, PairData<float> p32,
+                                                                 int *__restrict__ err) {
+    __shared__ int32_t q_b[kFillWarps][64];
+    __shared__ float2 q_r[kFillWarps][3][64];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     dfv L[3], halfL[3];
 #pragma unroll
@@ -822,20 +862,29 @@ __global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ 
         L[k] = dfv(ps.L[k]);
         halfL[k] = dfv(0.5 * ps.L[k]);
     }
+    // queue entries [0, cnt) -> pairs w .. w + cnt - 1, one per lane (cnt <= 32)
+    auto drain = [&](int cnt, int64_t w) {
+        if (lane < cnt) {
+            dfv r[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) r[k] = dfv(q_r[wid][k][lane].x, q_r[wid][k][lane].y);
+            df_pair_out(tab, pdf, p32, w + lane, q_b[wid][lane], r, err);
+        }
+    };
     for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
         const int32_t a = sorted[s];
         const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
         int64_t w = off27[(int64_t)a * 27];   // the row's pairs follow in (cell offset, position) order
+        int qn = 0;                           // kept pairs waiting in the queue (warp-uniform)
         for (int j0 = 0; j0 < cw.total; j0 += 32) {
             const int j = j0 + lane;
             int o;
             int64_t pos;
             walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
             (void)o;
-            bool keep = false, exact = false;
+            bool keep = false;
             int32_t b = -1;
             dfv r[3];
-            double r64[3] = {0, 0, 0};
             if (j < cw.total) {
                 b = sorted[pos];
                 const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
@@ -856,9 +905,11 @@ __global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ 
                     }
                     if (big || sc == SCREEN_NEAR) {
                         // float64 decides (and, for far-wrapped pairs, supplies the vector)
+                        double r64[3];
                         const double de = pair_exact(x, a, b, ps, r64);
                         keep = de < ps.rc;
-                        exact = big;
+                        if (big)
+                            for (int k = 0; k < 3; ++k) r[k] = dfv(r64[k]);
                     } else {
                         keep = true;
                     }
@@ -866,38 +917,28 @@ __global__ void __launch_bounds__(256) k_csr_fill_df(const double *__restrict__ 
             }
             const unsigned mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
-                const int64_t wp = w + __popc(mask & ((1u << lane) - 1u));
-                if (exact)
-                    for (int k = 0; k < 3; ++k) r[k] = dfv(r64[k]);
-                const dfv s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-                const dfv y = df_rsqrt(s2);
-                const dfv d = s2 * y;
-                const dfv rh[3] = {r[0] * y, r[1] * y, r[2] * y};
-                dfv A(0.f, 0.f), B(0.f, 0.f);
-                int64_t i = df_search(tab.rvf, tab.ntab, d.hi, tab.inv_dr);
-                // The float search can land one segment off when d lies within a float rounding of a node;
-                // settle the bracket r_{i-1} < d <= r_i (the reference's searchsorted 'left') in double-float,
-                // so the coupling is interpolated inside its segment instead of extrapolated across the node.
-                if (i > 1 && i < tab.ntab) {
-                    const dfv lo = d - df_lo(tab.seg_r[i]);
-                    if (lo.hi < 0.f || (lo.hi == 0.f && lo.lo <= 0.f)) --i;
-                }
-                if (i > 0 && i + 1 < tab.ntab) {
-                    const dfv hi = d - df_lo(tab.seg_r[i + 1]);
-                    if (hi.hi > 0.f || (hi.hi == 0.f && hi.lo > 0.f)) ++i;
-                }
-                if (i <= 0 || i >= tab.ntab) {
-                    atomicExch(err, 1);
-                } else {
-                    const float4 sr = tab.seg_r[i], sp = tab.seg_perp[i], sq = tab.seg_para[i];
-                    const dfv tt = (d - df_lo(sr)) * df_hi(sr);
-                    A = df_lo(sp) + tt * df_hi(sp);
-                    B = df_lo(sq) + tt * df_hi(sq);
-                }
-                store_pair_df(pdf, p32, wp, b, A, B, rh, d);
+                const int q = qn + __popc(mask & ((1u << lane) - 1u));
+                q_b[wid][q] = b;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) q_r[wid][k][q] = make_float2(r[k].hi, r[k].lo);
             }
-            w += __popc(mask);
+            qn += __popc(mask);
+            __syncwarp();
+            if (qn >= 32) {
+                drain(32, w);
+                w += 32;
+                qn -= 32;
+                __syncwarp();
+                if (lane < qn) {   // move the rest (entries 32 .. 32 + qn - 1) to the front
+                    q_b[wid][lane] = q_b[wid][32 + lane];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) q_r[wid][k][lane] = q_r[wid][k][32 + lane];
+                }
+                __syncwarp();
+            }
         }
+        if (qn > 0) drain(qn, w);
+        __syncwarp();
     }
 }
 
@@ -1104,7 +1145,7 @@ int csr_pairs_fill_df(const double *x, const float *xf, const float2 *xdf, doubl
     const int64_t n = cb.n;
     k_row_ptr<<<grid_for(n + 1, 256), 256, 0, s>>>(off27, cnt27, n, row_ptr);
     MPS_LAUNCH_CHECK();
-    k_csr_fill_df<<<grid_for(n * 32, 256, 152 * 64), 256, 0, s>>>(
+    k_csr_fill_df<<<grid_for(n * 32, kFillWarps * 32, 152 * 64), kFillWarps * 32, 0, s>>>(
         x, xf, xdf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts, cb.starts, n, cb.ncell[0],
         cb.ncell[1], cb.ncell[2], off27, tab, pdf, p32, err);
     MPS_LAUNCH_CHECK();
