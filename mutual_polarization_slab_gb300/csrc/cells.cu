@@ -836,9 +836,13 @@ __device__ __forceinline__ void df_pair_out(const DfTab &tab, PairData<dfv> &pdf
 }
 
 // Same traversal and pair order as k_csr_fill.  About one candidate in six is
-// kept, so the screened candidates go to a per-warp queue in shared memory (in
-// traversal order) and the double-float couplings are computed 32 kept pairs at
-// a time, one per lane, instead of by the few lanes of each round that kept one.
+// kept, so the screen only decides which candidates are kept (float screen, float64
+// for the few in its margin band) and queues their ids per warp in shared memory,
+// in traversal order; the double-float separations and couplings are then computed
+// 32 kept pairs at a time, one per lane, instead of by the few lanes of each round
+// that kept one.  The values are those of the per-round form: the keep decision is
+// the same (inside the screen's inner margin the float64 distance is below rc too),
+// and so is the separation (double-float difference, float64 for a far-wrapped pair).
 constexpr int kFillWarps = 8;
 
 __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *__restrict__ x,
@@ -853,7 +857,6 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
                                                                  PairData<dfv> pdf, PairData<float> p32,
                                                                  int *__restrict__ err) {
     __shared__ int32_t q_b[kFillWarps][64];
-    __shared__ float2 q_r[kFillWarps][3][64];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     dfv L[3], halfL[3];
@@ -862,14 +865,31 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
         L[k] = dfv(ps.L[k]);
         halfL[k] = dfv(0.5 * ps.L[k]);
     }
-    // queue entries [0, cnt) -> pairs w .. w + cnt - 1, one per lane (cnt <= 32)
-    auto drain = [&](int cnt, int64_t w) {
-        if (lane < cnt) {
-            dfv r[3];
+    // queue entries [0, cnt) of particle a -> pairs w .. w + cnt - 1, one per lane (cnt <= 32)
+    auto drain = [&](int32_t a, int cnt, int64_t w) {
+        if (lane >= cnt) return;
+        const int32_t b = q_b[wid][lane];
+        dfv r[3];
+        bool big = false;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) r[k] = dfv(q_r[wid][k][lane].x, q_r[wid][k][lane].y);
-            df_pair_out(tab, pdf, p32, w + lane, q_b[wid][lane], r, err);
+        for (int k = 0; k < 3; ++k) {
+            const float2 pa = xdf[3 * a + k], pb = xdf[3 * b + k];
+            dfv v = dfv_two_diff(pa.x, pb.x) + dfv_two_diff(pa.y, pb.y);
+            big = big || !(fabsf(v.hi) < ps.Lf[k] * 0.999f);
+            // minimum image with the float64 path's rule: v >= L/2 -> v - L, v <= -L/2 -> v + L
+            const dfv up = v - halfL[k], dn = v + halfL[k];
+            if (up.hi > 0.f || (up.hi == 0.f && up.lo >= 0.f))
+                v = v - L[k];
+            else if (dn.hi < 0.f || (dn.hi == 0.f && dn.lo <= 0.f))
+                v = v + L[k];
+            r[k] = v;
         }
+        if (big) {   // far-wrapped: float64 supplies the vector
+            double r64[3];
+            pair_exact(x, a, b, ps, r64);
+            for (int k = 0; k < 3; ++k) r[k] = dfv(r64[k]);
+        }
+        df_pair_out(tab, pdf, p32, w + lane, b, r, err);
     };
     for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
         const int32_t a = sorted[s];
@@ -884,60 +904,30 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
             (void)o;
             bool keep = false;
             int32_t b = -1;
-            dfv r[3];
             if (j < cw.total) {
                 b = sorted[pos];
                 const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
-                if (sc != SCREEN_OUT) {
-                    bool big = false;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const float2 pa = xdf[3 * a + k], pb = xdf[3 * b + k];
-                        dfv v = dfv_two_diff(pa.x, pb.x) + dfv_two_diff(pa.y, pb.y);
-                        big = big || !(fabsf(v.hi) < ps.Lf[k] * 0.999f);
-                        // minimum image with the float64 path's rule: v >= L/2 -> v - L, v <= -L/2 -> v + L
-                        const dfv up = v - halfL[k], dn = v + halfL[k];
-                        if (up.hi > 0.f || (up.hi == 0.f && up.lo >= 0.f))
-                            v = v - L[k];
-                        else if (dn.hi < 0.f || (dn.hi == 0.f && dn.lo <= 0.f))
-                            v = v + L[k];
-                        r[k] = v;
-                    }
-                    if (big || sc == SCREEN_NEAR) {
-                        // float64 decides (and, for far-wrapped pairs, supplies the vector)
-                        double r64[3];
-                        const double de = pair_exact(x, a, b, ps, r64);
-                        keep = de < ps.rc;
-                        if (big)
-                            for (int k = 0; k < 3; ++k) r[k] = dfv(r64[k]);
-                    } else {
-                        keep = true;
-                    }
+                if (sc == SCREEN_IN) {
+                    keep = true;
+                } else if (sc == SCREEN_NEAR) {   // the correctly rounded float64 separation decides
+                    double r64[3];
+                    keep = pair_exact(x, a, b, ps, r64) < ps.rc;
                 }
             }
             const unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (keep) {
-                const int q = qn + __popc(mask & ((1u << lane) - 1u));
-                q_b[wid][q] = b;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) q_r[wid][k][q] = make_float2(r[k].hi, r[k].lo);
-            }
+            if (keep) q_b[wid][qn + __popc(mask & ((1u << lane) - 1u))] = b;
             qn += __popc(mask);
             __syncwarp();
             if (qn >= 32) {
-                drain(32, w);
+                drain(a, 32, w);
                 w += 32;
                 qn -= 32;
                 __syncwarp();
-                if (lane < qn) {   // move the rest (entries 32 .. 32 + qn - 1) to the front
-                    q_b[wid][lane] = q_b[wid][32 + lane];
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) q_r[wid][k][lane] = q_r[wid][k][32 + lane];
-                }
+                if (lane < qn) q_b[wid][lane] = q_b[wid][32 + lane];   // the rest to the front
                 __syncwarp();
             }
         }
-        if (qn > 0) drain(qn, w);
+        if (qn > 0) drain(a, qn, w);
         __syncwarp();
     }
 }

@@ -32,11 +32,19 @@ __global__ void k_grid_geom(const double *__restrict__ x, int64_t n, GridParams 
         start[t] = (int32_t)wrap_index(n0 - lo - 1, gp.N[d]);
         const double base = __dsub_rn(__dmul_rn(node0, h), xv);
         const double c = (d == 0) ? gp.wconst : 1.0;
+        // exp(-q r_j^2) at r_j = r_0 + j h by the recurrence w_{j+1} = w_j g_j, g_j = exp(-q (2 r_0 h + (2j+1) h^2)),
+        // g_{j+1} = g_j exp(-2 q h^2): three exponentials per axis instead of P (float64 exp and division are slow
+        // on GB300); the weights agree with the direct exponentials to 2e-14 relative at P = 10 (3.5e-14 at P = 16)
+        const double q = 2.0 * gp.xi * gp.xi * gp.inv_eta[d];
+        const double r0 = base - (double)lo * h;
+        double v = c * exp(-q * (r0 * r0));
+        double g = exp(-q * (2.0 * r0 * h + h * h));
+        const double g2 = exp(-2.0 * q * (h * h));
         for (int j = 0; j < P; ++j) {
-            const double r = base + (double)(j - lo) * h;
-            const double v = c * exp(-2.0 * gp.xi * gp.xi * (r * r) / gp.eta[d]);
             w64[(a * 3 + d) * P + j] = v;
             if (w32) w32[(a * 3 + d) * P + j] = (float)v;
+            v *= g;
+            g *= g2;
         }
     }
 }

@@ -281,6 +281,7 @@ static void free_system(mps_system *s) {
     if (!s) return;
     // a matvec that failed between fork and join may leave pair-sum work on the side stream
     if (s->side) cudaStreamSynchronize(s->side);
+    if (s->cap) cudaStreamSynchronize(s->cap);   // set-up work of a failed create may still run there
     for (auto &e : s->pending)
         for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
     for (auto &e : s->spare)
@@ -2122,9 +2123,9 @@ static int acquire_green(const GridParams &gp, const double *box, double xi, int
     return MPS_OK;
 }
 
-// Grid geometry (start nodes, separable weights), Green's coefficients and the inner grid of a dipole or
-// quadrupole system, on stream gs: none of it depends on the pair list, so the caller runs it on the side stream
-// beside the pair-list construction.
+// Grid geometry (start nodes, separable weights) and Green's coefficients of a dipole or quadrupole system, on
+// stream gs: none of it depends on the pair list, so the caller runs it on the side stream beside the pair-list
+// construction (and the inner grid's set-up on a third stream).
 static int setup_grids(mps_system *s, const mps_system_desc *d, cudaStream_t gs) {
     const int64_t n = d->n;
 #define GS_TRY(expr)                   \
@@ -2139,7 +2140,18 @@ static int setup_grids(mps_system *s, const mps_system_desc *d, cudaStream_t gs)
     GS_TRY(acquire_green(s->gp, d->box, d->xi, s->Gc, s->green, gs));
     s->h64 = s->green->h64;
     s->h32 = s->green->h32;
-    // the inner grid of the gradient-form operator, when asked for (dipole operator, tiled kernels)
+#undef GS_TRY
+    return MPS_OK;
+}
+
+// The inner grid of the gradient-form operator, when asked for (dipole operator, tiled kernels), on stream gs.
+static int setup_inner_grid(mps_system *s, const mps_system_desc *d, cudaStream_t gs) {
+    const int64_t n = d->n;
+#define GS_TRY(expr)                   \
+    do {                               \
+        const int _r = (expr);         \
+        if (_r != MPS_OK) return _r;   \
+    } while (0)
     if (d->inner_P > 0) {
         for (int k = 0; k < 3; ++k)
             if (d->inner_Ngrid[k] < d->inner_P) GS_TRY(MPS_BAD_ARG);
@@ -2247,11 +2259,15 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     const bool grids_on_side = s->kind != MPS_POLYDISPERSE;
     if (grids_on_side) {
         if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventRecord(s->ev_fork, st) != cudaSuccess || cudaStreamWaitEvent(s->side, s->ev_fork, 0) != cudaSuccess)
+            cudaEventRecord(s->ev_fork, st) != cudaSuccess ||
+            cudaStreamWaitEvent(s->side, s->ev_fork, 0) != cudaSuccess ||
+            cudaStreamWaitEvent(s->cap, s->ev_fork, 0) != cudaSuccess)
             CR_TRY(MPS_CUDA_ERR);
         CR_TRY(setup_grids(s, d, s->side));
+        CR_TRY(setup_inner_grid(s, d, s->cap));   // the system's capture stream, idle until its first solve
     }
     // cell list + pair CSR
     compute_ncell(d->box, d->rc, s->ncell);
@@ -2407,11 +2423,16 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
         *out = s;
         return MPS_OK;
     }
-    // the grid and k-space set-up ran on the side stream beside the pair list: join it
+    // the grid and k-space set-up ran on the side and capture streams beside the pair list: join them
     if (grids_on_side) {
-        if (cudaEventRecord(s->ev_join, s->side) != cudaSuccess ||
-            cudaStreamWaitEvent(st, s->ev_join, 0) != cudaSuccess)
-            CR_TRY(MPS_CUDA_ERR);
+        cudaEvent_t ev_inner = nullptr;
+        const bool ok = cudaEventRecord(s->ev_join, s->side) == cudaSuccess &&
+                        cudaStreamWaitEvent(st, s->ev_join, 0) == cudaSuccess &&
+                        cudaEventCreateWithFlags(&ev_inner, cudaEventDisableTiming) == cudaSuccess &&
+                        cudaEventRecord(ev_inner, s->cap) == cudaSuccess &&
+                        cudaStreamWaitEvent(st, ev_inner, 0) == cudaSuccess;
+        if (ev_inner) cudaEventDestroy(ev_inner);
+        if (!ok) CR_TRY(MPS_CUDA_ERR);
     }
 #undef CR_TRY
     *out = s;
