@@ -165,21 +165,49 @@ __device__ __forceinline__ double green_coef(double kx, double ky, double kz, co
     return H;
 }
 
+// The Gaussian factor of H is separable, exp(-sum_d (1 - eta_d) k_d^2 / (4 xi^2)) =
+// prod_d f_d(k_d): the per-axis factors of the spectrum's quarter, f[0 .. Nxh) for
+// x, then Ny/2 + 1 for y and Nz/2 + 1 for z (one float64 exp per axis index
+// instead of one per spectrum point).
+__global__ void k_green_axes(GridParams gp, double *__restrict__ f) {
+    const HalfQuarter q(gp.N);
+    const int nx = q.Nxh, ny = q.Nyq, nz = q.Nzq;
+    const double s = 1.0 / (4.0 * gp.xi * gp.xi);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + ny + nz; i += gridDim.x * blockDim.x) {
+        const int d = i < nx ? 0 : (i < nx + ny ? 1 : 2);
+        const int idx = d == 0 ? i : (d == 1 ? i - nx : i - nx - ny);
+        const double k = fft_freq(idx, gp.N[d]) * gp.kfac[d];
+        f[i] = exp(-(1.0 - gp.eta[d]) * (k * k) * s);
+    }
+}
+
 // One thread per point of the spectrum's quarter (iy <= Ny/2, iz <= Nz/2), written
 // to its mirrored points as well: H depends on ky, kz only through their squares,
 // and the mirrored frequencies are exact negations, so every copy is the value the
-// point would compute itself (a quarter of the float64 sincos / exp work).
-__global__ void k_green_half(GridParams gp, double *__restrict__ h64, float *__restrict__ h32) {
+// point would compute itself (a quarter of the float64 sincos work).
+//   H = 9 (sin k - k cos k)^2 f_x f_y f_z / k^6 / G.
+__global__ void k_green_half(GridParams gp, const double *__restrict__ f, double *__restrict__ h64,
+                             float *__restrict__ h32) {
     const HalfQuarter q(gp.N);
     const int64_t Gq = q.size();
     const double invG = 1.0 / (double)gp.G;
+    const double *fy = f + q.Nxh, *fz = fy + q.Nyq;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gq; t += (int64_t)gridDim.x * blockDim.x) {
         int ix, iy, iz;
         q.point(t, &ix, &iy, &iz);
         const double kx = fft_freq(ix, gp.N[0]) * gp.kfac[0];
         const double ky = fft_freq(iy, gp.N[1]) * gp.kfac[1];
         const double kz = fft_freq(iz, gp.N[2]) * gp.kfac[2];
-        const double H = green_coef(kx, ky, kz, gp) * invG;
+        const double k2 = kx * kx + ky * ky + kz * kz;
+        double H = 0.0;
+        if (k2 > 0.0) {
+            const double kk = sqrt(k2);
+            double sk, ck;
+            sincos(kk, &sk, &ck);
+            const double u = sk - kk * ck;
+            H = 9.0 * u * u * (f[ix] * fy[iy] * fz[iz]) / (k2 * k2 * k2) * invG;
+            if (!isfinite(H)) H = 0.0;
+        }
         mirror_points(q, ix, iy, iz, [&](int64_t i, int, int) {
             h64[i] = H;
             if (h32) h32[i] = (float)H;
@@ -435,8 +463,15 @@ int grid_geometry(const double *x, int64_t n, const GridParams &gp, int32_t *sta
 }
 
 int green_half(const GridParams &gp, double *h64, float *h32, cudaStream_t s) {
-    k_green_half<<<grid_for(HalfQuarter(gp.N).size(), 256), 256, 0, s>>>(gp, h64, h32);
+    const HalfQuarter q(gp.N);
+    const int nf = q.Nxh + q.Nyq + q.Nzq;
+    double *f = nullptr;
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&f, sizeof(double) * nf, s));
+    k_green_axes<<<grid_for(nf, 128), 128, 0, s>>>(gp, f);
     MPS_LAUNCH_CHECK();
+    k_green_half<<<grid_for(q.size(), 256), 256, 0, s>>>(gp, f, h64, h32);
+    MPS_LAUNCH_CHECK();
+    MPS_CUDA_TRY(cudaFreeAsync(f, s));
     return MPS_OK;
 }
 
