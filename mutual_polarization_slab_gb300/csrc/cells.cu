@@ -616,25 +616,31 @@ __global__ void __launch_bounds__(256) k_csr_count(const double *__restrict__ x,
         const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
         if (lane < 27) hist[wid][lane] = 0;
         __syncwarp();
-        for (int j0 = 0; j0 < cw.total; j0 += 32) {
-            const int j = j0 + lane;
-            int o;
-            int64_t pos;
-            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
-            bool keep = false;
-            if (j < cw.total) {
-                const int32_t b = sorted[pos];
-                if (b != a) {
-                    const int sc = pair_screen(xf, a, b, ps);
+        // two candidates per lane per iteration: their dependent loads (position, then coordinates) overlap
+        for (int j0 = 0; j0 < cw.total; j0 += 64) {
+            int o[2];
+            int64_t pos[2];
+            int32_t b[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = j0 + 32 * h + lane;
+                walk_at(cw, j < cw.total ? j : cw.total - 1, o[h], pos[h]);
+                b[h] = j < cw.total ? sorted[pos[h]] : a;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                bool keep = false;
+                if (b[h] != a) {
+                    const int sc = pair_screen(xf, a, b[h], ps);
                     if (sc == SCREEN_IN) {
                         keep = true;
                     } else if (sc == SCREEN_NEAR) {
                         double r[3];
-                        keep = pair_exact(x, a, b, ps, r) < ps.rc;
+                        keep = pair_exact(x, a, b[h], ps, r) < ps.rc;
                     }
                 }
+                if (keep) atomicAdd(&hist[wid][o[h]], 1);
             }
-            if (keep) atomicAdd(&hist[wid][o], 1);
         }
         __syncwarp();
         if (lane < 27) cnt27[(int64_t)a * 27 + lane] = hist[wid][lane];
@@ -856,7 +862,7 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
                                                                  const int64_t *__restrict__ off27, DfTab tab,
                                                                  PairData<dfv> pdf, PairData<float> p32,
                                                                  int *__restrict__ err) {
-    __shared__ int32_t q_b[kFillWarps][64];
+    __shared__ int32_t q_b[kFillWarps][128];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     dfv L[3], halfL[3];
@@ -895,17 +901,23 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
         const int32_t a = sorted[s];
         const CellWalk cw = cell_walk(lin[a], lane, counts, starts, ncx, ncy, ncz);
         int64_t w = off27[(int64_t)a * 27];   // the row's pairs follow in (cell offset, position) order
-        int qn = 0;                           // kept pairs waiting in the queue (warp-uniform)
-        for (int j0 = 0; j0 < cw.total; j0 += 32) {
-            const int j = j0 + lane;
-            int o;
-            int64_t pos;
-            walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
-            (void)o;
-            bool keep = false;
-            int32_t b = -1;
-            if (j < cw.total) {
-                b = sorted[pos];
+        int qn = 0;                           // kept pairs waiting in the queue (warp-uniform, < 32 between rounds)
+        // two candidates per lane per iteration (candidates j0 + lane and j0 + 32 + lane, queued in that order)
+        for (int j0 = 0; j0 < cw.total; j0 += 64) {
+            int32_t bb[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = j0 + 32 * h + lane;
+                int o;
+                int64_t pos;
+                walk_at(cw, j < cw.total ? j : cw.total - 1, o, pos);
+                (void)o;
+                bb[h] = j < cw.total ? sorted[pos] : a;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int32_t b = bb[h];
+                bool keep = false;
                 const int sc = b != a ? pair_screen(xf, a, b, ps) : SCREEN_OUT;
                 if (sc == SCREEN_IN) {
                     keep = true;
@@ -913,17 +925,18 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_csr_fill_df(const double *_
                     double r64[3];
                     keep = pair_exact(x, a, b, ps, r64) < ps.rc;
                 }
+                const unsigned mask = __ballot_sync(0xffffffffu, keep);
+                if (keep) q_b[wid][qn + __popc(mask & ((1u << lane) - 1u))] = b;
+                qn += __popc(mask);
             }
-            const unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (keep) q_b[wid][qn + __popc(mask & ((1u << lane) - 1u))] = b;
-            qn += __popc(mask);
             __syncwarp();
-            if (qn >= 32) {
+            while (qn >= 32) {
                 drain(a, 32, w);
                 w += 32;
                 qn -= 32;
                 __syncwarp();
-                if (lane < qn) q_b[wid][lane] = q_b[wid][32 + lane];   // the rest to the front
+                if (lane < qn) q_b[wid][lane] = q_b[wid][32 + lane];   // the rest to the front (qn < 64 here)
+                if (lane + 32 < qn) q_b[wid][lane + 32] = q_b[wid][64 + lane];
                 __syncwarp();
             }
         }
