@@ -408,7 +408,7 @@ int mps_kspace_cache_clear(void);
 /* Tile depth of the tiled kernels: tile_depth[0] for the float64-width tiles
  * (float64 or double-float spread, whichever ran first, timed by the
  * autotuner), [1] for the float32 tiles (the gradient-form spread -- on the
- * inner grid when the system has one, depth 16 where the grid allows it, not
+ * inner grid when the system has one, depth 12 where the grid allows it, not
  * timed -- or the reference-form spread + contract) (0 = not used yet);
  * ms[4] = the timed candidates (depth 4, depth 8) of those kernels,
  * float64-width then float32, -1 where not timed. */

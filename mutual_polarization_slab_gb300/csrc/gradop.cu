@@ -81,9 +81,9 @@ constexpr int kGChunk = 96;
 
 // Bounds of 5 blocks per SM (48 registers, 36.5 KB of shared memory each): 0.293 ms per launch at the bench
 // workload against 0.299 at 4 blocks (64 registers), 0.300 at 6 (spills) and 0.342 unbounded.
-// Depth 16 (48 accumulators for 3 vectors) at 3 blocks per SM.
+// Depth 12 (36 accumulators for 3 vectors, 64 registers) at 4 blocks per SM, depth 16 (48) at 3.
 template <int TZ, int NR>
-__global__ void __launch_bounds__(256, TZ > 8 ? 3 : 5) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
+__global__ void __launch_bounds__(256, TZ > 12 ? 3 : (TZ > 8 ? 4 : 5)) k_spread_grad_tiled(const double *__restrict__ m, int64_t n, int r0,
                                                            const int32_t *__restrict__ start,
                                                            const float *__restrict__ w, const float *__restrict__ g,
                                                            GridParams gp, const int64_t *__restrict__ tstart,
@@ -445,25 +445,30 @@ static int grad_dispatch(const double *m, int64_t n, int nrhs, const int32_t *st
     return MPS_OK;
 }
 
+template <int TZ>
+static int spread_grad_deep(const double *m, int64_t n, int nrhs, const int32_t *start, const float *w,
+                            const float *g, const GridParams &gp, const TileBins &tb, float *grid, cudaStream_t s) {
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        const unsigned blocks = (unsigned)tb.ntiles;
+        if (nr == 3)
+            k_spread_grad_tiled<TZ, 3><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
+                                                              tb.ntx, tb.nty, grid);
+        else if (nr == 2)
+            k_spread_grad_tiled<TZ, 2><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
+                                                              tb.ntx, tb.nty, grid);
+        else
+            k_spread_grad_tiled<TZ, 1><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
+                                                              tb.ntx, tb.nty, grid);
+        MPS_LAUNCH_CHECK();
+    }
+    return MPS_OK;
+}
+
 int spread_grad_tiled(const double *m, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
                       const GridParams &gp, const TileBins &tb, float *grid, cudaStream_t s) {
-    if (tb.tz == 16) {
-        for (int r0 = 0; r0 < nrhs; r0 += 3) {
-            const int nr = min(3, nrhs - r0);
-            const unsigned blocks = (unsigned)tb.ntiles;
-            if (nr == 3)
-                k_spread_grad_tiled<16, 3><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
-                                                                  tb.ntx, tb.nty, grid);
-            else if (nr == 2)
-                k_spread_grad_tiled<16, 2><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
-                                                                  tb.ntx, tb.nty, grid);
-            else
-                k_spread_grad_tiled<16, 1><<<blocks, 256, 0, s>>>(m, n, r0, start, w, g, gp, tb.tile_start, tb.entries,
-                                                                  tb.ntx, tb.nty, grid);
-            MPS_LAUNCH_CHECK();
-        }
-        return MPS_OK;
-    }
+    if (tb.tz == 16) return spread_grad_deep<16>(m, n, nrhs, start, w, g, gp, tb, grid, s);
+    if (tb.tz == 12) return spread_grad_deep<12>(m, n, nrhs, start, w, g, gp, tb, grid, s);
     if (tb.tz == 8) return grad_dispatch<8>(m, n, nrhs, start, w, g, gp, tb, grid, nullptr, nullptr, true, s);
     if (tb.tz == 4) return grad_dispatch<4>(m, n, nrhs, start, w, g, gp, tb, grid, nullptr, nullptr, true, s);
     return MPS_BAD_ARG;

@@ -206,7 +206,7 @@ struct mps_system {
     void *fft_work = nullptr;
     size_t fft_work_bytes = 0;
     TileBins tb64, tb32;        // tile binning for the tiled spread/contract (per precision tile depth)
-    TileBins tbg;               // tiles of the gradient-form spread (depth 16 where the grid allows it)
+    TileBins tbg;               // tiles of the gradient-form spread (depth 12 where the grid allows it)
     double *partial64 = nullptr;
     int tb_use[2] = {-1, -1};         // tuner consumer that built tb64 / tb32
     float *partial32 = nullptr;
@@ -509,7 +509,7 @@ static int stage_begin(mps_system *s, int precision, StageEvents **ev, cudaStrea
 // system of each (grid, support, consumer, batch width) with the kernels that
 // consumer runs, and the fastest is kept for the rest of the process.  The
 // consumers: the float32 reference operator (tiled spread + contract), the
-// float32 gradient operator (its spread; depth 16 without timing where the grid
+// float32 gradient operator (its spread; depth 12 without timing where the grid
 // allows it, see tuned_depth), the float64 operator (spread) and the double-float
 // operator (spread).  The reference-form float32 kernels use tb32, the gradient
 // form tbg, the float64-width kernels tb64.
@@ -577,16 +577,17 @@ static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     // MPS_TILE_DEPTH=4 or 8 fixes the depth instead of timing (A/B comparisons and tests); not cached
     if (const char *fd = getenv("MPS_TILE_DEPTH")) {
         const int d = atoi(fd);
-        if ((d == 4 || d == 8 || (d == 16 && use == kTileGrad32)) && tiles_supported(s->gp, d)) {
+        if ((d == 4 || d == 8 || ((d == 12 || d == 16) && use == kTileGrad32)) && tiles_supported(s->gp, d)) {
             *tz = d;
             return MPS_OK;
         }
     }
-    // The gradient-form spread takes depth 16 where the grid allows it: timed alone it is a few per cent slower
-    // than depth 8, but the whole gradient matvec is 4-6 % faster (N = 1e5 at 192^3 and at 144^3), because its
-    // fewer, wider CTAs leave room for the pair sum running beside it on the side stream.
-    if (use == kTileGrad32 && tiles_supported(s->gp, 16)) {
-        *tz = 16;
+    // The gradient-form spread takes depth 12 where the grid allows it: timed alone depth 8 is a few per cent
+    // faster, but the whole gradient matvec is faster with fewer, wider CTAs that leave room for the pair sum
+    // running beside it on the side stream (depth 16: 4-6 % faster than 8 at N = 1e5, 192^3 and 144^3; depth 12,
+    // at 4 blocks per SM against 3, another 0.6 % of the whole solve at 144^3).
+    if (use == kTileGrad32 && tiles_supported(s->gp, 12)) {
+        *tz = 12;
         return MPS_OK;
     }
     TuneKey key;
@@ -1009,9 +1010,10 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     MPS_TRY(exec_plan(s, CUFFT_C2R, nrhs, s->spec32, s->grid32, 0, st));
     STAGE_MARK(5);
     {
-        // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing); default: warp gather
+        // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing; tiles of depth 4 or 8); default: warp
+        // gather
         const char *e = getenv("MPS_GRAD_CONTRACT");
-        if (e && strcmp(e, "tiled") == 0 && s->tbg.tz != 16) {
+        if (e && strcmp(e, "tiled") == 0 && (s->tbg.tz == 4 || s->tbg.tz == 8)) {
             if (!s->partial32)
                 MPS_TRY(dalloc(&s->partial32, (size_t)s->tbg.nentries * 9 * sizeof(float), st));
             MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tbg, s->partial32,
@@ -2167,11 +2169,11 @@ static int setup_inner_grid(mps_system *s, const mps_system_desc *d, cudaStream_
         GS_TRY(dalloc(&ig.g32, sizeof(float) * 3 * n * ig.gp.P, gs));
         GS_TRY(grid_geometry(s->x, n, ig.gp, ig.start, ig.w64, ig.w32, gs));
         GS_TRY(grad_factors(s->x, n, ig.gp, ig.w64, ig.g32, gs));
-        // depth 16 as for the system's own gradient-form tiles (tuned_depth); MPS_TILE_DEPTH overrides it
-        int tz_in = tiles_supported(ig.gp, 16) ? 16 : 8;
+        // depth 12 as for the system's own gradient-form tiles (tuned_depth); MPS_TILE_DEPTH overrides it
+        int tz_in = tiles_supported(ig.gp, 12) ? 12 : 8;
         if (const char *fd = getenv("MPS_TILE_DEPTH")) {
             const int dz = atoi(fd);
-            if ((dz == 4 || dz == 8 || dz == 16) && tiles_supported(ig.gp, dz)) tz_in = dz;
+            if ((dz == 4 || dz == 8 || dz == 12 || dz == 16) && tiles_supported(ig.gp, dz)) tz_in = dz;
         }
         GS_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, gs));
         GS_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, gs));

@@ -94,7 +94,6 @@ __global__ void k_tile_fill(const int32_t *__restrict__ start, int64_t n, TileGe
 // of k_tile_fill leave the unsorted order arbitrary; the sorted order makes every
 // tiled kernel's sums deterministic.
 constexpr int kSortCap = 4096;
-constexpr int kSortThreads = 256;
 
 __device__ __forceinline__ void tile_entry_out(int32_t v, int64_t pos, int tx, int ty, int tzi,
                                                const int32_t *__restrict__ start, const TileGeom &tg,
@@ -111,7 +110,8 @@ __device__ __forceinline__ void tile_entry_out(int32_t v, int64_t pos, int tx, i
     pentry[pstart[v] + ((int64_t)iz * c[1] + iy) * c[0] + ix] = (int32_t)pos;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_tile_sort(const int32_t *__restrict__ unsorted,
+template <int TPB>
+__global__ void __launch_bounds__(TPB) k_tile_sort(const int32_t *__restrict__ unsorted,
                                                             const int64_t *__restrict__ tstart, int64_t ntiles,
                                                             const int32_t *__restrict__ start, TileGeom tg,
                                                             const int64_t *__restrict__ pstart,
@@ -234,8 +234,13 @@ int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int t
     MPS_LAUNCH_CHECK();
     k_tile_fill<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tb.tile_start, cursor, unsorted);
     MPS_LAUNCH_CHECK();
-    k_tile_sort<<<grid_for(T, 1, 152 * 8), kSortThreads, 0, s>>>(unsorted, tb.tile_start, T, start, tg, tb.pstart,
-                                                                 tb.entries, tb.pentry);
+    // one block per tile; 128 threads where the tiles average a few hundred entries (depth-4 tiles), 256 for longer
+    if (Emax / T <= 512)
+        k_tile_sort<128><<<(unsigned)std::min<int64_t>(T, INT32_MAX), 128, 0, s>>>(unsorted, tb.tile_start, T, start,
+                                                                                tg, tb.pstart, tb.entries, tb.pentry);
+    else
+        k_tile_sort<256><<<(unsigned)std::min<int64_t>(T, INT32_MAX), 256, 0, s>>>(unsorted, tb.tile_start, T, start,
+                                                                                tg, tb.pstart, tb.entries, tb.pentry);
     MPS_LAUNCH_CHECK();
     cudaFreeAsync(tmp, s);
     return MPS_OK;

@@ -90,9 +90,12 @@ def test_grad_kernel_forms_agree(monkeypatch, nrhs):
     eps = np.full(900, 19.0)
     xi, rc, P = 0.7, 5.5, 10
     perp, para, rv = gcap.default_table(xi)
+    # the tiled contraction runs on depth-8 tiles (the default spread depth, 12, has none)
+    monkeypatch.setenv("MPS_TILE_DEPTH", "8")
     s = SpectralEwaldSystem(x, eps, box, xi, rc, (51, 47, 45), P, perp, para, rv, slab_factor=0.0, max_rhs=3)
     m = np.random.default_rng(5).standard_normal((nrhs, 900, 3))
     warp = s.matvec(m, precision="fp32grad").cpu().numpy()
+    assert s.tuning()["fp32"]["tile"][2] == 8
     monkeypatch.setenv("MPS_GRAD_CONTRACT", "tiled")
     tiled = s.matvec(m, precision="fp32grad").cpu().numpy()
     assert np.linalg.norm(warp - tiled) / np.linalg.norm(tiled) < 2e-6
