@@ -535,7 +535,10 @@ static int time_tiles(mps_system *s, int use, int tz, int nrhs, const double *m,
     TileBins tb;
     MPS_TRY(tile_bins_build(s->start, s->n, s->gp, tz, tb, st));
     float *partial = nullptr;
-    if (use == kTileRef32) MPS_TRY(dalloc(&partial, (size_t)tb.nentries * 9 * sizeof(float), st));
+    if (use == kTileRef32) {
+        MPS_TRY(tile_bins_pentry(s->start, s->gp, tb, st));
+        MPS_TRY(dalloc(&partial, (size_t)tb.nentries * 9 * sizeof(float), st));
+    }
     cudaEvent_t e0, e1;
     MPS_CUDA_TRY(cudaEventCreate(&e0));
     MPS_CUDA_TRY(cudaEventCreate(&e1));
@@ -741,8 +744,10 @@ static int matvec_impl(mps_system *s, const double *m, double *out, int nrhs, cu
     }
     // float64: the warp-per-particle gather keeps more lanes busy, which is what
     // matters at GB300's float64 issue rate; float32: the shared-memory tile.
-    if (use_tiles && !dbl)
+    if (use_tiles && !dbl) {
+        MPS_TRY(tile_bins_pentry(s->start, s->gp, s->tb32, st));
         MPS_TRY(contract_tiled<T>(grid, s->n, nrhs, s->start, w, s->gp, tb, partial, out, st));
+    }
     else
         MPS_TRY(contract<T>(grid, s->n, nrhs, s->start, w, s->gp, out, st));
     STAGE_MARK(6);
@@ -833,6 +838,7 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
         MPS_TRY(contract_df_warp(grid, s->n, nrhs, s->order, s->start, s->wdf, s->gp, out, st));
     } else if (use_tiles) {
         if (!s->partial64) MPS_TRY(dalloc(&s->partial64, (size_t)s->tb64.nentries * 9 * sizeof(double), st));
+        MPS_TRY(tile_bins_pentry(s->start, s->gp, s->tb64, st));
         MPS_TRY(contract_tiled_df(grid, s->n, nrhs, s->start, s->w64, s->gp, s->tb64, s->partial64, out, st));
     } else {
         MPS_TRY(dfv_to_f64_inplace(s->grid64, gvals, st));
@@ -1016,6 +1022,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
         if (e && strcmp(e, "tiled") == 0 && (s->tbg.tz == 4 || s->tbg.tz == 8)) {
             if (!s->partial32)
                 MPS_TRY(dalloc(&s->partial32, (size_t)s->tbg.nentries * 9 * sizeof(float), st));
+            MPS_TRY(tile_bins_pentry(s->start, s->gp, s->tbg, st));
             MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tbg, s->partial32,
                                         out, st));
         } else {

@@ -89,17 +89,15 @@ __global__ void k_tile_fill(const int32_t *__restrict__ start, int64_t n, TileGe
 }
 
 // One block per tile: order the tile's particles by id (bitonic sort in shared
-// memory for up to kSortCap entries, else a rank count over the whole list) and
-// record, for each particle, where its entry for this tile landed.  The atomics
-// of k_tile_fill leave the unsorted order arbitrary; the sorted order makes every
-// tiled kernel's sums deterministic.
+// memory for up to kSortCap entries, else a rank count over the whole list).  The
+// atomics of k_tile_fill leave the unsorted order arbitrary; the sorted order makes
+// every tiled kernel's sums deterministic.
 constexpr int kSortCap = 4096;
 
-__device__ __forceinline__ void tile_entry_out(int32_t v, int64_t pos, int tx, int ty, int tzi,
-                                               const int32_t *__restrict__ start, const TileGeom &tg,
-                                               const int64_t *__restrict__ pstart, int32_t *__restrict__ entries,
-                                               int32_t *__restrict__ pentry) {
-    entries[pos] = v;
+// Where particle v's entry for tile (tx, ty, tzi) landed: pentry[pstart[v] + its index in v's tile order] = pos.
+__device__ __forceinline__ void tile_pentry_out(int32_t v, int64_t pos, int tx, int ty, int tzi,
+                                                const int32_t *__restrict__ start, const TileGeom &tg,
+                                                const int64_t *__restrict__ pstart, int32_t *__restrict__ pentry) {
     int L[3][kMaxTileList];
     int c[3];
     for (int d = 0; d < 3; ++d) c[d] = axis_tiles(start[3 * (int64_t)v + d], tg.P, tg.N[d], tg.T[d], L[d]);
@@ -112,18 +110,13 @@ __device__ __forceinline__ void tile_entry_out(int32_t v, int64_t pos, int tx, i
 
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_tile_sort(const int32_t *__restrict__ unsorted,
-                                                            const int64_t *__restrict__ tstart, int64_t ntiles,
-                                                            const int32_t *__restrict__ start, TileGeom tg,
-                                                            const int64_t *__restrict__ pstart,
-                                                            int32_t *__restrict__ entries,
-                                                            int32_t *__restrict__ pentry) {
+                                                   const int64_t *__restrict__ tstart, int64_t ntiles,
+                                                   int32_t *__restrict__ entries) {
     __shared__ int32_t key[kSortCap];
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t s0 = tstart[t];
         const int len = (int)(tstart[t + 1] - s0);
         if (len == 0) continue;
-        const int tx = (int)(t % tg.nt[0]), ty = (int)((t / tg.nt[0]) % tg.nt[1]),
-                  tzi = (int)(t / ((int64_t)tg.nt[0] * tg.nt[1]));
         if (len <= kSortCap) {
             int L = 1;
             while (L < len) L <<= 1;
@@ -144,15 +137,14 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(const int32_t *__restrict__ u
                     }
                     __syncthreads();
                 }
-            for (int e = threadIdx.x; e < len; e += blockDim.x)
-                tile_entry_out(key[e], s0 + e, tx, ty, tzi, start, tg, pstart, entries, pentry);
+            for (int e = threadIdx.x; e < len; e += blockDim.x) entries[s0 + e] = key[e];
         } else {
             // ids are distinct within a tile: an entry's rank is the count of smaller ids
             for (int e = threadIdx.x; e < len; e += blockDim.x) {
                 const int32_t v = unsorted[s0 + e];
                 int rank = 0;
                 for (int j = 0; j < len; ++j) rank += (unsorted[s0 + j] < v);
-                tile_entry_out(v, s0 + rank, tx, ty, tzi, start, tg, pstart, entries, pentry);
+                entries[s0 + rank] = v;
             }
         }
     }
@@ -235,14 +227,45 @@ int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int t
     k_tile_fill<<<grid_for(n, 256), 256, 0, s>>>(start, n, tg, tb.tile_start, cursor, unsorted);
     MPS_LAUNCH_CHECK();
     // one block per tile; 128 threads where the tiles average a few hundred entries (depth-4 tiles), 256 for longer
+    const unsigned tblocks = (unsigned)std::min<int64_t>(T, INT32_MAX);
     if (Emax / T <= 512)
-        k_tile_sort<128><<<(unsigned)std::min<int64_t>(T, INT32_MAX), 128, 0, s>>>(unsorted, tb.tile_start, T, start,
-                                                                                tg, tb.pstart, tb.entries, tb.pentry);
+        k_tile_sort<128><<<tblocks, 128, 0, s>>>(unsorted, tb.tile_start, T, tb.entries);
     else
-        k_tile_sort<256><<<(unsigned)std::min<int64_t>(T, INT32_MAX), 256, 0, s>>>(unsorted, tb.tile_start, T, start,
-                                                                                tg, tb.pstart, tb.entries, tb.pentry);
+        k_tile_sort<256><<<tblocks, 256, 0, s>>>(unsorted, tb.tile_start, T, tb.entries);
     MPS_LAUNCH_CHECK();
     cudaFreeAsync(tmp, s);
+    return MPS_OK;
+}
+
+// A warp per tile: for each of its (sorted) entries, where it sits in the particle's own list.
+__global__ void k_tile_pentry(const int64_t *__restrict__ tstart, int64_t ntiles, const int32_t *__restrict__ entries,
+                              const int32_t *__restrict__ start, TileGeom tg, const int64_t *__restrict__ pstart,
+                              int32_t *__restrict__ pentry) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nw) {
+        const int tx = (int)(t % tg.nt[0]), ty = (int)((t / tg.nt[0]) % tg.nt[1]),
+                  tzi = (int)(t / ((int64_t)tg.nt[0] * tg.nt[1]));
+        for (int64_t e = tstart[t] + lane; e < tstart[t + 1]; e += 32)
+            tile_pentry_out(entries[e], e, tx, ty, tzi, start, tg, pstart, pentry);
+    }
+}
+
+int tile_bins_pentry(const int32_t *start, const GridParams &gp, TileBins &tb, cudaStream_t s) {
+    if (tb.has_pentry || !tb.mem) return MPS_OK;
+    TileGeom tg;
+    tg.P = gp.P;
+    tg.T[0] = kTileX;
+    tg.T[1] = kTileY;
+    tg.T[2] = tb.tz;
+    for (int d = 0; d < 3; ++d) {
+        tg.N[d] = gp.N[d];
+        tg.nt[d] = (gp.N[d] + tg.T[d] - 1) / tg.T[d];
+    }
+    k_tile_pentry<<<grid_for(tb.ntiles * 32, 256), 256, 0, s>>>(tb.tile_start, tb.ntiles, tb.entries, start, tg,
+                                                               tb.pstart, tb.pentry);
+    MPS_LAUNCH_CHECK();
+    tb.has_pentry = true;
     return MPS_OK;
 }
 

@@ -21,11 +21,14 @@ struct TileBins {
     int32_t *entries = nullptr;      // particle id per (tile, particle) entry, tiles in order, ids ascending
     int64_t *pstart = nullptr;       // n + 1: each particle's entries ...
     int32_t *pentry = nullptr;       // ... listed here (entry indices), in the particle's tile order
+    bool has_pentry = false;         // pentry filled (the tiled contractions' gathers need it; spreads do not)
     void *mem = nullptr;             // single allocation backing the arrays above
 };
 
 bool tiles_supported(const GridParams &gp, int tz);
 int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s);
+// Fills tb.pentry (once) for the gathers of the tiled contractions.
+int tile_bins_pentry(const int32_t *start, const GridParams &gp, TileBins &tb, cudaStream_t s);
 void tile_bins_free(TileBins &tb, cudaStream_t s);
 
 // grid[(r*3+c)][G] for r < nrhs, written completely (no zeroing needed).
