@@ -228,6 +228,7 @@ struct mps_system {
     // after the first matvec of that precision and batch width outside a capture)
     std::vector<ArnoldiGraph> graphs;
     cudaStream_t cap = nullptr;
+    cudaStream_t prep = nullptr;     // first-use set-up of the double-float residual beside the first inner solve
     cudaEvent_t ev_graph = nullptr;  // recorded after each graph launch (destroying the graphs waits on it)
     std::vector<std::pair<int, int>> mv_seen;   // (precision, batch width) of the matvecs run so far
     int32_t *host_step = nullptr;    // pinned: the step counter read back after a graph launch
@@ -282,6 +283,7 @@ static void free_system(mps_system *s) {
     // a matvec that failed between fork and join may leave pair-sum work on the side stream
     if (s->side) cudaStreamSynchronize(s->side);
     if (s->cap) cudaStreamSynchronize(s->cap);   // set-up work of a failed create may still run there
+    if (s->prep) cudaStreamSynchronize(s->prep);
     for (auto &e : s->pending)
         for (int k = 0; k <= kStages; ++k) cudaEventDestroy(e.ev[k]);
     for (auto &e : s->spare)
@@ -312,6 +314,7 @@ static void free_system(mps_system *s) {
         if (g.ws) cudaFreeAsync(g.ws, s->stream);
     }
     if (s->cap) cudaStreamDestroy(s->cap);
+    if (s->prep) cudaStreamDestroy(s->prep);
     tile_bins_free(s->tb64, s->stream);
     tile_bins_free(s->tb32, s->stream);
     tile_bins_free(s->tbg, s->stream);
@@ -576,6 +579,8 @@ static int time_tiles(mps_system *s, int use, int tz, int nrhs, const double *m,
     return rc;
 }
 
+static bool tile_depth_known(const mps_system *s, int use);
+
 static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     // MPS_TILE_DEPTH=4 or 8 fixes the depth instead of timing (A/B comparisons and tests); not cached
     if (const char *fd = getenv("MPS_TILE_DEPTH")) {
@@ -645,6 +650,25 @@ static int tuned_depth(mps_system *s, int use, cudaStream_t st, int *tz) {
     }
     *tz = res.tz;
     return MPS_OK;
+}
+
+// The tile depth of a consumer is settled without timing: fixed by MPS_TILE_DEPTH, the gradient form's fixed
+// depth, or already timed in this process for this (device, grid, support, consumer, batch width).
+static bool tile_depth_known(const mps_system *s, int use) {
+    if (const char *fd = getenv("MPS_TILE_DEPTH")) {
+        const int d = atoi(fd);
+        if (d == 4 || d == 8 || ((d == 12 || d == 16) && use == kTileGrad32)) return true;
+    }
+    if (use == kTileGrad32) return true;
+    TuneKey key;
+    memset(&key, 0, sizeof(key));
+    key.dev = current_device();
+    for (int k = 0; k < 3; ++k) key.N[k] = s->gp.N[k];
+    key.P = s->gp.P;
+    key.use = use;
+    key.nrhs = s->max_rhs < 3 ? s->max_rhs : 3;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune.find(key) != g_tune.end();
 }
 
 // Lazily bins the particles for the tiled kernels of one precision (tile depth
@@ -1979,6 +2003,25 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
     int rc = MPS_NOT_CONVERGED;
     int step = 0;
     int e = MPS_OK;
+    // The double-float residual's first-use set-up (weights, tiles, grids, scale tensor) runs on the system's
+    // prep stream beside the first inner solve, when nothing in it has to be timed (its tile depth is known).
+    cudaEvent_t ev_prep = nullptr;
+    if (s->resid_prec == MPS_DF && df_usable(s) && !s->wdf && tile_depth_known(s, kTileDF)) {
+        cudaEvent_t ev_in = nullptr;
+        bool ok = (s->prep || cudaStreamCreateWithFlags(&s->prep, cudaStreamNonBlocking) == cudaSuccess) &&
+                  cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventRecord(ev_in, st) == cudaSuccess && cudaStreamWaitEvent(s->prep, ev_in, 0) == cudaSuccess;
+        if (ev_in) cudaEventDestroy(ev_in);
+        bool used = false;
+        if (ok) ok = df_prepare(s, s->prep, &used) == MPS_OK;
+        ok = ok && cudaEventCreateWithFlags(&ev_prep, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventRecord(ev_prep, s->prep) == cudaSuccess;
+        if (!ok) {
+            cudaFreeAsync(buf, st);
+            if (ev_prep) cudaEventDestroy(ev_prep);
+            return MPS_CUDA_ERR;
+        }
+    }
     {
         GmresFlags f0;
         f0.final_check = false;
@@ -1987,6 +2030,10 @@ static int refine_mixed(mps_system *s, const double *b, double *x, int nrhs, con
         int icyc = 0;
         e = gmres_core(s, b, x, nrhs, inner_tol, o->restart, inner_maxit, s->inner_prec, ic.data(), ir.data(), &icyc, mv32,
                        st, f0);
+    }
+    if (ev_prep) {
+        if (cudaStreamWaitEvent(st, ev_prep, 0) != cudaSuccess && e == MPS_OK) e = MPS_CUDA_ERR;
+        cudaEventDestroy(ev_prep);
     }
     if (e == MPS_OK || e == MPS_NOT_CONVERGED) {
         e = true_residual(s, b, x, r, ax, nrhs, partial, nrm, rel, st);
