@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(256) k_rs_csr(const double *__restrict__ m, do
     const int lane = threadIdx.x % G;
     const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+    r0 += (int)blockIdx.y * R;   // several blocks of R vectors in one launch (grid y)
     const int nr = min(R, nrhs - r0);
     for (int64_t i = grp; i < n; i += ngrp) {
         // rows in `order` (cell order): neighbouring groups read overlapping neighbour moments
@@ -266,8 +267,12 @@ int real_space_csr(const double *m, double *out, int64_t n, int nrhs, const int6
     unsigned grid = grid_for(n * G, block, 152 * 64);
     for (int r0 = 0; r0 < nrhs; r0 += 4) {
         int nr = nrhs - r0;
-        if (nr >= 4)
-            k_rs_csr<T, G, 4><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
+        if (nr >= 4) {
+            const int nb = nr / 4;   // every full block of 4 vectors in one launch (grid y)
+            k_rs_csr<T, G, 4><<<dim3(grid, nb), block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                               slab, accumulate, m, nullptr);
+            r0 += 4 * (nb - 1);
+        }
         else if (nr == 3)
             k_rs_csr<T, G, 3><<<grid, block, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab, accumulate, m, nullptr);
         else if (nr == 2)
@@ -330,9 +335,11 @@ int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int 
     for (int r0 = 0; r0 < nrhs;) {
         const int nr = nrhs - r0;
         if (nr >= 8) {
-            k_rs_csr<float, G, 8, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
-                                                              slab, accumulate, m32, order);
-            r0 += 8;
+            // every full block of 8 vectors in one launch (grid y): small systems fill the GPU with all of them
+            const int nb = nr / 8;
+            k_rs_csr<float, G, 8, float><<<dim3(grid, nb), 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag,
+                                                                        diag_of_rhs, slab, accumulate, m32, order);
+            r0 += 8 * nb;
         } else if (nr >= 4) {
             k_rs_csr<float, G, 4, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
                                                               slab, accumulate, m32, order);
