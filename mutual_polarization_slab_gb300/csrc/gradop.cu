@@ -381,6 +381,189 @@ __global__ void __launch_bounds__(256, 3) k_contract_grad_warp(const float *__re
     }
 }
 
+// Contraction by home blocks (the default where the support is 8 or 10): one CTA per
+// kHomeBlock^3 block of grid nodes stages every node its particles' stencils can
+// reach -- the block grown by P - 1 nodes per axis, R = kHomeBlock + P - 1 per axis,
+// one plane of R^3 floats per vector -- in shared memory with coalesced loads, and
+// its particles' offsets and per-axis factors (kHomeChunk particles at a time).  One
+// warp per particle then runs the sums of k_contract_grad_warp in the same order,
+// from shared memory and registers instead of L2: the results are bit-identical.  P
+// is a template parameter, so the z runs unroll completely with the z factors in
+// registers and the shared-memory offsets are immediates.  A node is staged by about
+// (R / kHomeBlock)^3 blocks (9.6 at P = 10), all from L2.
+// 67 KB of shared memory at P = 10 and 3 vectors, 3 blocks per SM (80 registers): the mixed step at the bench
+// workload took 19.25 ms against 20.08 with the warp gather; float4 nodes (the 3 vectors interleaved, 87 KB,
+// 2 blocks per SM) took 20.17.
+constexpr int kHomeChunk = 32;
+
+template <int NR, int P>
+constexpr size_t home_smem_bytes() {
+    constexpr int R = kHomeBlock + P - 1;
+    return sizeof(float) * (size_t)NR * R * R * R + sizeof(float) * 2 * kHomeChunk * 3 * P +
+           sizeof(int) * 4 * kHomeChunk;
+}
+
+template <int NR, int P>
+__global__ void __launch_bounds__(256, 3) k_contract_grad_home(const float *__restrict__ grid, int64_t n, int r0,
+                                                               const int64_t *__restrict__ hstart,
+                                                               const int32_t *__restrict__ hentries, int nbx, int nby,
+                                                               const int32_t *__restrict__ start,
+                                                               const float *__restrict__ w, const float *__restrict__ g,
+                                                               GridParams gp, double *__restrict__ out) {
+    constexpr int R = kHomeBlock + P - 1;
+    constexpr int RR = R * R;
+    constexpr int VOL = RR * R;
+    constexpr int F = 3 * P;                        // per-axis factors of one particle
+    extern __shared__ float s_reg[];                // [NR][VOL] nodes, x fastest
+    float *s_w = s_reg + NR * VOL;                  // [kHomeChunk][F]
+    float *s_g = s_w + kHomeChunk * F;              // [kHomeChunk][F]
+    int *s_p = (int *)(s_g + kHomeChunk * F);       // [kHomeChunk][4]: offsets in the block, particle id
+    const int64_t b = blockIdx.x;
+    const int64_t e0 = hstart[b], e1 = hstart[b + 1];
+    if (e0 == e1) return;   // the whole CTA leaves: no barrier is left waiting
+    const int Nx = gp.N[0], Ny = gp.N[1], Nz = gp.N[2];
+    const int64_t G = gp.G;
+    const int X0 = (int)(b % nbx) * kHomeBlock, Y0 = (int)((b / nbx) % nby) * kHomeBlock,
+              Z0 = (int)(b / ((int64_t)nbx * nby)) * kHomeBlock;
+    const float *g0 = grid + (int64_t)r0 * G;
+#pragma unroll 4
+    for (int q = threadIdx.x; q < VOL; q += blockDim.x) {
+        const int row = q / R, x = q - row * R;
+        const int z = row / R, y = row - z * R;
+        // origin + offset < 3 N (the host requires N >= kHomeBlock and N >= P): at most two wraps
+        int gx = X0 + x, gy = Y0 + y, gz = Z0 + z;
+        gx -= gx >= Nx ? Nx : 0;
+        gx -= gx >= Nx ? Nx : 0;
+        gy -= gy >= Ny ? Ny : 0;
+        gy -= gy >= Ny ? Ny : 0;
+        gz -= gz >= Nz ? Nz : 0;
+        gz -= gz >= Nz ? Nz : 0;
+        const int64_t node = ((int64_t)gz * Ny + gy) * Nx + gx;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) s_reg[r * VOL + q] = __ldg(g0 + r * G + node);
+    }
+    const int lane = threadIdx.x & 31;
+    for (int64_t c0 = e0; c0 < e1; c0 += kHomeChunk) {
+        const int cnt = (int)min((int64_t)kHomeChunk, e1 - c0);
+        for (int q = threadIdx.x; q < cnt * F; q += blockDim.x) {
+            const int p = q / F, k = q - p * F;
+            const int64_t a = hentries[c0 + p];
+            s_w[q] = w[a * F + k];
+            s_g[q] = g[a * F + k];
+        }
+        if (threadIdx.x < cnt) {
+            const int64_t a = hentries[c0 + threadIdx.x];
+            // the home block holds the stencil's first node: offsets in [0, kHomeBlock)
+            s_p[4 * threadIdx.x + 0] = start[3 * a] - X0;
+            s_p[4 * threadIdx.x + 1] = start[3 * a + 1] - Y0;
+            s_p[4 * threadIdx.x + 2] = start[3 * a + 2] - Z0;
+            s_p[4 * threadIdx.x + 3] = (int)a;
+        }
+        __syncthreads();   // the region (first pass) and this chunk's particle data are in place
+        for (int pp = threadIdx.x >> 5; pp < cnt; pp += blockDim.x >> 5) {
+            const int ox = s_p[4 * pp], oy = s_p[4 * pp + 1], oz = s_p[4 * pp + 2];
+            const int64_t a = s_p[4 * pp + 3];
+            const float *wa = s_w + pp * F, *ga = s_g + pp * F;
+            float wz[P], gz[P];
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                wz[j] = wa[2 * P + j];
+                gz[j] = ga[2 * P + j];
+            }
+            float acc[3 * NR];
+#pragma unroll
+            for (int c = 0; c < 3 * NR; ++c) acc[c] = 0.f;
+#pragma unroll
+            for (int row0 = 0; row0 < P * P; row0 += 32) {
+                int idx, sub, lpp;   // lpp is a constant of each unrolled round
+                if (!stencil_row(row0, P, lane, &idx, &sub, &lpp)) continue;
+                const int jx = idx % P, jy = idx / P;
+                const float *col = s_reg + (oz * R + oy + jy) * R + ox + jx;
+                float s0[NR], s1[NR];
+#pragma unroll
+                for (int r = 0; r < NR; ++r) s0[r] = s1[r] = 0.f;
+                if (lpp == 1) {
+#pragma unroll
+                    for (int jz = 0; jz < P; ++jz) {
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            const float v = col[r * VOL + jz * RR];
+                            s0[r] += v * wz[jz];
+                            s1[r] += v * gz[jz];
+                        }
+                    }
+                } else {
+                    for (int jz = sub; jz < P; jz += lpp) {
+                        const float wzj = wa[2 * P + jz], gzj = ga[2 * P + jz];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            const float v = col[r * VOL + jz * RR];
+                            s0[r] += v * wzj;
+                            s1[r] += v * gzj;
+                        }
+                    }
+                }
+                const float wx = wa[jx], wy = wa[P + jy], gx = ga[jx], gy = ga[P + jy];
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    acc[3 * r + 0] += gx * wy * s0[r];
+                    acc[3 * r + 1] += wx * gy * s0[r];
+                    acc[3 * r + 2] += wx * wy * s1[r];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3 * NR; ++c) acc[c] = warp_sum(acc[c]);
+            if (lane == 0)
+#pragma unroll
+                for (int r = 0; r < NR; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        out[((int64_t)(r0 + r) * n + a) * 3 + c] = (double)acc[3 * r + c] * gp.hprod;
+        }
+        __syncthreads();   // this chunk's particle data is read before the next chunk overwrites it
+    }
+}
+
+bool contract_grad_home_supported(const GridParams &gp) {
+    if (gp.P != 8 && gp.P != 10) return false;
+    for (int d = 0; d < 3; ++d)
+        if (gp.N[d] < kHomeBlock || gp.N[d] < gp.P) return false;
+    return true;
+}
+
+template <int NR, int P>
+static int home_launch(const float *grid, int64_t n, int r0, const int32_t *start, const float *w, const float *g,
+                       const GridParams &gp, const TileBins &tb, double *out, cudaStream_t s) {
+    constexpr size_t smem = home_smem_bytes<NR, P>();
+    if (smem > 48 * 1024)
+        MPS_CUDA_TRY(cudaFuncSetAttribute(k_contract_grad_home<NR, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+    k_contract_grad_home<NR, P><<<(unsigned)tb.nhome, 256, smem, s>>>(grid, n, r0, tb.hstart, tb.hentries, tb.nhb[0],
+                                                                       tb.nhb[1], start, w, g, gp, out);
+    MPS_LAUNCH_CHECK();
+    return MPS_OK;
+}
+
+template <int P>
+static int home_dispatch(const float *grid, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                         const GridParams &gp, const TileBins &tb, double *out, cudaStream_t s) {
+    for (int r0 = 0; r0 < nrhs; r0 += 3) {
+        const int nr = min(3, nrhs - r0);
+        const int rc = nr == 3   ? home_launch<3, P>(grid, n, r0, start, w, g, gp, tb, out, s)
+                       : nr == 2 ? home_launch<2, P>(grid, n, r0, start, w, g, gp, tb, out, s)
+                                 : home_launch<1, P>(grid, n, r0, start, w, g, gp, tb, out, s);
+        if (rc) return rc;
+    }
+    return MPS_OK;
+}
+
+int contract_grad_home(const float *grid, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                       const GridParams &gp, const TileBins &tb, double *out, cudaStream_t s) {
+    if (!tb.has_home || !contract_grad_home_supported(gp)) return MPS_BAD_ARG;
+    if (gp.P == 10) return home_dispatch<10>(grid, n, nrhs, start, w, g, gp, tb, out, s);
+    return home_dispatch<8>(grid, n, nrhs, start, w, g, gp, tb, out, s);
+}
+
 int contract_grad_warp(const float *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start,
                        const float *w, const float *g, const GridParams &gp, double *out, cudaStream_t s) {
     const unsigned blocks = grid_for(n * 32, 256, 152 * 64);

@@ -18,5 +18,10 @@ int contract_grad_tiled(const float *grid, int64_t n, int nrhs, const int32_t *s
 // The same contraction as one warp per particle gathering from the grids (no tiles).
 int contract_grad_warp(const float *grid, int64_t n, int nrhs, const int32_t *order, const int32_t *start,
                        const float *w, const float *g, const GridParams &gp, double *out, cudaStream_t s);
+// The same sums (bit-identical) with each home block's reachable nodes staged in shared memory first; tb must hold
+// home bins (tile_bins_home) of the same start.
+bool contract_grad_home_supported(const GridParams &gp);
+int contract_grad_home(const float *grid, int64_t n, int nrhs, const int32_t *start, const float *w, const float *g,
+                       const GridParams &gp, const TileBins &tb, double *out, cudaStream_t s);
 
 }  // namespace mps

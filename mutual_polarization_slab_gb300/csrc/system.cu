@@ -210,6 +210,8 @@ struct mps_system {
     double *partial64 = nullptr;
     int tb_use[2] = {-1, -1};         // tuner consumer that built tb64 / tb32
     float *partial32 = nullptr;
+    float *partialg = nullptr;        // partial sums of the tiled gradient-form contraction (A/B form) ...
+    int64_t partialg_n = 0;           // ... and its capacity in floats
     bool tiled = true;
     bool profile = false;
     std::vector<StageEvents> pending;
@@ -320,6 +322,7 @@ static void free_system(mps_system *s) {
     tile_bins_free(s->tbg, s->stream);
     if (s->partial64) cudaFreeAsync(s->partial64, s->stream);
     if (s->partial32) cudaFreeAsync(s->partial32, s->stream);
+    if (s->partialg) cudaFreeAsync(s->partialg, s->stream);
     if (InnerGrid *ig = s->inner) {
         void *ip[] = {ig->start, ig->w64, ig->w32, ig->g32, ig->grid, ig->spec};
         for (void *q : ip)
@@ -997,6 +1000,38 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
 
 static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st);
 
+// The gradient-form contraction: staged home blocks (default), one warp per particle gathering from L2
+// (MPS_GRAD_CONTRACT=warp), or the tiled partial sums on tiles of depth 4 or 8 (MPS_GRAD_CONTRACT=tiled); the
+// other forms are kept for A/B timing.  The home and warp forms give bit-identical results.
+enum { kGradHome = 0, kGradWarp = 1, kGradTiled = 2 };
+static int grad_contract_mode(const GridParams &gp, const TileBins &tb) {
+    const char *e = getenv("MPS_GRAD_CONTRACT");
+    if (e && strcmp(e, "tiled") == 0 && (tb.tz == 4 || tb.tz == 8)) return kGradTiled;
+    if (e && strcmp(e, "warp") == 0) return kGradWarp;
+    return contract_grad_home_supported(gp) ? kGradHome : kGradWarp;
+}
+
+static int grad_contract(mps_system *s, const float *grid, int nrhs, const int32_t *start, const float *w,
+                         const float *g, const GridParams &gp, TileBins &tb, double *out, cudaStream_t st) {
+    const int mode = grad_contract_mode(gp, tb);
+    if (mode == kGradTiled) {
+        if (s->partialg_n < tb.nentries * 9) {
+            if (s->partialg) MPS_CUDA_TRY(cudaFreeAsync(s->partialg, st));
+            s->partialg = nullptr;
+            s->partialg_n = 0;
+            MPS_TRY(dalloc(&s->partialg, (size_t)tb.nentries * 9 * sizeof(float), st));
+            s->partialg_n = tb.nentries * 9;
+        }
+        MPS_TRY(tile_bins_pentry(start, gp, tb, st));
+        return contract_grad_tiled(grid, s->n, nrhs, start, w, g, gp, tb, s->partialg, out, st);
+    }
+    if (mode == kGradHome) {
+        MPS_TRY(tile_bins_home(start, s->n, gp, tb, st));
+        return contract_grad_home(grid, s->n, nrhs, start, w, g, gp, tb, out, st);
+    }
+    return contract_grad_warp(grid, s->n, nrhs, s->order, start, w, g, gp, out, st);
+}
+
 static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     // the gradient form exists for the dipole operator only: the others run their own float32 operator
     if (s->kind == MPS_DIPOLE_QUADRUPOLE) return matvec_quad<float>(s, m, out, nrhs, st);
@@ -1039,20 +1074,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     STAGE_MARK(4);
     MPS_TRY(exec_plan(s, CUFFT_C2R, nrhs, s->spec32, s->grid32, 0, st));
     STAGE_MARK(5);
-    {
-        // MPS_GRAD_CONTRACT=tiled selects the tiled contraction (A/B timing; tiles of depth 4 or 8); default: warp
-        // gather
-        const char *e = getenv("MPS_GRAD_CONTRACT");
-        if (e && strcmp(e, "tiled") == 0 && (s->tbg.tz == 4 || s->tbg.tz == 8)) {
-            if (!s->partial32)
-                MPS_TRY(dalloc(&s->partial32, (size_t)s->tbg.nentries * 9 * sizeof(float), st));
-            MPS_TRY(tile_bins_pentry(s->start, s->gp, s->tbg, st));
-            MPS_TRY(contract_grad_tiled(s->grid32, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tbg, s->partial32,
-                                        out, st));
-        } else {
-            MPS_TRY(contract_grad_warp(s->grid32, s->n, nrhs, s->order, s->start, s->w32, s->g32, s->gp, out, st));
-        }
-    }
+    MPS_TRY(grad_contract(s, s->grid32, nrhs, s->start, s->w32, s->g32, s->gp, s->tbg, out, st));
     STAGE_MARK(6);
     if (beside)
         MPS_TRY(pair_sum_join(s, out, nrhs, st));
@@ -1096,7 +1118,7 @@ static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nr
     STAGE_MARK(4);
     MPS_TRY(exec_plan_gp(s, ig.gp, CUFFT_C2R, nrhs, ig.spec, ig.grid, 0, st));
     STAGE_MARK(5);
-    MPS_TRY(contract_grad_warp(ig.grid, s->n, nrhs, s->order, ig.start, ig.w32, ig.g32, ig.gp, out, st));
+    MPS_TRY(grad_contract(s, ig.grid, nrhs, ig.start, ig.w32, ig.g32, ig.gp, ig.tb, out, st));
     STAGE_MARK(6);
     if (beside)
         MPS_TRY(pair_sum_join(s, out, nrhs, st));
@@ -2230,6 +2252,7 @@ static int setup_inner_grid(mps_system *s, const mps_system_desc *d, cudaStream_
             if ((dz == 4 || dz == 8 || dz == 12 || dz == 16) && tiles_supported(ig.gp, dz)) tz_in = dz;
         }
         GS_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, gs));
+        if (contract_grad_home_supported(ig.gp)) GS_TRY(tile_bins_home(ig.start, n, ig.gp, ig.tb, gs));
         GS_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, gs));
     }
 #undef GS_TRY

@@ -269,8 +269,65 @@ int tile_bins_pentry(const int32_t *start, const GridParams &gp, TileBins &tb, c
     return MPS_OK;
 }
 
+__device__ __forceinline__ int64_t home_block(const int32_t *__restrict__ start, int64_t a, int nbx, int nby) {
+    return ((int64_t)(start[3 * a + 2] / kHomeBlock) * nby + start[3 * a + 1] / kHomeBlock) * nbx +
+           start[3 * a] / kHomeBlock;
+}
+
+__global__ void k_home_count(const int32_t *__restrict__ start, int64_t n, int nbx, int nby,
+                             int32_t *__restrict__ count) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&count[home_block(start, a, nbx, nby)], 1);
+}
+
+// The order inside a block is that of the atomics; each particle's sum does not depend on it.
+__global__ void k_home_fill(const int32_t *__restrict__ start, int64_t n, int nbx, int nby,
+                            const int64_t *__restrict__ hstart, int32_t *__restrict__ cursor,
+                            int32_t *__restrict__ hentries) {
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = home_block(start, a, nbx, nby);
+        hentries[hstart[b] + atomicAdd(&cursor[b], 1)] = (int32_t)a;
+    }
+}
+
+int tile_bins_home(const int32_t *start, int64_t n, const GridParams &gp, TileBins &tb, cudaStream_t s) {
+    if (tb.has_home) return MPS_OK;
+    if (n < 1) return MPS_BAD_ARG;
+    int64_t H = 1;
+    for (int d = 0; d < 3; ++d) {
+        tb.nhb[d] = (int)((gp.N[d] + kHomeBlock - 1) / kHomeBlock);
+        H *= tb.nhb[d];
+    }
+    tb.nhome = H;
+    size_t tmp_bytes = 256 * 3 + (size_t)H * 4 * 2 + scan_workspace(H + 1);
+    char *tmp = nullptr;
+    MPS_CUDA_TRY(cudaMallocAsync((void **)&tmp, tmp_bytes, s));
+    char *p = tmp;
+    int32_t *count = (int32_t *)carve_t(p, (size_t)H * 4);
+    int32_t *cursor = (int32_t *)carve_t(p, (size_t)H * 4);
+    void *scan_tmp = carve_t(p, scan_workspace(H + 1));
+    MPS_CUDA_TRY(cudaMallocAsync(&tb.hmem, 256 * 2 + (size_t)(H + 1) * 8 + (size_t)n * 4, s));
+    p = (char *)tb.hmem;
+    tb.hstart = (int64_t *)carve_t(p, (size_t)(H + 1) * 8);
+    tb.hentries = (int32_t *)carve_t(p, (size_t)n * 4);
+    MPS_CUDA_TRY(cudaMemsetAsync(count, 0, (size_t)H * 4, s));
+    MPS_CUDA_TRY(cudaMemsetAsync(cursor, 0, (size_t)H * 4, s));
+    k_home_count<<<grid_for(n, 256), 256, 0, s>>>(start, n, tb.nhb[0], tb.nhb[1], count);
+    MPS_LAUNCH_CHECK();
+    int r = exclusive_scan_i32_to_i64(count, tb.hstart, H, scan_tmp, s);
+    if (r) return r;
+    k_scan_total<int32_t><<<1, 32, 0, s>>>(count, tb.hstart, H);
+    MPS_LAUNCH_CHECK();
+    k_home_fill<<<grid_for(n, 256), 256, 0, s>>>(start, n, tb.nhb[0], tb.nhb[1], tb.hstart, cursor, tb.hentries);
+    MPS_LAUNCH_CHECK();
+    cudaFreeAsync(tmp, s);
+    tb.has_home = true;
+    return MPS_OK;
+}
+
 void tile_bins_free(TileBins &tb, cudaStream_t s) {
     if (tb.mem) cudaFreeAsync(tb.mem, s);
+    if (tb.hmem) cudaFreeAsync(tb.hmem, s);
     tb = TileBins();
 }
 

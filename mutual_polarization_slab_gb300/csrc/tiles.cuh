@@ -23,12 +23,24 @@ struct TileBins {
     int32_t *pentry = nullptr;       // ... listed here (entry indices), in the particle's tile order
     bool has_pentry = false;         // pentry filled (the tiled contractions' gathers need it; spreads do not)
     void *mem = nullptr;             // single allocation backing the arrays above
+    // Home bins (on demand, tile_bins_home): every particle once, under the kHomeBlock^3 block of grid nodes that
+    // holds the first node of its stencil; the stencil then lies inside the block grown by P - 1 nodes per axis.
+    bool has_home = false;
+    int nhb[3] = {0, 0, 0};          // home blocks per axis
+    int64_t nhome = 0;
+    int64_t *hstart = nullptr;       // nhome + 1
+    int32_t *hentries = nullptr;     // n particle ids, grouped by home block
+    void *hmem = nullptr;
 };
+
+constexpr int kHomeBlock = 8;
 
 bool tiles_supported(const GridParams &gp, int tz);
 int tile_bins_build(const int32_t *start, int64_t n, const GridParams &gp, int tz, TileBins &tb, cudaStream_t s);
 // Fills tb.pentry (once) for the gathers of the tiled contractions.
 int tile_bins_pentry(const int32_t *start, const GridParams &gp, TileBins &tb, cudaStream_t s);
+// Fills the home bins (once) for the staged contractions.
+int tile_bins_home(const int32_t *start, int64_t n, const GridParams &gp, TileBins &tb, cudaStream_t s);
 void tile_bins_free(TileBins &tb, cudaStream_t s);
 
 // grid[(r*3+c)][G] for r < nrhs, written completely (no zeroing needed).
