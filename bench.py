@@ -375,7 +375,7 @@ def roofline(w, st, inner="grad", inner_disc=None):
         avg_ms = cand[top] / cnt
     achieved = algo[top] / (avg_ms / 1e3) / 1e9
     kname = {"spread": "k_spread_grad_tiled" if inner == "grad" else "k_spread_tiled",
-             "contract": "k_contract_grad_warp" if inner == "grad" else "k_contract_tiled + gather",
+             "contract": "k_contract_grad_home" if inner == "grad" else "k_contract_tiled + gather",
              "scale": "k_scale_cs" if inner == "grad" else "k_scale_half"}.get(top, top)
     traffic = measured_traffic(kname, n, ngrid)
     return {"bound": "hbm", "kernel": f"{kname} (fp32, 3 vectors, {int(ngrid[0])}x{int(ngrid[1])}x{int(ngrid[2])} "
