@@ -317,9 +317,97 @@ int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrh
     return MPS_OK;
 }
 
-__global__ void k_to_f32(const double *__restrict__ m, int64_t total, float *__restrict__ mf) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
-        mf[i] = (float)m[i];
+// Float copy of the moments with each particle's nrhs x 3 components side by side (stride S floats, a multiple of
+// 4): the pair loop gathers a neighbour's block of vectors with 16-byte loads from one place instead of one
+// 4-byte load per vector and component from nrhs planes.
+__global__ void k_to_f32_rows(const double *__restrict__ m, int64_t n, int nrhs, int S, float *__restrict__ mf) {
+    const int64_t total = (int64_t)nrhs * n * 3;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / (n * 3), rem = t - r * n * 3;
+        const int64_t a = rem / 3;
+        const int c = (int)(rem - a * 3);
+        mf[a * S + r * 3 + c] = (float)m[t];
+    }
+}
+
+size_t m32_floats(int64_t n, int nrhs) { return (size_t)n * (size_t)((3 * nrhs + 3) & ~3); }
+
+// The float32 pair sum of k_rs_csr (same sums, same order) on the row copy of k_to_f32_rows: a neighbour's R
+// vectors are ceil(3R / 4) float4 loads at a 16-byte aligned offset (r0 is a multiple of 4 and S of 4, so
+// 3 r0 + 4 ceil(3R / 4) <= S: a read past the block's last component stays inside the particle's row).
+template <int G, int R>
+__global__ void __launch_bounds__(256) k_rs_csr_f32(const double *__restrict__ m, double *__restrict__ out, int64_t n,
+                                                    int nrhs, int r0, const int64_t *__restrict__ row_ptr,
+                                                    PairData<float> pd, const double *__restrict__ diag,
+                                                    const int32_t *__restrict__ diag_of_rhs,
+                                                    const double *__restrict__ slab, int accumulate,
+                                                    const float *__restrict__ mf, int S,
+                                                    const int32_t *__restrict__ order) {
+    constexpr int NQ = (3 * R + 3) / 4;   // float4 loads per neighbour
+    const int lane = threadIdx.x % G;
+    const int64_t grp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+    const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / G;
+    r0 += (int)blockIdx.y * R;
+    const int nr = min(R, nrhs - r0);
+    const float *mb0 = mf + 3 * r0;
+    for (int64_t i = grp; i < n; i += ngrp) {
+        const int64_t a = order ? (int64_t)order[i] : i;
+        float acc[R][3];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.f;
+        const int64_t e0 = row_ptr[a], e1 = row_ptr[a + 1];
+#pragma unroll 2
+        for (int64_t e = e0 + lane; e < e1; e += G) {
+            const int32_t b = pd.nbr[e];
+            const float av = pd.A[e], ba = pd.BA[e];
+            const float rx = pd.rx[e], ry = pd.ry[e], rz = pd.rz[e];
+            const float4 *q = reinterpret_cast<const float4 *>(mb0 + (int64_t)b * S);
+            float v[4 * NQ];
+#pragma unroll
+            for (int k = 0; k < NQ; ++k) {
+                const float4 t = __ldg(q + k);
+                v[4 * k] = t.x;
+                v[4 * k + 1] = t.y;
+                v[4 * k + 2] = t.z;
+                v[4 * k + 3] = t.w;
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (r < nr) {
+                    const float mx = v[3 * r], my = v[3 * r + 1], mz = v[3 * r + 2];
+                    const float s = ba * (mx * rx + my * ry + mz * rz);
+                    acc[r][0] += av * mx + s * rx;
+                    acc[r][1] += av * my + s * ry;
+                    acc[r][2] += av * mz + s * rz;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) acc[r][c] += __shfl_xor_sync(0xffffffffu, acc[r][c], o, G);
+        if (lane == 0) {
+            for (int r = 0; r < nr; ++r) {
+                const int rr = r0 + r;
+                const double dg = diag[(int64_t)(diag_of_rhs ? diag_of_rhs[rr] : 0) * n + a];
+                const double *ma = m + ((int64_t)rr * n + a) * 3;
+                double *o = out + ((int64_t)rr * n + a) * 3;
+                double v0 = dg * ma[0] + (double)acc[r][0];
+                double v1 = dg * ma[1] + (double)acc[r][1];
+                double v2 = dg * ma[2] + (double)acc[r][2] + slab[rr];
+                if (accumulate) {
+                    v0 += o[0];
+                    v1 += o[1];
+                    v2 += o[2];
+                }
+                o[0] = v0;
+                o[1] = v1;
+                o[2] = v2;
+            }
+        }
+    }
 }
 
 // Float32 pair sum on a float copy of the moments (converted once per matvec, not
@@ -328,33 +416,35 @@ __global__ void k_to_f32(const double *__restrict__ m, int64_t total, float *__r
 int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
                        PairData<float> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
                        bool accumulate, const int32_t *order, cudaStream_t s) {
-    k_to_f32<<<grid_for((int64_t)nrhs * n * 3, 256), 256, 0, s>>>(m, (int64_t)nrhs * n * 3, m32);
+    const int S = (3 * nrhs + 3) & ~3;
+    k_to_f32_rows<<<grid_for((int64_t)nrhs * n * 3, 256), 256, 0, s>>>(m, n, nrhs, S, m32);
     MPS_LAUNCH_CHECK();
     constexpr int G = 8;
     const unsigned grid = grid_for(n * G, 256, 152 * 64);
+    // blocks of 8 vectors, then one of 4, then the last 3, 2 or 1: every block starts at a multiple of 4
     for (int r0 = 0; r0 < nrhs;) {
         const int nr = nrhs - r0;
         if (nr >= 8) {
             // every full block of 8 vectors in one launch (grid y): small systems fill the GPU with all of them
             const int nb = nr / 8;
-            k_rs_csr<float, G, 8, float><<<dim3(grid, nb), 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag,
-                                                                        diag_of_rhs, slab, accumulate, m32, order);
+            k_rs_csr_f32<G, 8><<<dim3(grid, nb), 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
+                                                              slab, accumulate, m32, S, order);
             r0 += 8 * nb;
         } else if (nr >= 4) {
-            k_rs_csr<float, G, 4, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
-                                                              slab, accumulate, m32, order);
+            k_rs_csr_f32<G, 4><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                    accumulate, m32, S, order);
             r0 += 4;
         } else if (nr == 3) {
-            k_rs_csr<float, G, 3, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
-                                                              slab, accumulate, m32, order);
+            k_rs_csr_f32<G, 3><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                    accumulate, m32, S, order);
             r0 += 3;
         } else if (nr == 2) {
-            k_rs_csr<float, G, 2, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
-                                                              slab, accumulate, m32, order);
+            k_rs_csr_f32<G, 2><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                    accumulate, m32, S, order);
             r0 += 2;
         } else {
-            k_rs_csr<float, G, 1, float><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs,
-                                                              slab, accumulate, m32, order);
+            k_rs_csr_f32<G, 1><<<grid, 256, 0, s>>>(m, out, n, nrhs, r0, row_ptr, pd, diag, diag_of_rhs, slab,
+                                                    accumulate, m32, S, order);
             r0 += 1;
         }
         MPS_LAUNCH_CHECK();

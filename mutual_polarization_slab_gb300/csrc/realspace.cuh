@@ -13,7 +13,9 @@ int real_space_csr(const double *m, double *out, int64_t n, int nrhs, const int6
 int real_space_csr_df(const double *m, dfv *mdf, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
                       PairData<dfv> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
                       bool accumulate, const int32_t *order, cudaStream_t s);
-// Float32 pair sum on a float copy m32 (nrhs x n x 3, scratch) of the moments.
+// Float32 pair sum on a float copy m32 of the moments (scratch of m32_floats(n, nrhs) floats or more: per particle
+// its nrhs x 3 components side by side, padded to a multiple of 4).
+size_t m32_floats(int64_t n, int nrhs);
 int real_space_csr_f32(const double *m, float *m32, double *out, int64_t n, int nrhs, const int64_t *row_ptr,
                        PairData<float> pd, const double *diag, const int32_t *diag_of_rhs, const double *slab,
                        bool accumulate, const int32_t *order, cudaStream_t s);

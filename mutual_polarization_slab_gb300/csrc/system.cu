@@ -704,7 +704,7 @@ static bool df_usable(mps_system *s);
 
 // Float32 pair sum (accumulates into out) on the system's float copy of the moments.
 static int real_space_f32(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
-    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * 3 * (size_t)s->n * s->max_rhs, st));
+    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * m32_floats(s->n, s->max_rhs), st));
     return real_space_csr_f32(m, s->m32, out, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab, true,
                               s->order, st);
 }
@@ -942,7 +942,7 @@ static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t 
     // the real operator's vectors: 3 components per particle (complex systems run it on 2 nc real vectors)
     const size_t vals = (size_t)3 * s->n * s->max_rhs;
     if (!s->rs_buf) MPS_TRY(dalloc(&s->rs_buf, sizeof(double) * vals, st));
-    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * vals, st));
+    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * m32_floats(s->n, s->max_rhs), st));
     MPS_CUDA_TRY(cudaEventRecord(s->ev_fork, st));
     MPS_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
     MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab,
