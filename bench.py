@@ -399,9 +399,12 @@ def run_e2e(args, w, world):
     from mutual_polarization_slab_gb300.system import clear_kspace_cache
     n = w["n"]
     phi = 4.0 * math.pi * n / (3.0 * float(np.prod(w["box"])))
-    guess = gcap.dilute_guess(w["eps"], phi, [1.0, 0.0, 0.0])
-    xh = np.ascontiguousarray(w["x"])
-    eh = np.ascontiguousarray(w["eps"])
+    # the step's inputs in page-locked host memory (torch's pinned allocator), as a caller that streams
+    # configurations from the host would keep them
+    pinned = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    guess = pinned(gcap.dilute_guess(w["eps"], phi, [1.0, 0.0, 0.0]))
+    xh = pinned(w["x"])
+    eh = pinned(w["eps"])
 
     def call():
         C, S, info = gcap.capacitance_tensor(xh, eh, w["box"], guess, w["xi"], args.tol, rc=w["rc"],
@@ -424,10 +427,11 @@ def run_e2e(args, w, world):
         torch.cuda.synchronize()
         dt += time.perf_counter() - t0
     dt /= steps
-    h2d = xh.nbytes + eh.nbytes + guess.nbytes
+    # capacitance_tensor copies the positions, the permittivities and the guess's x column to the device
+    h2d = xh.nbytes + eh.nbytes + guess[:, 0].nbytes
     d2h = S.nbytes + C.nbytes
     return {"value": world * n * 3 / dt, "unit": UNIT, "ms_per_step": dt * 1e3, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "api": "capacitance.capacitance_tensor(numpy in, numpy out)"}
+            "d2h_bytes_per_step": int(d2h), "api": "capacitance.capacitance_tensor(numpy in from pinned host memory, numpy out)"}
 
 
 # ----------------------------------------------------------------------------- CPU legs (the oracle)

@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import ewald
-from .system import SpectralEwaldSystem, as_device, spectral_parameters
+from .system import SpectralEwaldSystem, as_device, spectral_parameters, to_host
 
 __all__ = ["gmres_restarted", "magnetic_dipole", "capacitance", "run_capacitance", "capacitance_tensor",
            "capacitance_tensor_spectrum", "dilute_guess", "default_table"]
@@ -149,7 +149,7 @@ def gmres_restarted(matvec: Callable, b, x0, tol: float, restart: int, maxit: in
 
 
 def _np_or_t(t, asnp):
-    return t.cpu().numpy() if asnp else t
+    return to_host(t) if asnp else t
 
 
 def _inner(precision, inner_operator, inner_grid):
@@ -261,6 +261,23 @@ def run_capacitance(x, box, eps_p, xi, H0, errortol=1e-5, slab_factor=1.0, use_s
     return C, p
 
 
+_UNIT_FIELDS: dict = {}
+
+
+def _unit_fields(N):
+    """(3, N, 3) unit fields along x, y, z on the current device, kept per (N, device): the solves only read
+    their right-hand sides, and building them is several launches per call."""
+    key = (int(N), torch.cuda.current_device())
+    b = _UNIT_FIELDS.get(key)
+    if b is None:
+        if len(_UNIT_FIELDS) >= 8:
+            _UNIT_FIELDS.clear()
+        b = torch.zeros((3, int(N), 3), dtype=torch.float64, device="cuda")
+        b.diagonal(dim1=0, dim2=2).fill_(1.0)
+        _UNIT_FIELDS[key] = b
+    return b
+
+
 def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None, dipoletable2=None, rtable=None,
                        offset=None, offsetxyz=None, *, slab_factor=0.0, rc=None, Ngrid=None, P=None, restart=None,
                        maxit=None, precision="fp64", inner_tol=1e-4, inner_maxit=4, batched=True, system=None,
@@ -289,20 +306,22 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
                                          inner=_inner(precision, inner_operator, inner_grid))
     restart = min(3 * N, 10) if restart is None else int(restart)
     maxit = min(3 * N, 100) if maxit is None else int(maxit)
-    g0 = as_device(np.real(Sguess) if not isinstance(Sguess, torch.Tensor) else Sguess.real).reshape(N, 3)
-    eye = torch.eye(3, dtype=torch.float64, device="cuda")
     infos = []
     if batched:
-        b = eye[:, None, :].expand(3, N, 3).contiguous()
-        # dilute-type guess along each axis: amplitude of the given guess projected on x, rotated
-        amp = g0[:, 0:1]
-        x0 = torch.stack([amp * eye[i] for i in range(3)]).contiguous()
+        b = _unit_fields(N)
+        # dilute-type guess along each axis: amplitude of the given guess projected on x, rotated (only that
+        # column goes to the device); x0[i, :, i] = amplitude
+        g0x = Sguess.real.reshape(N, 3)[:, 0] if isinstance(Sguess, torch.Tensor) else \
+            np.real(np.asarray(Sguess)).reshape(N, 3)[:, 0]
+        x0 = torch.zeros((3, N, 3), dtype=torch.float64, device="cuda")
+        x0.diagonal(dim1=0, dim2=2).copy_(as_device(g0x).reshape(N, 1))
         S3, infos = sysm.solve(b, x0, tol=float(errortol), restart=restart, maxit=maxit, precision=precision,
                                inner_tol=inner_tol, inner_maxit=inner_maxit, residual_precision=residual_precision,
                                inner_operator=inner_operator)
     else:
+        eye = torch.eye(3, dtype=torch.float64, device="cuda")
         sols = []
-        guess = g0
+        guess = as_device(np.real(Sguess) if not isinstance(Sguess, torch.Tensor) else Sguess.real).reshape(N, 3)
         for i in range(3):
             b = eye[i].repeat(N, 1)
             Si, inf = sysm.solve(b, guess, tol=float(errortol), restart=restart, maxit=maxit, precision=precision,
@@ -317,7 +336,7 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
     if system is None:
         sysm.close()
     if asnp:
-        return Cm.cpu().numpy(), S.cpu().numpy(), infos
+        return to_host(Cm), to_host(S), infos
     return Cm, S, infos
 
 

@@ -27,6 +27,18 @@ def as_device(a, dtype=torch.float64) -> torch.Tensor:
     return torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dtype, device="cuda")
 
 
+def to_host(t: torch.Tensor) -> np.ndarray:
+    """NumPy copy of a device tensor in page-locked host memory (torch's caching
+    host allocator: the block returns to its cache when the array is dropped), so
+    the device-to-host copy runs at the link's DMA rate instead of through a
+    pageable staging buffer."""
+    if t.is_cuda:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t)
+        return h.numpy()
+    return t.numpy()
+
+
 def clear_kspace_cache():
     """Drop the process's cached Green's coefficients and scale tensors (shared by
     systems built on the same device, grid, box, xi and eta), so the next system
