@@ -1073,18 +1073,15 @@ int positions_f32(const double *x, int64_t n, float *xf, unsigned *maxbits, doub
 }
 
 int csr_pairs_count(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
-                    int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *total_host, cudaStream_t s) {
+                    int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *last2, cudaStream_t s) {
     int64_t n = cb.n;
     k_csr_count<<<grid_for(n * 32, 256, 152 * 64), 256, 0, s>>>(x, xf, make_screen(box, rc, maxabs), cb.sorted, cb.lin, cb.counts,
                                                       cb.starts, n, cb.ncell[0], cb.ncell[1], cb.ncell[2], cnt27);
     MPS_LAUNCH_CHECK();
     int r = exclusive_scan_i64(cnt27, off27, 27 * n, scan_tmp, s);
     if (r) return r;
-    int64_t last[2];
-    MPS_CUDA_TRY(cudaMemcpyAsync(&last[0], off27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaMemcpyAsync(&last[1], cnt27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_TRY(cudaStreamSynchronize(s));
-    *total_host = last[0] + last[1];
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last2[0], off27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_TRY(cudaMemcpyAsync(&last2[1], cnt27 + 27 * n - 1, 8, cudaMemcpyDeviceToHost, s));
     return MPS_OK;
 }
 

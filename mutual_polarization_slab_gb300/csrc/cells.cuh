@@ -34,8 +34,10 @@ size_t cell_bins_bytes(int64_t n, int64_t ncells);
 int cell_assign(const double *x, int64_t n, const double *box, const int64_t *ncell, int64_t *cell3, cudaStream_t s);
 int cell_bins_build(const int64_t *cell3, int64_t n, const int64_t *ncell, void *ws, CellBins &cb, cudaStream_t s);
 int positions_f32(const double *x, int64_t n, float *xf, unsigned *maxbits, double *maxabs, cudaStream_t s);
+// Enqueues the pair count on s and the copies of the last offset and count into last2 (two int64 in page-locked
+// host memory): once s is synchronised the number of pairs is last2[0] + last2[1].
 int csr_pairs_count(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
-                    int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *total_host, cudaStream_t s);
+                    int64_t *cnt27, int64_t *off27, void *scan_tmp, int64_t *last2, cudaStream_t s);
 int csr_pairs_fill(const double *x, const float *xf, double maxabs, const double *box, double rc, const CellBins &cb,
                    const int64_t *cnt27,
                    const int64_t *off27, const double *perp, const double *para, const double *rv, int64_t ntab,

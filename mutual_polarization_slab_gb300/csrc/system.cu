@@ -2349,8 +2349,7 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
             cudaStreamWaitEvent(s->side, s->ev_fork, 0) != cudaSuccess ||
             cudaStreamWaitEvent(s->cap, s->ev_fork, 0) != cudaSuccess)
             CR_TRY(MPS_CUDA_ERR);
-        CR_TRY(setup_grids(s, d, s->side));
-        CR_TRY(setup_inner_grid(s, d, s->cap));   // the system's capture stream, idle until its first solve
+        // setup_grids / setup_inner_grid are enqueued below, while the GPU counts the pairs
     }
     // cell list + pair CSR
     compute_ncell(d->box, d->rc, s->ncell);
@@ -2389,7 +2388,15 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     if (!rc) s->gp.order = s->order;
     int64_t np = 0;
     if (!rc) rc = positions_f32(s->x, n, xf, maxbits, &maxabs, st);
-    if (!rc) rc = csr_pairs_count(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, scan_tmp, &np, st);
+    int64_t *last2 = reinterpret_cast<int64_t *>(s->host_scr);   // page-locked, free until the first solve
+    if (!rc) rc = csr_pairs_count(s->x, xf, maxabs, d->box, d->rc, cb, cnt27, off27, scan_tmp, last2, st);
+    // the grid geometry and k-space (side stream) and the inner grid (the capture stream, idle until the first
+    // solve) are enqueued while the GPU runs the count: their host work (allocations, cache lookups, launches)
+    // no longer delays the pair list, the longest chain of the build
+    if (!rc && grids_on_side) rc = setup_grids(s, d, s->side);
+    if (!rc && grids_on_side) rc = setup_inner_grid(s, d, s->cap);
+    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (!rc) np = last2[0] + last2[1];
     if (rc) {
         tmp_free();
         free_system(s);
