@@ -1086,23 +1086,29 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
 
 // The gradient-form operator on the inner grid: the same stages as matvec_grad with the inner grid's geometry,
 // tiles, grids, Green's coefficient and FFT plans (its tiles, weights and factors are built with the system).
+// The inner grid's gradient-form scale coefficient H / |k|^2, from the process cache or computed on stream st.
+static int inner_hs32(mps_system *s, cudaStream_t st) {
+    InnerGrid &ig = *s->inner;
+    if (ig.hs32_ready) return MPS_OK;
+    std::lock_guard<std::mutex> lk(g_green_mu);
+    if (!ig.green->hs32) {
+        float *hs = nullptr;
+        MPS_TRY(dalloc_persistent(&hs, sizeof(float) * ig.Gc));
+        MPS_TRY(grad_scale_coef(ig.gp, ig.green->h64, hs, st));
+        MPS_TRY(green_mark_filled(&ig.green->ev_hs32, st));
+        ig.green->hs32 = hs;
+    } else {
+        MPS_CUDA_TRY(cudaStreamWaitEvent(st, ig.green->ev_hs32, 0));   // filled by another system
+    }
+    ig.hs32_ready = true;
+    return MPS_OK;
+}
+
 static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     InnerGrid &ig = *s->inner;
     if (!ig.grid) MPS_TRY(dalloc(&ig.grid, (size_t)s->max_rhs * ig.gp.G * sizeof(float), st));
     if (!ig.spec) MPS_TRY(dalloc(&ig.spec, (size_t)s->max_rhs * ig.Gc * 2 * sizeof(float), st));
-    if (!ig.hs32_ready) {
-        std::lock_guard<std::mutex> lk(g_green_mu);
-        if (!ig.green->hs32) {
-            float *hs = nullptr;
-            MPS_TRY(dalloc_persistent(&hs, sizeof(float) * ig.Gc));
-            MPS_TRY(grad_scale_coef(ig.gp, ig.green->h64, hs, st));
-            MPS_TRY(green_mark_filled(&ig.green->ev_hs32, st));
-            ig.green->hs32 = hs;
-        } else {
-            MPS_CUDA_TRY(cudaStreamWaitEvent(st, ig.green->ev_hs32, 0));   // filled by another system
-        }
-        ig.hs32_ready = true;
-    }
+    MPS_TRY(inner_hs32(s, st));
     const double vol = s->box[0] * s->box[1] * s->box[2];
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
@@ -2258,6 +2264,8 @@ static int setup_inner_grid(mps_system *s, const mps_system_desc *d, cudaStream_
         GS_TRY(tile_bins_build(ig.start, n, ig.gp, tz_in, ig.tb, gs));
         if (contract_grad_home_supported(ig.gp)) GS_TRY(tile_bins_home(ig.start, n, ig.gp, ig.tb, gs));
         GS_TRY(acquire_green(ig.gp, d->box, d->xi, ig.Gc, ig.green, gs));
+        // the inner operator's scale coefficient too: the first inner matvec then finds it ready
+        GS_TRY(inner_hs32(s, gs));
     }
 #undef GS_TRY
     return MPS_OK;

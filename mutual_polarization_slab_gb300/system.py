@@ -20,11 +20,24 @@ PRECISIONS = {"fp64": L.MPS_FP64, "fp32": L.MPS_FP32, "mixed": L.MPS_FP32, "df":
               "fp32grad": L.MPS_FP32_GRAD}
 
 
+_NP_TYPES = {torch.float64: np.dtype(np.float64), torch.float32: np.dtype(np.float32),
+             torch.complex128: np.dtype(np.complex128), torch.int32: np.dtype(np.int32),
+             torch.int64: np.dtype(np.int64)}
+
+
 def as_device(a, dtype=torch.float64) -> torch.Tensor:
-    """Contiguous CUDA tensor view/copy of a numpy array or tensor."""
+    """Contiguous CUDA tensor view/copy of a numpy array or tensor.  A contiguous
+    numpy array of the target type in page-locked memory is copied without
+    blocking the host (in the order of the current stream; the caller's array
+    outlives the copy, which every later use on that stream follows)."""
     if isinstance(a, torch.Tensor):
         return a.to(device="cuda", dtype=dtype).contiguous()
-    return torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dtype, device="cuda")
+    arr = np.asarray(a)
+    if arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == _NP_TYPES.get(dtype):
+        t = torch.from_numpy(arr)
+        if t.is_pinned():
+            return t.to(device="cuda", non_blocking=True)
+    return torch.as_tensor(np.ascontiguousarray(arr), dtype=dtype, device="cuda")
 
 
 def to_host(t: torch.Tensor) -> np.ndarray:
