@@ -265,7 +265,13 @@ enum mps_operator_kind { MPS_DIPOLE = 0, MPS_DIPOLE_QUADRUPOLE = 1, MPS_POLYDISP
 
 /* Builds cell list, filtered CSR pair list with interpolated couplings, grid
  * geometry, Green's coefficients and FFT plans (EW/capacitance.py:369-385).
- * Allocates device memory; synchronises once (pair count). */
+ * Allocates device memory; synchronises on the positions' range and the pair
+ * count.  A pair separation outside the real-space table is MPS_TABLE_RANGE:
+ * returned here for kinds MPS_DIPOLE_QUADRUPOLE and MPS_POLYDISPERSE; for
+ * MPS_DIPOLE the check completes on the stream after this call returns (the
+ * GPU is still filling the pair list) and the first mps_matvec,
+ * mps_matvec_complex, mps_adjoint_forces or mps_gmres call (and every later
+ * one) returns it instead. */
 int mps_system_create(const mps_system_desc *desc, mps_system **out, mps_stream_t stream);
 void mps_system_destroy(mps_system *sys);
 

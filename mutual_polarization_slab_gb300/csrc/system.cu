@@ -234,6 +234,10 @@ struct mps_system {
     cudaEvent_t ev_graph = nullptr;  // recorded after each graph launch (destroying the graphs waits on it)
     std::vector<std::pair<int, int>> mv_seen;   // (precision, batch width) of the matvecs run so far
     int32_t *host_step = nullptr;    // pinned: the step counter read back after a graph launch
+    int32_t *host_herr = nullptr;    // pinned: the pair fill's table-range flag (dipole systems)
+    cudaEvent_t ev_build = nullptr;  // recorded after that flag's copy at the end of the build
+    bool build_check = false;        // the flag has not been read yet (build_status)
+    bool build_failed = false;       // it was set: every later call returns MPS_TABLE_RANGE
 };
 
 // Pinned host blocks of destroyed systems, kept for the next system (cudaMallocHost and cudaFreeHost cost a
@@ -307,6 +311,7 @@ static void free_system(mps_system *s) {
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->ev_res) cudaEventDestroy(s->ev_res);
     if (s->ev_diag) cudaEventDestroy(s->ev_diag);
+    if (s->ev_build) cudaEventDestroy(s->ev_build);
     if (s->ev_graph) {
         cudaEventSynchronize(s->ev_graph);
         cudaEventDestroy(s->ev_graph);
@@ -2338,12 +2343,13 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
     CR_TRY(dalloc(&s->diag_idx, sizeof(int32_t) * s->max_rhs, st));
     {
         const size_t ints = ((size_t)2 * s->max_rhs + 1) & ~(size_t)1;   // even: the doubles stay 8-byte aligned
-        const size_t pinned = sizeof(int32_t) * ints + sizeof(double) * (6 * s->max_rhs + 1);
+        const size_t pinned = sizeof(int32_t) * ints + sizeof(double) * (6 * s->max_rhs + 2);
         s->diag_idx_host = static_cast<int32_t *>(pinned_take(pinned));
         if (!s->diag_idx_host) CR_TRY(MPS_NO_MEMORY);
         s->host_frozen = s->diag_idx_host + s->max_rhs;
         s->host_scr = reinterpret_cast<double *>(s->diag_idx_host + ints);
         s->host_step = reinterpret_cast<int32_t *>(s->host_scr + 6 * s->max_rhs);
+        s->host_herr = reinterpret_cast<int32_t *>(s->host_scr + 6 * s->max_rhs + 1);
     }
     if (cudaMemsetAsync(s->diag_idx, 0, sizeof(int32_t) * s->max_rhs, st) != cudaSuccess) CR_TRY(MPS_CUDA_ERR);
     // grids and k-space on the side stream, beside the pair list below (joined before returning)
@@ -2459,8 +2465,20 @@ extern "C" int mps_system_create(const mps_system_desc *d, mps_system **out, mps
                             s->row_ptr, s->p64, s->p32, err, st);
     }
     int herr = 0;
-    if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = MPS_CUDA_ERR;
-    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    if (s->kind == MPS_DIPOLE) {
+        // The table-range flag is read by the first call that uses the system (build_status), not here: the
+        // host goes on to the caller's first solve while the GPU still fills the pair list.
+        if (!rc && cudaMemcpyAsync(s->host_herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = MPS_CUDA_ERR;
+        if (!rc && (cudaEventCreateWithFlags(&s->ev_build, cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventRecord(s->ev_build, st) != cudaSuccess))
+            rc = MPS_CUDA_ERR;
+        if (!rc) s->build_check = true;
+    } else {
+        if (!rc && cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = MPS_CUDA_ERR;
+        if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = MPS_CUDA_ERR;
+    }
     tmp_free();
     if (!rc && herr) rc = MPS_TABLE_RANGE;
     if (!rc && s->kind == MPS_POLYDISPERSE) {
@@ -2542,6 +2560,16 @@ extern "C" void mps_system_destroy(mps_system *sys) {
     free_system(sys);
 }
 
+// The result of the build's table-range check (MPS_TABLE_RANGE when a pair separation fell outside the
+// real-space table), read once the build's copy of the flag has completed.
+static int build_status(mps_system *s) {
+    if (!s->build_check) return s->build_failed ? MPS_TABLE_RANGE : MPS_OK;
+    MPS_CUDA_TRY(cudaEventSynchronize(s->ev_build));
+    s->build_check = false;
+    if (*s->host_herr) s->build_failed = true;
+    return s->build_failed ? MPS_TABLE_RANGE : MPS_OK;
+}
+
 extern "C" int mps_system_info(const mps_system *sys, int64_t *n_pairs, int64_t *ncell) {
     if (!sys) return MPS_BAD_ARG;
     if (n_pairs) *n_pairs = sys->n_pairs;
@@ -2557,6 +2585,7 @@ extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t
     if (!sys || !m || !out || nrhs < 1 || nrhs > rhs_limit(sys)) return MPS_BAD_ARG;
     if (precision != MPS_FP64 && precision != MPS_FP32 && precision != MPS_DF && precision != MPS_FP32_GRAD)
         return MPS_BAD_ARG;
+    MPS_TRY(build_status(sys));
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     return matvec_any(sys, m, out, nrhs, precision, st);
@@ -2565,6 +2594,7 @@ extern "C" int mps_matvec(mps_system *sys, const double *m, double *out, int32_t
 extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *out_ri, int32_t diag_index,
                                   mps_stream_t stream) {
     if (!sys || !m_ri || !out_ri || sys->max_rhs < 2 || sys->kind != MPS_DIPOLE || sys->cplx) return MPS_BAD_ARG;
+    MPS_TRY(build_status(sys));
     cudaStream_t st = (cudaStream_t)stream;
     int32_t di[2] = {diag_index, diag_index};
     MPS_TRY(upload_diag_idx(sys, di, 2, st));
@@ -2623,7 +2653,9 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
             info[q].matvecs_fp32 = mv32;
         }
     }
-    return rc;
+    // the build's table-range check, read after the solve (which the pair fill preceded on the stream)
+    const int bs = build_status(sys);
+    return bs != MPS_OK ? bs : rc;
 }
 
 extern "C" int mps_system_profile(mps_system *sys, int32_t enable) {
@@ -2948,6 +2980,7 @@ extern "C" int mps_adjoint_forces(mps_system *sys, const double *m, const double
     if (!sys || !m || !perp || !para || !rvals || n_tab < 2 || !forces) return MPS_BAD_ARG;
     if (sys->kind != MPS_DIPOLE || sys->cplx) return MPS_BAD_ARG;
     if (diag_index < 0 || diag_index >= sys->n_diag) return MPS_BAD_ARG;
+    MPS_TRY(build_status(sys));
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(ensure_p64(sys, st));
     const int64_t n = sys->n;

@@ -99,6 +99,29 @@ def test_table_range_error():
         gew.prepare_real_space_pairs(x, box, np.array([0, 1]), np.array([1, 0]), 3.0, perp[1:], para[1:], rv[1:])
 
 
+def test_system_table_range_reported_by_first_use():
+    """A dipole system whose pair list holds a separation below the table's
+    first entry builds (its table-range check completes on the stream after
+    mps_system_create returns) and every call that uses it raises: a matvec, a
+    solve (after it ran) and the calls after them."""
+    x = np.array([[1.0, 1.0, 1.0], [1.0005, 1.0, 1.0], [5.0, 5.0, 5.0]])
+    box = np.array([10.0, 10.0, 10.0])
+    perp, para, rv = ew.default_table(0.5)
+    s = SpectralEwaldSystem(x, np.full(3, 4.0), box, 0.5, 3.0, [16, 16, 16], 6, perp[1:], para[1:], rv[1:],
+                            max_rhs=1)
+    m = np.ones((3, 3))
+    with pytest.raises(ValueError):
+        s.matvec(m, precision="fp64")
+    with pytest.raises(ValueError):
+        s.solve(m, None, tol=1e-6, restart=5, maxit=2, precision="fp64")
+    s.close()
+    s = SpectralEwaldSystem(x, np.full(3, 4.0), box, 0.5, 3.0, [16, 16, 16], 6, perp[1:], para[1:], rv[1:],
+                            max_rhs=1)
+    with pytest.raises(ValueError):
+        s.solve(m, None, tol=1e-6, restart=5, maxit=2, precision="fp64")
+    s.close()
+
+
 def test_rc_greater_than_half_box_raises():
     x, box, _ = rsa(20, 0.1, seed=2)
     perp, para, rv = ew.default_table(0.5)
