@@ -332,11 +332,30 @@ __global__ void __launch_bounds__(256, MB) k_spread_cs(const double *__restrict_
 }
 
 template <typename T>
+struct CsCplx;
+template <>
+struct CsCplx<float> {
+    using type = float2;
+};
+template <>
+struct CsCplx<double> {
+    using type = double2;
+};
+
+// spec[r][k] *= coef[k]: one thread per spectrum point reads its coefficient once for every vector, with one
+// complex (8 or 16 byte) load and store per value.
+template <typename T>
 __global__ void k_scale_cs(T *__restrict__ spec, int nrhs, int64_t Gc, const T *__restrict__ coef) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc * nrhs; t += (int64_t)gridDim.x * blockDim.x) {
-        const T c = coef[t % Gc];
-        spec[2 * t] *= c;
-        spec[2 * t + 1] *= c;
+    using C = typename CsCplx<T>::type;
+    C *sp = reinterpret_cast<C *>(spec);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Gc; t += (int64_t)gridDim.x * blockDim.x) {
+        const T c = coef[t];
+        for (int r = 0; r < nrhs; ++r) {
+            C v = sp[(int64_t)r * Gc + t];
+            v.x *= c;
+            v.y *= c;
+            sp[(int64_t)r * Gc + t] = v;
+        }
     }
 }
 
@@ -469,7 +488,7 @@ int spread_cs(const double *m, int64_t n, int nrhs, const int32_t *start, const 
 template <typename T>
 int scale_cs(void *spec, int nrhs, const GridParams &gp, const T *coef, cudaStream_t s) {
     const int64_t Gc = (int64_t)(gp.N[0] / 2 + 1) * gp.N[1] * gp.N[2];
-    k_scale_cs<T><<<grid_for(Gc * nrhs, 256), 256, 0, s>>>((T *)spec, nrhs, Gc, coef);
+    k_scale_cs<T><<<grid_for(Gc, 256), 256, 0, s>>>((T *)spec, nrhs, Gc, coef);
     MPS_LAUNCH_CHECK();
     return MPS_OK;
 }
