@@ -299,7 +299,7 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
     rc, Ngrid, h, P, eta = _resolve_params(box, xi, errortol, rc, Ngrid, P)
     if dipoletable1 is None:
         dipoletable1, dipoletable2, rtable = default_table(xi)
-    xd = as_device(x).reshape(-1, 3)
+    xd = as_device(x, non_blocking=system is None).reshape(-1, 3)   # the system's creation synchronises
     N = xd.shape[0]
     sysm = system or SpectralEwaldSystem(xd, lambdap, box, xi, rc, Ngrid, P, dipoletable1, dipoletable2, rtable,
                                          slab_factor=slab_factor, eta=eta, max_rhs=3,
@@ -314,7 +314,7 @@ def capacitance_tensor(x, lambdap, box, Sguess, xi, errortol, dipoletable1=None,
         g0x = Sguess.real.reshape(N, 3)[:, 0] if isinstance(Sguess, torch.Tensor) else \
             np.real(np.asarray(Sguess)).reshape(N, 3)[:, 0]
         x0 = torch.zeros((3, N, 3), dtype=torch.float64, device="cuda")
-        x0.diagonal(dim1=0, dim2=2).copy_(as_device(g0x).reshape(N, 1))
+        x0.diagonal(dim1=0, dim2=2).copy_(as_device(g0x, non_blocking=True).reshape(N, 1))   # the solve syncs
         S3, infos = sysm.solve(b, x0, tol=float(errortol), restart=restart, maxit=maxit, precision=precision,
                                inner_tol=inner_tol, inner_maxit=inner_maxit, residual_precision=residual_precision,
                                inner_operator=inner_operator)

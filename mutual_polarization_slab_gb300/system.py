@@ -25,15 +25,16 @@ _NP_TYPES = {torch.float64: np.dtype(np.float64), torch.float32: np.dtype(np.flo
              torch.int64: np.dtype(np.int64)}
 
 
-def as_device(a, dtype=torch.float64) -> torch.Tensor:
-    """Contiguous CUDA tensor view/copy of a numpy array or tensor.  A contiguous
-    numpy array of the target type in page-locked memory is copied without
-    blocking the host (in the order of the current stream; the caller's array
-    outlives the copy, which every later use on that stream follows)."""
+def as_device(a, dtype=torch.float64, non_blocking=False) -> torch.Tensor:
+    """Contiguous CUDA tensor view/copy of a numpy array or tensor.  With
+    ``non_blocking`` a contiguous numpy array of the target type in page-locked
+    memory is copied without blocking the host, in the order of the current
+    stream: only for callers that synchronise that stream before they return
+    (system creation, solves), so the caller's array cannot change under the copy."""
     if isinstance(a, torch.Tensor):
         return a.to(device="cuda", dtype=dtype).contiguous()
     arr = np.asarray(a)
-    if arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == _NP_TYPES.get(dtype):
+    if non_blocking and arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == _NP_TYPES.get(dtype):
         t = torch.from_numpy(arr)
         if t.is_pinned():
             return t.to(device="cuda", non_blocking=True)
@@ -171,7 +172,7 @@ class SpectralEwaldSystem:
         lib = L.lib()
         self._lib = lib
         self._h = C.c_void_p(0)
-        self.x = as_device(x).reshape(-1, 3)
+        self.x = as_device(x, non_blocking=True).reshape(-1, 3)
         # complex permittivities (frequency-dependent eps, as the MATLAB spectrum drivers allow): vectors become
         # complex; the device stores them as (Re m, Im m) per particle
         self.cplx = bool(torch.is_complex(lambdap)) if isinstance(lambdap, torch.Tensor) else \
@@ -184,7 +185,7 @@ class SpectralEwaldSystem:
             lam = lc.real.contiguous()
             self.lambdap_imag = lc.imag.contiguous()
         else:
-            lam = as_device(lambdap)
+            lam = as_device(lambdap, non_blocking=True)
             if lam.dim() == 1:
                 lam = lam.reshape(1, -1)
             self.lambdap_imag = None
@@ -393,7 +394,7 @@ class SpectralEwaldSystem:
         ``b``, ``x0``: (N,ndof) or (R,N,ndof); complex (N,3) / (R,N,3) with complex
         permittivities.  Returns (x, [SolveInfo] * R)."""
         nd = 6 if self.cplx else self.ndof
-        b = self._pack(b) if self.cplx else as_device(b)
+        b = self._pack(b) if self.cplx else as_device(b, non_blocking=True)
         single = b.dim() == 2
         b = b.reshape(-1, self.n, nd).contiguous()
         nrhs = b.shape[0]
@@ -401,7 +402,8 @@ class SpectralEwaldSystem:
         if x0 is None:
             x0d = None
         else:
-            x0d = (self._pack(x0) if self.cplx else as_device(x0)).reshape(nrhs, self.n, nd).contiguous()
+            x0d = (self._pack(x0) if self.cplx else as_device(x0, non_blocking=True)).reshape(nrhs, self.n,
+                                                                                             nd).contiguous()
         opts = L.SolveOpts(tol=float(tol), restart=int(restart), maxit=int(maxit),
                            precision=PRECISIONS[precision], inner_tol=float(inner_tol), inner_maxit=int(inner_maxit),
                            residual_policy=int(residual_policy), verify=1 if verify else 0,
