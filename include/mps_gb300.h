@@ -64,6 +64,7 @@ enum mps_precision {
 };
 
 const char *mps_status_string(int status);
+/* 5: adds mps_batch_item and mps_solve_batched (4: the inner-grid fields of mps_system_desc). */
 int mps_abi_version(void);
 
 /* ------------------------------------------------------------------------- */
@@ -327,6 +328,32 @@ typedef struct mps_solve_info {
 int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
               const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
               mps_stream_t stream);
+
+/* One configuration of a many-configuration solve (mps_solve_batched). */
+typedef struct mps_batch_item {
+    mps_system_desc desc;       /* the configuration, as for mps_system_create     */
+    const double *b;            /* device nrhs x n x ndof right-hand sides          */
+    const double *x0;           /* device nrhs x n x ndof guesses, or NULL (zero)   */
+    double *x;                  /* device nrhs x n x ndof solutions (not aliasing b) */
+    int32_t nrhs;               /* 1 .. desc.max_rhs                                */
+    const int32_t *diag_index;  /* host int32[nrhs]: permittivity set of each       */
+                                /* right-hand side, or NULL (set 0)                 */
+    mps_solve_info *info;       /* host nrhs results, or NULL                       */
+    int32_t status;             /* out: this configuration's status                 */
+} mps_batch_item;
+
+/* Replaces the loop over configurations of the spectrum drivers (the parfor of
+ * CH/CapacitanceTensorSpectrum.m:45 and CS/CapacitanceTensorSpectrum.m:44, each
+ * iteration a CapacitanceTensor call): every item is built (mps_system_create),
+ * solved (mps_gmres with opts) and released, n_streams configurations at a time,
+ * each worker on a host thread and CUDA stream of its own, largest (n x nrhs)
+ * first.  The work is ordered after what `stream` holds at the call (the
+ * inputs); the call returns once every solution has been written.  Each item
+ * gets its own status.  Returns MPS_OK when all are MPS_OK, otherwise the
+ * status of the first item (in array order) that failed with an error, else
+ * MPS_NOT_CONVERGED.  n_streams is capped at 32. */
+int mps_solve_batched(mps_batch_item *items, int32_t n_items, const mps_solve_opts *opts, int32_t n_streams,
+                      mps_stream_t stream);
 
 /* ------------------------------------------------------------------------- */
 /* Adjoint forces (no counterpart in the reference, which computes forces from */

@@ -77,7 +77,7 @@ def build(verbose: bool = False, extra_flags=None) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "shared", "-lcufft"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "shared", "-lcufft", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

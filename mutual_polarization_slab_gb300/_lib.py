@@ -28,7 +28,7 @@ EXPORTS = (
     "mps_system_stage_times", "mps_neighbor_list_noalloc", "mps_system_tuning", "mps_system_graphs",
     "mps_dipole_forces", "mps_quad_table", "mps_sizes_table", "mps_adjoint_forces",
     "mps_real_space_table_probe", "mps_field_map", "mps_quad_table_probe", "mps_field_map_quad",
-    "mps_field_map_sizes", "mps_kspace_cache_clear",
+    "mps_field_map_sizes", "mps_kspace_cache_clear", "mps_solve_batched",
 )
 
 p = C.c_void_p
@@ -61,6 +61,11 @@ class SolveInfo(C.Structure):
                 ("relres", f64)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("desc", SystemDesc), ("b", p), ("x0", p), ("x", p), ("nrhs", i32), ("diag_index", C.POINTER(i32)),
+                ("info", C.POINTER(SolveInfo)), ("status", i32)]
+
+
 _SIGS = {
     "mps_status_string": (C.c_char_p, [C.c_int]),
     "mps_abi_version": (C.c_int, []),
@@ -85,6 +90,7 @@ _SIGS = {
     "mps_matvec": (C.c_int, [p, p, p, i32, C.POINTER(i32), i32, p]),
     "mps_matvec_complex": (C.c_int, [p, p, p, i32, p]),
     "mps_gmres": (C.c_int, [p, p, p, p, i32, C.POINTER(i32), C.POINTER(SolveOpts), C.POINTER(SolveInfo), p]),
+    "mps_solve_batched": (C.c_int, [C.POINTER(BatchItem), i32, C.POINTER(SolveOpts), i32, p]),
     "mps_kernel_launches": (C.c_uint64, []),
     "mps_system_profile": (C.c_int, [p, i32]),
     "mps_system_stage_times": (C.c_int, [p, PD, P64]),

@@ -23,7 +23,8 @@ import numpy as np
 
 from .system import fft_size  # noqa: F401  (part of this module's interface)
 
-__all__ = ["Configuration", "make_configurations", "partition", "solve_configuration", "solve_configurations"]
+__all__ = ["Configuration", "make_configurations", "partition", "solve_configuration", "solve_configurations",
+           "solve_batched"]
 
 
 @dataclass
@@ -98,18 +99,11 @@ def grid_for(box, xi, tol, fft_friendly=True):
     return ng, int(math.ceil(2 / hm - 2 * math.log(tol) / math.pi))
 
 
-def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None,
-                        fft_friendly=True, return_moments=False, solver_tol=None):
-    """C (K, 3, 3) (row i = mean dipole for the unit field along i) of one
-    configuration for every contrast scaling, all 3K solves in one batch.
-    ``tol`` sets the spectral parameters (cutoff, grid, support) and, unless
-    ``solver_tol`` is given, the GMRES tolerance too.  Returns (C, converged), or
-    (C, converged, moments (3K, N, 3) on the device) with ``return_moments``."""
+def _configuration_inputs(cfg: Configuration, s, tol, xi, fft_friendly):
+    """Spectral parameters, permittivity sets, right-hand sides, guesses and permittivity-set indices of one
+    configuration's 3K solves: (xi, Ngrid, P, eps_sets (K, N), b, x0 (3K, N, 3) on the device, diag_index)."""
     import torch
 
-    from .sizes import PolydisperseSystem, spectral_parameters
-
-    s = np.asarray(scalings, dtype=np.float64).reshape(-1)
     K = s.size
     box = np.asarray(cfg.box, dtype=np.float64).reshape(3)
     lt = math.sqrt(-math.log(tol))
@@ -121,18 +115,34 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
     eps_sets = np.stack([_eps(cfg.beta * sk) for sk in s])           # (K, N)
     n = cfg.n
     ng, P = grid_for(box, xi, tol, fft_friendly)
-    sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, box, xi, tol, Ngrid=ng, P=P, max_rhs=3 * K)
+    # right-hand side 3k + i: unit field along i with contrast scaling k; guess 4 pi a^3 beta / (1 - beta phi)
+    # along the field (CS/CapacitanceTensorSpectrum.m:45-48), built in a few tensor operations (one
+    # assignment per right-hand side costs more host time than a small configuration's solve)
+    phi_v = 4 * math.pi * float(np.sum(cfg.radii ** 3)) / (3 * float(np.prod(box)))
+    beta = s[:, None] * np.asarray(cfg.beta, dtype=np.float64)[None, :]                  # (K, N)
+    amp = torch.as_tensor(4 * math.pi * cfg.radii[None, :] ** 3 * beta / (1 - beta * phi_v), device="cuda")
+    eye = torch.eye(3, dtype=torch.float64, device="cuda")
+    b = eye[None, :, None, :].expand(K, 3, n, 3).reshape(3 * K, n, 3).contiguous()
+    x0 = (amp[:, None, :, None] * eye[None, :, None, :]).reshape(3 * K, n, 3).contiguous()
+    diag_index = [k for k in range(K) for _ in range(3)]
+    return xi, ng, P, eps_sets, b, x0, diag_index
+
+
+def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed", xi=None, max_rhs_batch=None,
+                        fft_friendly=True, return_moments=False, solver_tol=None):
+    """C (K, 3, 3) (row i = mean dipole for the unit field along i) of one
+    configuration for every contrast scaling, all 3K solves in one batch.
+    ``tol`` sets the spectral parameters (cutoff, grid, support) and, unless
+    ``solver_tol`` is given, the GMRES tolerance too.  Returns (C, converged), or
+    (C, converged, moments (3K, N, 3) on the device) with ``return_moments``."""
+    from .sizes import PolydisperseSystem
+
+    s = np.asarray(scalings, dtype=np.float64).reshape(-1)
+    K = s.size
+    n = cfg.n
+    xi, ng, P, eps_sets, b, x0, diag_index = _configuration_inputs(cfg, s, tol, xi, fft_friendly)
+    sysm = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, cfg.box, xi, tol, Ngrid=ng, P=P, max_rhs=3 * K)
     try:
-        # right-hand side 3k + i: unit field along i with contrast scaling k; guess 4 pi a^3 beta / (1 - beta phi)
-        # along the field (CS/CapacitanceTensorSpectrum.m:45-48), built in a few tensor operations (one
-        # assignment per right-hand side costs more host time than a small configuration's solve)
-        phi_v = 4 * math.pi * float(np.sum(cfg.radii ** 3)) / (3 * float(np.prod(box)))
-        beta = s[:, None] * np.asarray(cfg.beta, dtype=np.float64)[None, :]                  # (K, N)
-        amp = torch.as_tensor(4 * math.pi * cfg.radii[None, :] ** 3 * beta / (1 - beta * phi_v), device="cuda")
-        eye = torch.eye(3, dtype=torch.float64, device="cuda")
-        b = eye[None, :, None, :].expand(K, 3, n, 3).reshape(3 * K, n, 3).contiguous()
-        x0 = (amp[:, None, :, None] * eye[None, :, None, :]).reshape(3 * K, n, 3).contiguous()
-        diag_index = [k for k in range(K) for _ in range(3)]
         sol, info = sysm.solve(b, x0, tol=tol if solver_tol is None else solver_tol, restart=min(3 * n, 30),
                                maxit=100 if precision != "mixed" else 8,
                                precision=precision, diag_index=diag_index)
@@ -141,6 +151,62 @@ def solve_configuration(cfg: Configuration, scalings, tol=1e-4, precision="mixed
     finally:
         sysm.close()
     return (C, conv, sol) if return_moments else (C, conv)
+
+
+def solve_batched(configs: Sequence[Configuration], scalings, tol=1e-4, precision="mixed", xi=None,
+                  fft_friendly=True, solver_tol=None, streams=4, return_moments=False):
+    """The same results as ``solve_configuration`` for every configuration, solved by one native call
+    (``mps_solve_batched``): the library builds, solves and releases the configurations ``streams`` at a
+    time, each on a host thread and CUDA stream of its own, with no Python between them.  All inputs are
+    prepared on the device first (every configuration's positions, radii, permittivity sets, right-hand
+    sides, guesses and solutions are resident at once).  Returns {index: (C, converged)}, with the
+    moments as a third entry when ``return_moments``."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib as L
+    from .sizes import PolydisperseSystem
+    from .system import PRECISIONS
+
+    s = np.asarray(scalings, dtype=np.float64).reshape(-1)
+    K = s.size
+    specs, keep = [], []
+    items = (L.BatchItem * len(configs))()
+    for j, cfg in enumerate(configs):
+        n = cfg.n
+        xi_c, ng, P, eps_sets, b, x0, diag_index = _configuration_inputs(cfg, s, tol, xi, fft_friendly)
+        spec = PolydisperseSystem(cfg.x, cfg.radii, eps_sets, cfg.box, xi_c, tol, Ngrid=ng, P=P, max_rhs=3 * K,
+                                  create=False)
+        x = torch.empty_like(b)
+        dix = (C.c_int32 * (3 * K))(*diag_index)
+        info = (L.SolveInfo * (3 * K))()
+        it = items[j]
+        it.desc = spec.desc
+        it.b, it.x0, it.x = b.data_ptr(), x0.data_ptr(), x.data_ptr()
+        it.nrhs = 3 * K
+        it.diag_index = C.cast(dix, C.POINTER(C.c_int32))
+        it.info = C.cast(info, C.POINTER(L.SolveInfo))
+        specs.append((cfg, spec, x, info))
+        keep += [b, x0, dix]
+    # solve_configuration's options: restart min(3N, 30), the solver's default inner settings
+    restart = min([30] + [3 * c.n for c in configs])
+    opts = L.SolveOpts(tol=float(tol if solver_tol is None else solver_tol), restart=restart,
+                       maxit=100 if precision != "mixed" else 8, precision=PRECISIONS[precision], inner_tol=1e-4,
+                       inner_maxit=4, residual_policy=0, verify=0, residual_precision=PRECISIONS["df"],
+                       inner_operator=1)
+    lib = L.lib()
+    st = lib.mps_solve_batched(items, len(configs), C.byref(opts), int(streams), L.stream_handle())
+    if st != L.MPS_NOT_CONVERGED:
+        L.check(st, "mps_solve_batched")
+    out = {}
+    for j, (cfg, spec, x, info) in enumerate(specs):
+        n = cfg.n
+        Cm = x.reshape(K, 3, n, 3).mean(dim=2).cpu().numpy()
+        conv = items[j].status == L.MPS_OK and all(i.converged for i in info)
+        out[cfg.index] = (Cm, conv, x) if return_moments else (Cm, conv)
+    del keep
+    return out
 
 
 def _solve_concurrently(todo: List[Configuration], solve: Callable, workers: int) -> dict:

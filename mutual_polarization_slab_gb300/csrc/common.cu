@@ -166,6 +166,6 @@ extern "C" const char *mps_status_string(int status) {
     }
 }
 
-extern "C" int mps_abi_version(void) { return 4; }
+extern "C" int mps_abi_version(void) { return 5; }
 
 extern "C" uint64_t mps_kernel_launches(void) { return (uint64_t)mps::g_launches.load(); }

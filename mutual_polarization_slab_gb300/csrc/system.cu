@@ -6,9 +6,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "grid.cuh"
@@ -2673,6 +2675,84 @@ extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, dou
     // the build's table-range check, read after the solve (which the pair fill preceded on the stream)
     const int bs = build_status(sys);
     return bs != MPS_OK ? bs : rc;
+}
+
+// ---------------------------------------------------------------------------
+// Many configurations (the parfor over configurations of CH/CapacitanceTensorSpectrum.m:45 and
+// CS/CapacitanceTensorSpectrum.m:44)
+// ---------------------------------------------------------------------------
+constexpr int kMaxBatchStreams = 32;
+
+// Builds, solves and releases one configuration on stream st.  Everything the system runs is on st or on its
+// own side streams, so waiting for st (and, in free_system, for those) is enough before the release: unlike
+// mps_system_destroy, the other workers' streams keep running.
+static int solve_batch_item(mps_batch_item *it, const mps_solve_opts *o, cudaStream_t st) {
+    mps_system *s = nullptr;
+    int rc = mps_system_create(&it->desc, &s, (mps_stream_t)st);
+    if (rc == MPS_OK)
+        rc = mps_gmres(s, it->b, it->x0, it->x, it->nrhs, it->diag_index, o, it->info, (mps_stream_t)st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && (rc == MPS_OK || rc == MPS_NOT_CONVERGED)) rc = MPS_CUDA_ERR;
+    if (s) free_system(s);
+    return rc;
+}
+
+extern "C" int mps_solve_batched(mps_batch_item *items, int32_t n_items, const mps_solve_opts *opts,
+                                 int32_t n_streams, mps_stream_t stream) {
+    if (n_items < 0 || (n_items > 0 && !items) || !opts || n_streams < 1) return MPS_BAD_ARG;
+    if (n_items == 0) return MPS_OK;
+    int dev = 0;
+    MPS_CUDA_TRY(cudaGetDevice(&dev));
+    // largest configurations first, so the last ones to start are the short ones
+    std::vector<int32_t> order((size_t)n_items);
+    for (int32_t i = 0; i < n_items; ++i) {
+        order[i] = i;
+        items[i].status = MPS_CUDA_ERR;   // until a worker has run it
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return items[a].desc.n * (int64_t)items[a].nrhs > items[b].desc.n * (int64_t)items[b].nrhs;
+    });
+    cudaEvent_t ready = nullptr;
+    MPS_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    if (cudaEventRecord(ready, (cudaStream_t)stream) != cudaSuccess) {
+        cudaEventDestroy(ready);
+        return MPS_CUDA_ERR;
+    }
+    std::atomic<int32_t> next{0};
+    auto work = [&]() {
+        cudaStream_t ws = nullptr;
+        try {
+            if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaStreamWaitEvent(ws, ready, 0) != cudaSuccess) {
+                if (ws) cudaStreamDestroy(ws);
+                return;   // the other workers take this one's share
+            }
+            for (int32_t k = next.fetch_add(1); k < n_items; k = next.fetch_add(1)) {
+                mps_batch_item *it = &items[order[k]];
+                it->status = solve_batch_item(it, opts, ws);
+            }
+        } catch (...) {   // no exception crosses the C ABI; the items not run keep MPS_CUDA_ERR
+        }
+        if (ws) {
+            cudaStreamSynchronize(ws);
+            cudaStreamDestroy(ws);
+        }
+    };
+    const int nw = std::min({(int)n_streams, (int)n_items, kMaxBatchStreams});
+    std::vector<std::thread> threads;
+    try {
+        for (int w = 1; w < nw; ++w) threads.emplace_back(work);
+    } catch (...) {   // fewer threads than asked: the workers started (and this thread) share the items
+    }
+    work();
+    for (auto &t : threads) t.join();
+    cudaEventDestroy(ready);
+    int rc = MPS_OK;
+    for (int32_t i = 0; i < n_items; ++i) {
+        const int si = items[i].status;
+        if (si != MPS_OK && si != MPS_NOT_CONVERGED) return si;
+        if (si == MPS_NOT_CONVERGED) rc = MPS_NOT_CONVERGED;
+    }
+    return rc;
 }
 
 extern "C" int mps_system_profile(mps_system *sys, int32_t enable) {

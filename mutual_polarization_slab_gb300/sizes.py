@@ -92,7 +92,7 @@ class PolydisperseSystem(SpectralEwaldSystem):
     ``eps_p`` may hold several permittivity sets (K, N) for a spectrum batch."""
 
     def __init__(self, x, a, eps_p, box, xi, tol, r_table=None, Ep_perp=None, Ep_para=None, *, rc=None,
-                 Ngrid=None, P=None, max_rhs=3):
+                 Ngrid=None, P=None, max_rhs=3, create=True):
         box = np.asarray(box, dtype=np.float64).reshape(3)
         rc0, ng0, _, P0, _ = spectral_parameters(box, xi, tol)
         rc = rc0 if rc is None else float(rc)
@@ -119,7 +119,7 @@ class PolydisperseSystem(SpectralEwaldSystem):
             rvals = None
         self.radii = a_np
         super().__init__(x, eps_p, box, xi, rc, Ngrid, P, None, None, rvals, slab_factor=0.0,
-                         eta=[eta, eta, eta], max_rhs=max_rhs, radius=a_np, **kw)
+                         eta=[eta, eta, eta], max_rhs=max_rhs, radius=a_np, create=create, **kw)
         self.eta_scalar = eta
         self.tol = float(tol)
 

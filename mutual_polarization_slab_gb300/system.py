@@ -164,11 +164,15 @@ class SpectralEwaldSystem:
     ``radius_class`` (class of each particle among ``n_class`` distinct radii)
     interpolates the couplings like ``CS/RealSpace.m``; without them every pair's
     couplings are evaluated in closed form at its separation.
+
+    ``create=False`` checks the arguments and prepares the device arrays and the
+    C descriptor (``desc``) without building the system: the many-configuration
+    solve (``mps_solve_batched``) builds and releases it itself.
     """
 
     def __init__(self, x, lambdap, box, xi, rc, Ngrid, P, perp, para, rvals, slab_factor=1.0, eta=None,
                  max_rhs=3, quad_tables=None, radius=None, radius_class=None, n_class=0, sizes_tables=None,
-                 inner=None):
+                 inner=None, *, create=True):
         lib = L.lib()
         self._lib = lib
         self._h = C.c_void_p(0)
@@ -267,6 +271,12 @@ class SpectralEwaldSystem:
             d.inner_P = self.inner[1]
         if self.cplx and self.kind != L.MPS_DIPOLE:
             raise ValueError("complex permittivities are supported for the dipole operator")
+        self.desc = d
+        if not create:
+            # the validated descriptor and the device arrays it points to, for mps_solve_batched, which builds
+            # and releases the system itself
+            self.n_pairs, self.ncell = None, None
+            return
         L.check(lib.mps_system_create(C.byref(d), C.byref(self._h), L.stream_handle()), "mps_system_create")
         np_ = C.c_int64(0)
         nc = (C.c_int64 * 3)()

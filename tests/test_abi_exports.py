@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     missing = [name for name in _declared() if not hasattr(lib, name)]
     assert not missing, f"not exported: {missing}"
     assert set(_declared()) == set(_lib.EXPORTS) | set(n for n in _declared() if n in _lib.EXPORTS)
-    assert lib.mps_abi_version() == 4
+    assert lib.mps_abi_version() == 5
     assert lib.mps_status_string(3).decode().startswith("pair separation")
 
 
@@ -58,3 +58,52 @@ def test_neighbor_list_sizes_that_overflow_are_rejected_on_the_host():
         assert st == _lib.MPS_BAD_ARG and npairs.value == 0
     ok = (C.c_int64 * 3)(19, 19, 19)
     assert lib.mps_neighbor_list_workspace(1000, ok) < size_max
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the ABI's structs have the C compiler's sizes and
+    field offsets (compiled from include/mps_gb300.h on this host)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+
+    from mutual_polarization_slab_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"mps_system_desc": _lib.SystemDesc, "mps_solve_opts": _lib.SolveOpts,
+               "mps_solve_info": _lib.SolveInfo, "mps_batch_item": _lib.BatchItem}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mps_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    want = []
+    for cname, py in structs.items():
+        want.append(f"{cname} size {C.sizeof(py)}")
+        want += [f"{cname} {fname} {getattr(py, fname).offset}" for fname, _ in py._fields_]
+    assert [g for g in got if g] == want
+
+
+def test_solve_batched_rejects_bad_arguments_on_the_host():
+    """Argument errors return MPS_BAD_ARG before any CUDA call (no device here),
+    and an empty batch is MPS_OK."""
+    from mutual_polarization_slab_gb300 import _build, _lib
+    if _build.is_stale():
+        pytest.skip("library not built")
+    import ctypes as C
+    lib = _lib.load_library()
+    opts = _lib.SolveOpts(tol=1e-8, restart=30, maxit=10)
+    items = (_lib.BatchItem * 1)()
+    null = C.c_void_p(0)
+    assert lib.mps_solve_batched(items, -1, C.byref(opts), 1, null) == _lib.MPS_BAD_ARG
+    assert lib.mps_solve_batched(items, 1, None, 1, null) == _lib.MPS_BAD_ARG
+    assert lib.mps_solve_batched(items, 1, C.byref(opts), 0, null) == _lib.MPS_BAD_ARG
+    assert lib.mps_solve_batched(None, 1, C.byref(opts), 1, null) == _lib.MPS_BAD_ARG
+    assert lib.mps_solve_batched(items, 0, C.byref(opts), 4, null) == _lib.MPS_OK
