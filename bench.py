@@ -646,6 +646,23 @@ def workload_batch(args):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     units = sum(c.n for c in cfgs) * 3 * len(scal)
+    if args.batch_native:
+        # the same configurations through one native call (mps_solve_batched): inputs prepared on the device,
+        # then the library's worker threads build, solve and release them; compared with the pass above
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        nat = batch.solve_batched(cfgs, scal, tol=args.batch_tol, solver_tol=stol, precision="mixed",
+                                  streams=args.batch_workers)
+        torch.cuda.synchronize()
+        dtn = time.perf_counter() - t1
+        diff = max(float(np.abs(nat[k][0] - res[k][0]).max() / np.abs(res[k][0]).max()) for k in res)
+        return {"workload": f"{len(cfgs)} polydisperse configurations, 3 fields x 16 contrast scalings each, "
+                            f"spectral tol {args.batch_tol}, solver tol {stol}, {args.batch_workers} workers",
+                "python_threads": {"value": units / dt, "seconds": dt,
+                                   "converged": sum(1 for v in res.values() if v[1])},
+                "native": {"value": units / dtn, "seconds": dtn, "converged": sum(1 for v in nat.values() if v[1])},
+                "max_rel_capacitance_difference": diff, "metric": "particle-solves/s",
+                "distinct_grids": len(seen), "plan_warmup_seconds_untimed": plan_s}
     # accuracy on a sample of the configurations: mixed vs a tight float64 solve of the same discretisation
     merr, cerr = [], []
     for c in cfgs[::8]:
@@ -822,6 +839,9 @@ def main():
                     help="batch workload: spectral tolerance (cutoff, grid, support)")
     ap.add_argument("--batch-solver-tol", dest="batch_solver_tol", type=float, default=1e-7,
                     help="batch workload: GMRES tolerance")
+    ap.add_argument("--batch-native", dest="batch_native", action="store_true",
+                    help="batch workload: also time the native many-configuration call (mps_solve_batched) "
+                         "against the Python-thread pass (no float64 accuracy pass)")
     ap.add_argument("--batch-workers", dest="batch_workers", type=int, default=4,
                     help="batch workload: configurations solved at a time (host threads, one CUDA stream each)")
     ap.add_argument("--bd-steps", dest="bd_steps", type=int, default=1000, help="forces workload: BD steps")
