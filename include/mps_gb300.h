@@ -351,7 +351,8 @@ typedef struct mps_batch_item {
  * inputs); the call returns once every solution has been written.  Each item
  * gets its own status.  Returns MPS_OK when all are MPS_OK, otherwise the
  * status of the first item (in array order) that failed with an error, else
- * MPS_NOT_CONVERGED.  n_streams is capped at 32. */
+ * MPS_NOT_CONVERGED.  n_streams is capped at 32.  Bad arguments (invalid
+ * opts included) return MPS_BAD_ARG before any CUDA work. */
 int mps_solve_batched(mps_batch_item *items, int32_t n_items, const mps_solve_opts *opts, int32_t n_streams,
                       mps_stream_t stream);
 

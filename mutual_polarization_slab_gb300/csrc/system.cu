@@ -2634,14 +2634,18 @@ extern "C" int mps_matvec_complex(mps_system *sys, const double *m_ri, double *o
                                   true, st);
 }
 
+// The solver options every solve entry point accepts (host-side check, no CUDA call).
+static bool solve_opts_valid(const mps_solve_opts *o) {
+    if (!o || o->restart < 1 || o->restart >= kMaxCols || o->maxit < 1 || !(o->tol > 0)) return false;
+    if (o->precision != MPS_FP64 && o->precision != MPS_FP32 && o->precision != MPS_DF) return false;
+    if (o->residual_precision != MPS_FP64 && o->residual_precision != MPS_DF) return false;
+    return o->inner_operator == 0 || o->inner_operator == 1;
+}
+
 extern "C" int mps_gmres(mps_system *sys, const double *b, const double *x0, double *x, int32_t nrhs,
                          const int32_t *diag_index, const mps_solve_opts *opts, mps_solve_info *info,
                          mps_stream_t stream) {
-    if (!sys || !b || !x || !opts || nrhs < 1 || nrhs > rhs_limit(sys)) return MPS_BAD_ARG;
-    if (opts->restart < 1 || opts->restart >= kMaxCols || opts->maxit < 1 || !(opts->tol > 0)) return MPS_BAD_ARG;
-    if (opts->precision != MPS_FP64 && opts->precision != MPS_FP32 && opts->precision != MPS_DF) return MPS_BAD_ARG;
-    if (opts->residual_precision != MPS_FP64 && opts->residual_precision != MPS_DF) return MPS_BAD_ARG;
-    if (opts->inner_operator != 0 && opts->inner_operator != 1) return MPS_BAD_ARG;
+    if (!sys || !b || !x || nrhs < 1 || nrhs > rhs_limit(sys) || !solve_opts_valid(opts)) return MPS_BAD_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     MPS_TRY(upload_diag_idx(sys, diag_index, nrhs, st));
     const int64_t n3 = (int64_t)sys->ndof * sys->n;
@@ -2698,7 +2702,7 @@ static int solve_batch_item(mps_batch_item *it, const mps_solve_opts *o, cudaStr
 
 extern "C" int mps_solve_batched(mps_batch_item *items, int32_t n_items, const mps_solve_opts *opts,
                                  int32_t n_streams, mps_stream_t stream) {
-    if (n_items < 0 || (n_items > 0 && !items) || !opts || n_streams < 1) return MPS_BAD_ARG;
+    if (n_items < 0 || (n_items > 0 && !items) || !solve_opts_valid(opts) || n_streams < 1) return MPS_BAD_ARG;
     if (n_items == 0) return MPS_OK;
     int dev = 0;
     MPS_CUDA_TRY(cudaGetDevice(&dev));

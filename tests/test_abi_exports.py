@@ -92,8 +92,8 @@ def test_struct_layouts_match_the_header(tmp_path):
 
 
 def test_solve_batched_rejects_bad_arguments_on_the_host():
-    """Argument errors return MPS_BAD_ARG before any CUDA call (no device here),
-    and an empty batch is MPS_OK."""
+    """Argument errors, invalid solver options included, return MPS_BAD_ARG
+    before any CUDA call (no device here), and an empty batch is MPS_OK."""
     from mutual_polarization_slab_gb300 import _build, _lib
     if _build.is_stale():
         pytest.skip("library not built")
@@ -107,3 +107,9 @@ def test_solve_batched_rejects_bad_arguments_on_the_host():
     assert lib.mps_solve_batched(items, 1, C.byref(opts), 0, null) == _lib.MPS_BAD_ARG
     assert lib.mps_solve_batched(None, 1, C.byref(opts), 1, null) == _lib.MPS_BAD_ARG
     assert lib.mps_solve_batched(items, 0, C.byref(opts), 4, null) == _lib.MPS_OK
+    for bad in (dict(restart=0), dict(maxit=0), dict(tol=0.0), dict(precision=7), dict(residual_precision=1),
+                dict(inner_operator=2)):
+        o = _lib.SolveOpts(tol=1e-8, restart=30, maxit=10)
+        for k, v in bad.items():
+            setattr(o, k, v)
+        assert lib.mps_solve_batched(items, 1, C.byref(o), 1, null) == _lib.MPS_BAD_ARG, bad
