@@ -34,11 +34,12 @@ _REALSPACE_TABLE_CACHE: dict = {}
 
 def default_table(xi):
     """r = 0.001..10 step 0.001 with 0 prepended and its two field/dipole tables,
-    cached per xi (capacitance.py:471-477).  Returns device tensors (perp, para, rvals)."""
-    key = float(xi)
+    cached per xi (capacitance.py:471-477) and per device (a system reads them on
+    its own device).  Returns device tensors (perp, para, rvals) on the current device."""
+    key = (float(xi), torch.cuda.current_device())
     if key not in _REALSPACE_TABLE_CACHE:
         r = np.arange(0.001, 10.0 + 1e-12, 0.001, dtype=np.float64)
-        tabs = ewald.real_space_table(torch.as_tensor(r, device="cuda"), key)
+        tabs = ewald.real_space_table(torch.as_tensor(r, device="cuda"), float(xi))
         rv = torch.cat((torch.zeros(1, dtype=torch.float64, device="cuda"), torch.as_tensor(r, device="cuda")))
         _REALSPACE_TABLE_CACHE[key] = (tabs[2], tabs[3], rv)
     return _REALSPACE_TABLE_CACHE[key]

@@ -354,10 +354,10 @@ def _fingerprint(a):
 
 
 def system_for(x, lambdap, box, Ngrid, P, xi, eta, rc, Hperp, Hpara, rvals, slab_factor, max_rhs=2):
-    """A cached SpectralEwaldSystem for repeated matvecs on one configuration."""
+    """A cached SpectralEwaldSystem for repeated matvecs on one configuration (on the current device)."""
     key = (_fingerprint(x), _fingerprint(lambdap), tuple(_host3(box)), tuple(_host3(Ngrid, np.int64)), int(P),
            float(xi), tuple(_host3(eta)), float(rc), _fingerprint(Hperp), _fingerprint(rvals), float(slab_factor),
-           int(max_rhs))
+           int(max_rhs), torch.cuda.current_device())
     s = _SYS_CACHE.get(key)
     if s is None:
         _SYS_CACHE.clear()

@@ -56,9 +56,9 @@ def real_space_table(r, xi):
 
 
 def default_table(xi, rmin=0.001, dr=0.001, rmax=10.0):
-    """Tables on r = rmin..rmax step dr with 0 prepended, cached per xi.
-    Returns ((9, n+1) tables, (n+1,) separations) as CUDA tensors."""
-    key = (float(xi), float(rmin), float(dr), float(rmax))
+    """Tables on r = rmin..rmax step dr with 0 prepended, cached per xi and device.
+    Returns ((9, n+1) tables, (n+1,) separations) as CUDA tensors on the current device."""
+    key = (float(xi), float(rmin), float(dr), float(rmax), torch.cuda.current_device())
     if key not in _TABLE_CACHE:
         r = np.arange(rmin, rmax + 1e-12, dr, dtype=np.float64)
         tabs = real_space_table(r, float(xi))
