@@ -348,7 +348,8 @@ typedef struct mps_batch_item {
  * solved (mps_gmres with opts) and released, n_streams configurations at a time,
  * each worker on a host thread and CUDA stream of its own, largest (n x nrhs)
  * first.  The work is ordered after what `stream` holds at the call (the
- * inputs); the call returns once every solution has been written.  Each item
+ * inputs); the call returns once every solution has been written (the host
+ * waits, so the call does not belong inside a stream capture).  Each item
  * gets its own status.  Returns MPS_OK when all are MPS_OK, otherwise the
  * status of the first item (in array order) that failed with an error, else
  * MPS_NOT_CONVERGED.  n_streams is capped at 32.  Bad arguments (invalid
