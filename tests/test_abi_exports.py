@@ -113,3 +113,43 @@ def test_solve_batched_rejects_bad_arguments_on_the_host():
         for k, v in bad.items():
             setattr(o, k, v)
         assert lib.mps_solve_batched(items, 1, C.byref(o), 1, null) == _lib.MPS_BAD_ARG, bad
+
+
+def _c_kind(param):
+    """('ptr', 8) / ('float', size) / ('int', size) of one C parameter of the header."""
+    import ctypes as C
+    if "*" in param or "mps_stream_t" in param:
+        return ("ptr", C.sizeof(C.c_void_p))
+    words = param.replace("const", " ").split()
+    t = words[0]
+    if t in ("double", "float"):
+        return ("float", 8 if t == "double" else 4)
+    return ("int", {"int64_t": 8, "uint64_t": 8, "size_t": C.sizeof(C.c_size_t), "int32_t": 4, "int": 4}[t])
+
+
+def _py_kind(t):
+    import ctypes as C
+    if t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
+        return ("ptr", C.sizeof(C.c_void_p))
+    if t in (C.c_double, C.c_float):
+        return ("float", C.sizeof(t))
+    return ("int", C.sizeof(t))
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every prototype of include/mps_gb300.h has a ctypes signature of the same
+    arity, argument kinds and widths, and return type (no library needed)."""
+    import ctypes as C
+
+    from mutual_polarization_slab_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "mps_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    decls = re.findall(r"\b(int|void|size_t|uint64_t|const char \*)\s*(mps_[a-z0-9_]+)\s*\(([^;]*?)\)\s*;", src,
+                       flags=re.S)
+    assert sorted(name for _, name, _ in decls) == sorted(_lib._SIGS)
+    ret = {"int": C.c_int, "void": None, "size_t": C.c_size_t, "uint64_t": C.c_uint64, "const char *": C.c_char_p}
+    for rt, name, args in decls:
+        restype, argtypes = _lib._SIGS[name]
+        assert restype is ret[rt], name
+        params = [] if args.strip() in ("", "void") else [a.strip() for a in args.split(",")]
+        assert [_c_kind(a) for a in params] == [_py_kind(t) for t in argtypes], name
